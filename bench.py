@@ -1,0 +1,376 @@
+"""Benchmark: real-time OPAW-TDDFT RK4 steps on one GB300.
+
+Workload (the Hamiltonian-apply microbenchmark's shapes, run through the full
+propagation step): 96^3 grid at h = 0.4 Bohr, 128 orbitals per set, two sets
+(unperturbed + delta-kicked, gamma = 1e-3 along x), 40 atoms x 8 projectors
+(16^3 boxes), Martyna-Tuckerman Hartree on the 192^3 box, LDA, dt = 0.05 a.u.
+One step = the opaw_tddft loop body: rebuild of both sets, rk4_prop_shs of
+both sets (4 S^-1/2 H S^-1/2 applies + 3 rebuilds each) and the dipole.
+Inputs are seeded synthetic data (no PAW datasets or checkpoints).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is whole-job orbital-steps/s in
+mixed precision with the orbitals resident in HBM; `e2e` is the same metric
+through the C-ABI host-buffer entry point (orbitals copied from pinned host
+memory and back every step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NORB = 128
+GAMMA = 1e-3
+DT = 0.05
+METRIC = "RK4 orbital-steps/s (mixed precision, stage-wise rebuild)"
+UNIT = "orbital-steps/s"
+CPU_SAMPLE_NORB = 2
+
+
+def workload_config(norb):
+    return {
+        "workload": f"OPAW-TDDFT RK4 step, synthetic 96^3 grid h=0.4, {norb} orbitals x 2 sets, 40 atoms x 8 "
+                    "projectors (16^3 boxes), MT Hartree 192^3, LDA, dt=0.05, kick gamma=1e-3 along x",
+        "grid": [96, 96, 96],
+        "orbitals_per_set": norb,
+        "sets": 2,
+        "atoms": 40,
+        "projectors_per_atom": 8,
+        "l2": "inputs larger than L2 (orbitals 3.6 GB resident)",
+    }
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_sample(system, psi_full):
+    """The FP64 oracle on the host cores: one full TDDFT step of the same
+    system with CPU_SAMPLE_NORB orbitals per set."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    o = orc.Oracle(system)
+    psi = np.ascontiguousarray(psi_full[:CPU_SAMPLE_NORB].reshape(CPU_SAMPLE_NORB, -1))
+    pp = o.excite(psi, 1, GAMMA)
+    t = time.perf_counter()
+    o.tddft_steps(psi, pp, 1, DT, GAMMA)
+    dt = time.perf_counter() - t
+    return {
+        "value": 2 * CPU_SAMPLE_NORB / dt,
+        "unit": UNIT,
+        "cores": orc.nthreads(),
+        "kind": "port",
+        "sample": f"one full TDDFT step (rebuild both sets, RK4 both sets, dipole) of the same 96^3 / 40-atom "
+                  f"system with {CPU_SAMPLE_NORB} orbitals per set instead of {NORB}; FP64 C oracle, OpenMP; "
+                  f"{dt:.1f} s",
+        "seconds": dt,
+    }
+
+
+def run_reference(args):
+    """--impl reference: the reference path's CPU implementation (the FP64
+    oracle port: the Fortran reference needs gfortran/MPI/FFTW3/libxc, absent
+    here), all host threads, a bounded sample per step."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as ge
+
+    ge.load_package()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    from opaw_tddft_gb300 import synthetic
+
+    s = synthetic.hamiltonian_microbench(norb=NORB)
+    psi = synthetic.orbitals(s, CPU_SAMPLE_NORB, seed=2025).reshape(CPU_SAMPLE_NORB, -1)
+    o = orc.Oracle(s)
+    pp = o.excite(psi, 1, GAMMA)
+    for _ in range(args.warmup):
+        psi, pp, _d = o.tddft_steps(psi, pp, 1, DT, GAMMA)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        psi, pp, _d = o.tddft_steps(psi, pp, 1, DT, GAMMA)
+    el = time.perf_counter() - t
+    v = 2 * CPU_SAMPLE_NORB * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(NORB),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": orc.nthreads(), "kind": "port",
+                         "sample": f"each step: one full TDDFT step of the 96^3 / 40-atom system with "
+                                   f"{CPU_SAMPLE_NORB} orbitals per set (of {NORB}); FP64 C oracle restating "
+                                   "the reference (the Fortran reference does not build: no gfortran, MPI, "
+                                   "FFTW3 or libxc)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--norb", type=int, default=NORB)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = init_dist(world)
+    import __graft_entry__ as ge
+
+    ge.build()
+    pkg = ge.load_package()
+    from opaw_tddft_gb300 import synthetic
+
+    norb = args.norb
+    s = synthetic.hamiltonian_microbench(norb=norb)
+    psi0 = synthetic.orbitals(s, norb, seed=2025).reshape(norb, -1)
+    ipol = 1 + (rank % 3)  # replicas: independent kick directions
+    ctx = pkg.Context(s)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def fresh():
+        ctx.upload(0, psi0)
+        ctx.excite(ipol, GAMMA)
+
+    # warm-up (also allocates every scratch buffer)
+    fresh()
+    for _ in range(args.warmup):
+        ctx.tddft_steps(1, DT, GAMMA, pkg.PREC_MIXED, want_dipoles=False)
+    fresh()
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = ctx.launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    dd_mixed = []
+    for _ in range(args.steps):
+        dd_mixed.append(ctx.tddft_steps(1, DT, GAMMA, pkg.PREC_MIXED)[0])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    el_ms = e0.elapsed_time(e1)
+    launches = ctx.launches - l0
+    clk = clocks.stop()
+    barrier(dist)
+    el_max = max_over_ranks(dist, el_ms)
+    units = sum_over_ranks(dist, 2.0 * norb * args.steps)
+    value = units / (el_max / 1e3)
+
+    # FP64 path from the same initial state: speed and dipole error of the mixed run
+    ncmp = min(args.steps, 3)
+    fresh()
+    ctx.tddft_steps(1, DT, GAMMA, pkg.PREC_FP64, want_dipoles=False)  # allocates the FP64 buffers
+    fresh()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    f0.record(stream)
+    dd64 = ctx.tddft_steps(ncmp, DT, GAMMA, pkg.PREC_FP64)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = f0.elapsed_time(f1) / ncmp
+    dm = np.array(dd_mixed[:ncmp])[:, ipol - 1]
+    d64 = dd64[:, ipol - 1]
+    dip_err = float(np.abs(dm - d64).max() / max(np.abs(d64).max(), 1e-300))
+
+    # roofline: the batched FFT axis kernel on the complex64 orbital batch
+    peak, peak_kind = load_peaks()
+    batch = torch.empty((norb, s.nn), dtype=torch.complex64, device="cuda")
+    batch.copy_(torch.from_numpy(psi0.astype(np.complex64)).to("cuda"))
+    torch.cuda.synchronize()
+    for _ in range(2):
+        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, -1)
+        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, +1)
+    ctx.sync()
+    reps = 5
+    r0 = torch.cuda.Event(enable_timing=True)
+    r1 = torch.cuda.Event(enable_timing=True)
+    l1 = ctx.launches
+    r0.record(stream)
+    for _ in range(reps):
+        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, -1)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    nl = ctx.launches - l1
+    per_launch_s = r0.elapsed_time(r1) / 1e3 / nl
+    alg_bytes = 2.0 * norb * s.nn * 8  # read + write the complex64 batch once per axis pass
+    achieved = alg_bytes / per_launch_s / 1e9
+    del batch
+
+    e2e = None
+    if not args.no_e2e:
+        nh = min(args.steps, 3)
+        a = torch.empty((norb, s.nn), dtype=torch.complex128, pin_memory=True).numpy()
+        b = torch.empty((norb, s.nn), dtype=torch.complex128, pin_memory=True).numpy()
+        a[:] = psi0
+        ctx.upload(0, psi0)
+        ctx.excite(ipol, GAMMA)
+        b[:] = ctx.download(1, norb).reshape(norb, -1)
+        ctx.tddft_steps_host(a, b, 1, DT, GAMMA, pkg.PREC_MIXED)  # warm
+        barrier(dist)
+        t = time.perf_counter()
+        for _ in range(nh):
+            ctx.tddft_steps_host(a, b, 1, DT, GAMMA, pkg.PREC_MIXED)
+        el = max_over_ranks(dist, time.perf_counter() - t)
+        e2e = {"value": sum_over_ranks(dist, 2.0 * norb * nh) / el, "unit": UNIT,
+               "h2d_bytes_per_step": int(2 * norb * s.nn * 16),
+               "d2h_bytes_per_step": int(2 * norb * s.nn * 16 + 3 * 8),
+               "api": "opaw_tddft_steps_host (psi, psi_pert host arrays in/out each step)", "steps": nh}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_sample(s, psi0)
+        cpu.pop("seconds", None)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "mixed: c64 FFT/v_ks/projectors, f64 RK4 sum/D_ij/dipole",
+            "data": "synthetic (seeded)", "config": workload_config(norb),
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "fp64": {"orbital_steps_per_s": 2.0 * norb / (fp64_ms / 1e3), "ms_per_step": fp64_ms,
+                     "mixed_speedup": (2.0 * norb / (el_max / 1e3 / args.steps)) / (2.0 * norb / (fp64_ms / 1e3)),
+                     "dipole_rel_err_mixed_vs_fp64": dip_err, "compared_steps": ncmp},
+            "roofline": {"kernel": "k_fft_axis<float2> (batched 3D FFT axis pass, 128 x 96^3 complex64)",
+                         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": per_launch_s * 1e3},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,190 @@
+/*
+ * opaw_gb300.h — C ABI of the GB300 (sm_103a) OPAW-TDDFT propagation path.
+ *
+ * The reference (minhchemucla/OPAW-TDDFT) is Fortran 90 over module globals
+ * with no FFI layer.  Each entry point below replaces one reference subroutine
+ * (cited beside it) and is callable from Fortran through ISO_C_BINDING: plain
+ * pointers, sizes and doubles, an int status return, no C++ or torch types.
+ *
+ * Conventions shared with the reference:
+ *   - grids are (nx,ny,nz), x fastest (Fortran column-major), index
+ *     ix + nx*(iy + ny*iz) with 0-based ix,iy,iz;
+ *   - complex data is interleaved (re,im) complex128 (Fortran complex*16) on
+ *     the host; device buffers are complex128 (OPAW_C128) or complex64
+ *     (OPAW_C64);
+ *   - ir_start and local_grid are 1-based, as the reference stores them;
+ *   - per-atom ms x ms matrices (D_ij, rho_ij) are column-major (i fastest);
+ *   - set 0 is the unperturbed orbital set (phi_bar), set 1 the kicked one
+ *     (phi_bar_pert).
+ *
+ * Errors: every function returns OPAW_OK (0) or a nonzero status and never
+ * exits the process (the reference calls `stop`).  opaw_last_error() returns
+ * the message of the last failure on the calling thread.
+ */
+#ifndef OPAW_GB300_H
+#define OPAW_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum opaw_status {
+  OPAW_OK = 0,
+  OPAW_ERR_ARG = 1,       /* bad argument (size, index, null pointer) */
+  OPAW_ERR_CUDA = 2,      /* CUDA runtime failure */
+  OPAW_ERR_STATE = 3,     /* call out of order (e.g. no orbitals uploaded) */
+  OPAW_ERR_BOX = 4,       /* projector box outside a non-periodic grid */
+  OPAW_ERR_NOMEM = 5,     /* device allocation failed */
+  OPAW_ERR_NONFINITE = 6, /* NaN/Inf detected in a checked reduction */
+  OPAW_ERR_NODEV = 7      /* no CUDA device */
+};
+
+/* element type of a device orbital buffer */
+enum opaw_dtype { OPAW_C128 = 0, OPAW_C64 = 1 };
+
+/* arithmetic of a propagation: FP64 everywhere, or FP32 FFT / v_ks /
+ * projector work with FP64 RK4 accumulation, D_ij, S^-1/2 coefficients and
+ * dipole */
+enum opaw_precision { OPAW_PREC_FP64 = 0, OPAW_PREC_MIXED = 1 };
+
+/*
+ * System description: the operator tables the reference builds once in its
+ * set-up (ncpaw_libpaw_prepare.f90, prepare_paw.f90, g3d.f90, vloc.f90) and
+ * keeps in main_mod / atom_mod (4_main.f90:1-51, 3_atom.f90:17-101).
+ * Per-atom arrays are concatenated in atom order.
+ */
+typedef struct opaw_system {
+  int nx, ny, nz;          /* grid (main_mod nx,ny,nz) */
+  double dx, dy, dz;       /* spacing, Bohr */
+  double ekcut;            /* kinetic clamp, Ha (ek.f90:42-44); <=0: none */
+  int scale_vh;            /* Hartree box factor: 2 non-periodic (MT), 1 periodic */
+  int periodic;            /* 0: Martyna-Tuckerman, 1: periodic 4pi/k^2 */
+  double rnel;             /* electron count for the charge renormalisation */
+  int natom;
+  const int *ir_start;     /* [3*natom] 1-based box origin (get_irs.f90:22-26) */
+  const int *nrough;       /* [3*natom] box extents (read_paw.f90:250-253) */
+  const int *ms;           /* [natom] projectors per atom */
+  const double *p3d;       /* raw projectors p~, per atom [ms][nbox], box x fastest */
+  const double *p3d1;      /* orthogonalised projectors p1, same layout */
+  const double *s;         /* [sum ms] spectrum s_i of the p1 overlap (transform_p3d.f90:53-55) */
+  const double *sinv;      /* [sum ms] used by sn_phi for n = -1 */
+  const int *ngrid;        /* [natom] compensation-sphere points (map_localgrid.f90) */
+  const int *local_grid;   /* [3*sum ngrid] 1-based ix,iy,iz per point */
+  const int *nlm;          /* [natom] (2*nl-1)^2 shape-function channels */
+  const double *g3d;       /* per atom [nlm][ngrid], ig fastest (local_g3d) */
+  const double *qijlm;     /* per atom [ms][ms][nlm], lm fastest (qijlm) */
+  const double *vloc;      /* [nn] local ionic potential (vloc_tot) */
+  const double *ncoret;    /* [nn] pseudo core density */
+  const double *dij0;      /* per atom [ms*ms] frozen on-site term D0 */
+  const double *eijkl;     /* per atom [ms^4] on-site Hartree tensor: D_H_ij = sum_kl E[i,j,k,l] rho_kl */
+  double dij_max;          /* |D_ij| clamp (param_dij_max, 0_parameter.f90:17) */
+} opaw_system;
+
+typedef struct opaw_ctx opaw_ctx;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Builds the device copy of every operator table, the kinetic table
+ * (ek.f90:1-51, A15) and the Martyna-Tuckerman kernel (vk_TuMa.f90:2-117,
+ * vk_scale.f90:23-48, A14).  Replaces ncpaw_libpaw_prepare's device-side
+ * outputs.  Checks every projector box (get_irs.f90:30-38). */
+int opaw_dev_init(const opaw_system *sys, opaw_ctx **out);
+int opaw_dev_free(opaw_ctx *ctx);
+const char *opaw_last_error(void);
+/* the cudaStream_t all work of this context is issued on */
+void *opaw_stream(opaw_ctx *ctx);
+/* number of this library's kernels launched since the context was made */
+int64_t opaw_kernel_launches(opaw_ctx *ctx);
+/* waits for all work issued on the context's stream (the *_dev entry points
+ * below are asynchronous on that stream) */
+int opaw_sync(opaw_ctx *ctx);
+
+/* ---- orbital storage (psi stays resident between calls) ------------------ */
+
+/* Copies norb complex128 orbitals (nn each) of `set` host->device.
+ * Replaces the scatter of phi_bar_tot (tddft.f90:246-267). */
+int opaw_psi_upload(opaw_ctx *ctx, int set, const double *psi, int norb);
+int opaw_psi_download(opaw_ctx *ctx, int set, double *psi, int norb);
+/* device pointer of the resident complex128 orbitals of `set` */
+void *opaw_psi_device(opaw_ctx *ctx, int set);
+
+/* ---- operator state (per set) ------------------------------------------- */
+
+int opaw_set_vks(opaw_ctx *ctx, int set, const double *vks);   /* [nn] */
+int opaw_get_vks(opaw_ctx *ctx, int set, double *vks);
+int opaw_set_dij(opaw_ctx *ctx, int set, const double *dij);   /* [sum ms^2] */
+int opaw_get_dij(opaw_ctx *ctx, int set, double *dij);
+int opaw_get_rhoij(opaw_ctx *ctx, int set, double *rhoij);     /* [sum ms^2] */
+int opaw_get_density(opaw_ctx *ctx, int set, double *dens);    /* [nn] dens / dens_pert */
+int opaw_get_nhat(opaw_ctx *ctx, int set, double *nhat);       /* [nn] */
+
+/* ---- per-routine operators over device buffers -------------------------
+ * pin/out are device pointers to norb orbitals of nn points, dtype elements;
+ * `set` selects v_ks / D_ij (unpert or pert twin). */
+
+/* h_phi / h_phi_pert (hphi.f90:1-66, hphi_pert.f90:1-62) */
+int opaw_h_apply_dev(opaw_ctx *ctx, int set, int dtype, const void *pin, void *hp, int norb);
+/* sn_phi (snphi.f90:1-49): n in {-1, -0.5, 0.5, 1}; n == -1 uses sinv */
+int opaw_sn_apply_dev(opaw_ctx *ctx, int dtype, double n, const void *pin, void *sp, int norb);
+/* shs / shs_pert (shs.f90:3-23,50-70) */
+int opaw_shs_apply_dev(opaw_ctx *ctx, int set, int dtype, const void *pin, void *pout, int norb);
+/* proj / proj1 (proj.f90:1-44, proj1.f90:1-46): ca[orb][atom offset + i],
+ * complex128 host output, which = 0 raw p~, 1 orthogonalised p1 */
+int opaw_proj_dev(opaw_ctx *ctx, int which, int dtype, const void *pin, int norb, double *ca);
+
+/* fft3d_forward / fft3d_backward (lib/library_fftw_v3.f90:56-83): in-place
+ * unnormalised 3D DFT of norb device arrays, sign -1 forward, +1 backward */
+int opaw_fft3d_dev(opaw_ctx *ctx, int dtype, void *data, int norb, int sign);
+
+/* ---- host-buffer twins of the operators (Fortran arrays in and out) ---- */
+
+int opaw_h_phi(opaw_ctx *ctx, int set, int dtype, const double *pin, double *hp, int norb);
+int opaw_sn_phi(opaw_ctx *ctx, int dtype, double n, const double *pin, double *sp, int norb);
+int opaw_shs(opaw_ctx *ctx, int set, int dtype, const double *pin, double *pout, int norb);
+
+/* ---- rebuild chain on the resident orbitals ----------------------------- */
+
+/* tddft_rhoij_2 (tddft_rhoij.f90:75-115) on the resident orbitals of `set`
+ * as they are (inside the rebuild the reference calls it on S^-1/2 psi_bar) */
+int opaw_rhoij(opaw_ctx *ctx, int set, int precision);
+/* tddft_dens_2 (tddft_dens.f90:44-85) on the resident orbitals as they are */
+int opaw_density(opaw_ctx *ctx, int set, int precision);
+/* get_nhat / get_nhat_pert with the charge renormalisation (nhat.f90:1-43) */
+int opaw_nhat(opaw_ctx *ctx, int set);
+/* get_pot_tddft_2 (tddft_pot.f90:110-181): v_ks = v_H[n~+n^] + v_xc[n~+n~c] + v_loc */
+int opaw_vks(opaw_ctx *ctx, int set);
+/* get_dij / get_dij_pert (get_dij.f90:1-156) */
+int opaw_dij(opaw_ctx *ctx, int set);
+/* ncpaw_make_hamiltonian_tddft_{unpert,pert} (ncpaw_make_hamiltonian.f90:213-281) */
+int opaw_rebuild(opaw_ctx *ctx, int set, int precision);
+
+/* vh_sub (vh_big.f90:1-75) on host arrays: vh = Hartree potential of dens */
+int opaw_vh(opaw_ctx *ctx, const double *dens, double *vh);
+/* rconv (library_vh_convolution_r8_r2c.f90:13-39) on an arbitrary real grid:
+ * gout = 1/N ifft(bk * fft(gin)), host arrays of n0*n1*n2 */
+int opaw_rconv(int n0, int n1, int n2, const double *gin, const double *bk, double *gout);
+/* LDA v_xc (libxc LDA_X + LDA_C_PW, vxc_libxc.f90:15-23), host arrays */
+int opaw_vxc_lda(opaw_ctx *ctx, const double *dens, double *vxc, int64_t n);
+
+/* ---- kick, propagation, dipole ------------------------------------------ */
+
+/* excite_psi_bar_pert (tddft_excite.f90:1-16): set 1 = set 0 * exp(-i gamma r_ipol) */
+int opaw_excite(opaw_ctx *ctx, int ipol, double gamma);
+/* plot_dip (tddft_plot.f90:1-155): dip, dip_pert (3 each) and d_dip = (dip_pert-dip)/gamma */
+int opaw_dipole(opaw_ctx *ctx, double gamma, double *dip, double *dip_pert, double *d_dip);
+/* nsteps iterations of the opaw_tddft loop body (tddft.f90:67-91):
+ * rebuild both sets, rk4_prop_shs (rk4.f90:1-103), plot_dip.  d_dip_out
+ * receives 3*nsteps values (may be NULL). */
+int opaw_tddft_steps(opaw_ctx *ctx, int nsteps, double dt, double gamma, int precision,
+                     double *d_dip_out);
+/* the same, with psi uploaded from and downloaded to host arrays around the
+ * steps (the propdt boundary with Fortran-resident phi_bar/phi_bar_pert) */
+int opaw_tddft_steps_host(opaw_ctx *ctx, double *psi, double *psi_pert, int norb, int nsteps,
+                          double dt, double gamma, int precision, double *d_dip_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OPAW_GB300_H */

@@ -1,0 +1,202 @@
+// common.cuh — context, error plumbing and precision traits shared by the
+// translation units of libopaw_gb300.so (the sm_103a OPAW-TDDFT path).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/opaw_gb300.h"
+
+namespace opaw {
+
+// ---------------------------------------------------------------- errors --
+void set_error(const std::string &msg);
+const char *get_error();
+
+#define OPAW_CUDA(call)                                                                 \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      ::opaw::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));          \
+      return OPAW_ERR_CUDA;                                                             \
+    }                                                                                   \
+  } while (0)
+
+#define OPAW_CHECK(call)         \
+  do {                           \
+    int s_ = (call);             \
+    if (s_ != OPAW_OK) return s_; \
+  } while (0)
+
+#define OPAW_ARG(cond, msg)                  \
+  do {                                       \
+    if (!(cond)) {                           \
+      ::opaw::set_error(msg);                \
+      return OPAW_ERR_ARG;                   \
+    }                                        \
+  } while (0)
+
+// ------------------------------------------------------- precision traits --
+template <typename R> struct Tr;
+template <> struct Tr<float> {
+  typedef float2 C;
+  static constexpr int dtype = OPAW_C64;
+};
+template <> struct Tr<double> {
+  typedef double2 C;
+  static constexpr int dtype = OPAW_C128;
+};
+
+__host__ __device__ inline float2 cmake(float a, float b) { return make_float2(a, b); }
+__host__ __device__ inline double2 cmake(double a, double b) { return make_double2(a, b); }
+
+template <typename C> __host__ __device__ inline C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __host__ __device__ inline C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __host__ __device__ inline C cmul(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename C, typename R> __host__ __device__ inline C cscale(C a, R s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
+template <typename C> __host__ __device__ inline C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
+
+// ---------------------------------------------------------- FFT planning --
+struct FFTAxis {
+  int n = 0;
+  int nstage = 0;
+  int radix[16];
+  // twiddle table exp(-2 pi i t / n), t in [0, n)
+  double2 *tw64 = nullptr;
+  float2 *tw32 = nullptr;
+};
+
+struct FFT3 {
+  int n[3] = {0, 0, 0};
+  FFTAxis ax[3];
+};
+
+int fft3_init(FFT3 &f, int nx, int ny, int nz);
+void fft3_free(FFT3 &f);
+
+// ------------------------------------------------------------- context --
+struct DeviceBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace opaw
+
+struct opaw_ctx {
+  // scalars of the system
+  int nx, ny, nz;
+  int64_t nn;
+  double dx, dy, dz, dv, ekcut, rnel, dij_max;
+  int scale_vh, periodic;
+  int nxb, nyb, nzb;
+  int64_t nnb;
+  int natom;
+  int ns;   // sum of ms
+  int nd;   // sum of ms^2
+  int msmax;
+
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+
+  // host copies of small tables
+  std::vector<int> h_ms, h_nrough, h_ir0;  // ir0 is 0-based
+  std::vector<int64_t> h_poff, h_soff, h_doff;
+
+  // atom tables (device)
+  int *d_ms = nullptr, *d_nrough = nullptr, *d_ir0 = nullptr;
+  int64_t *d_poff = nullptr, *d_soff = nullptr, *d_doff = nullptr;
+  double *d_p3d = nullptr, *d_p3d1 = nullptr;
+  float *d_p3d_f = nullptr, *d_p3d1_f = nullptr;
+  double *d_s = nullptr, *d_sinv = nullptr;
+  double *d_sigma[4] = {nullptr, nullptr, nullptr, nullptr};  // (1+s)^n - 1 for n = -1(sinv), -1/2, 1/2, 1
+  int *d_slot_atom = nullptr;    // [ns] atom of each projector slot
+  int *d_dslot_atom = nullptr;   // [nd] atom of each ms x ms matrix entry
+  // union of projector boxes: CSR over grid points
+  int nunion = 0, nuent = 0;
+  int *d_upt = nullptr, *d_ustart = nullptr, *d_uatom = nullptr, *d_ubox = nullptr;
+
+  // compensation charge tables
+  int ncomp = 0;             // total sphere points
+  int nlmmax = 0;
+  std::vector<int64_t> h_goff, h_g3off, h_qoff, h_eoff;
+  std::vector<int> h_ngrid, h_nlm;
+  int *d_ngrid = nullptr, *d_nlm = nullptr;
+  int64_t *d_goff = nullptr, *d_g3off = nullptr, *d_qoff = nullptr, *d_eoff = nullptr;
+  int *d_gpt = nullptr;      // linear grid index per sphere point
+  double *d_g3d = nullptr, *d_qijlm = nullptr, *d_dij0 = nullptr, *d_eijkl = nullptr;
+  // union of sphere points: CSR
+  int ncunion = 0;
+  int *d_cpt = nullptr, *d_cstart = nullptr, *d_catom = nullptr, *d_cig = nullptr;
+
+  // kinetic separable tables: k^2 per axis (double, exact copies of the
+  // reference's kx*kx) and float twins
+  double *d_k2[3] = {nullptr, nullptr, nullptr};
+  float *d_k2f[3] = {nullptr, nullptr, nullptr};
+
+  // potentials
+  double *d_vloc = nullptr, *d_ncoret = nullptr;
+  double *d_vk = nullptr;        // MT kernel on the big box, 1/Nb folded in
+  double *d_vks[2] = {nullptr, nullptr};
+  float *d_vks_f[2] = {nullptr, nullptr};
+  double *d_dij[2] = {nullptr, nullptr};
+  double *d_rhoij[2] = {nullptr, nullptr};
+  double *d_dens[2] = {nullptr, nullptr};
+  double *d_nhat[2] = {nullptr, nullptr};
+  double *d_vh[2] = {nullptr, nullptr};
+  double *d_vxc[2] = {nullptr, nullptr};
+
+  // FFT plans
+  opaw::FFT3 fft, fftb;
+
+  // resident orbitals (complex128)
+  double2 *d_psi[2] = {nullptr, nullptr};
+  int norb[2] = {0, 0};
+
+  // scratch (grown on demand)
+  // 0 FFT work, 1 shs intermediate, 2 Hartree source, 3 Hartree 2x box,
+  // 4 rebuild psi~, 5-6 host-twin staging, 7 RK4 k, 8 RK4 y, 9 RK4 ksum
+  opaw::DeviceBuf work[12];
+  opaw::DeviceBuf coef[4];       // [norb][ns] double2
+  opaw::DeviceBuf red;           // reductions
+  double *h_red = nullptr;       // pinned host mirror of small reductions
+};
+
+namespace opaw {
+
+int ensure(DeviceBuf &b, size_t bytes);
+
+inline int grid1(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+// ---------------------------------------------------- operator building blocks --
+// (hamiltonian.cu)
+template <typename R>
+int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, double2 *coef);
+template <typename R>
+int union_scatter(opaw_ctx *c, int which, typename Tr<R>::C *out, int norb, const double2 *coef);
+template <typename R>
+int h_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>::C *hp, int norb);
+template <typename R>
+int sn_apply(opaw_ctx *c, double n, const typename Tr<R>::C *pin, typename Tr<R>::C *sp, int norb);
+template <typename R>
+int shs_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>::C *pout, int norb);
+
+// (fft.cu) batched 3D FFT of `batch` arrays; sign -1 forward, +1 backward
+template <typename R>
+int fft3d(opaw_ctx *c, const FFT3 &f, typename Tr<R>::C *data, int batch, int sign);
+
+// (rebuild.cu)
+int hartree(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1);
+// LDA potential of n points (device arrays)
+int vxc_points(opaw_ctx *c, const double *dens, double *vxc, int64_t n);
+// gout = 1/N ifft(bk fft(a)) on the context's main FFT plan; a is overwritten
+int rconv_device(opaw_ctx *c, double2 *a, const double *bk, double *gout, int n0, int n1, int n2);
+
+}  // namespace opaw

@@ -1,0 +1,307 @@
+// fft.cuh — batched 3D FFT building block: one kernel per axis that stages a
+// tile of lines in shared memory and runs a mixed-radix Stockham autosort
+// transform on it (radices 2, 3, 4, 5, 7, 8).  Element-wise work that belongs
+// next to an FFT (kinetic scaling, v_ks multiply, Hartree kernel, embedding
+// and cropping of the 2x box) is fused into the load / mid / store hooks of
+// an operation functor, so it costs no extra pass over HBM.
+//
+// Conventions follow FFTW as the reference calls it
+// (lib/library_fftw_v3.f90:56-83): unnormalised, forward sign -1, backward +1.
+#pragma once
+
+#include "common.cuh"
+
+namespace opaw {
+
+struct AxisDev {
+  int n;
+  int nstage;
+  int radix[16];
+};
+
+// n0,n1,n2: array extents (x fastest)
+struct Dims3 {
+  int n0, n1, n2;
+};
+
+template <typename C> struct CplxOf;
+template <> struct CplxOf<float2> { typedef float R; };
+template <> struct CplxOf<double2> { typedef double R; };
+
+// multiply by sign*i (sign = -1 forward): (a+ib)*(s*i) = -s*b + i*s*a
+template <typename C> __device__ __forceinline__ C mul_si(C z, int sign) {
+  C r;
+  r.x = -sign * z.y;
+  r.y = sign * z.x;
+  return r;
+}
+
+// twiddle W_n^t for the transform direction (table holds exp(-2 pi i t/n))
+template <typename C> __device__ __forceinline__ C twid(const C *tw, int t, int sign) {
+  C w = tw[t];
+  if (sign > 0) w.y = -w.y;
+  return w;
+}
+
+template <typename C, int R> struct Butterfly;
+
+template <typename C> struct Butterfly<C, 2> {
+  static __device__ __forceinline__ void run(C *u, const C *, int, int) {
+    C a = u[0], b = u[1];
+    u[0] = cadd(a, b);
+    u[1] = csub(a, b);
+  }
+};
+
+template <typename C> struct Butterfly<C, 4> {
+  static __device__ __forceinline__ void run(C *u, const C *, int, int sign) {
+    C a = cadd(u[0], u[2]), b = csub(u[0], u[2]);
+    C c = cadd(u[1], u[3]), d = mul_si(csub(u[1], u[3]), sign);
+    u[0] = cadd(a, c);
+    u[2] = csub(a, c);
+    u[1] = cadd(b, d);
+    u[3] = csub(b, d);
+  }
+};
+
+template <typename C> struct Butterfly<C, 8> {
+  static __device__ __forceinline__ void run(C *u, const C *, int, int sign) {
+    typedef typename CplxOf<C>::R R;
+    const R h = (R)0.70710678118654752440084436210485;  // 1/sqrt(2)
+    C e[4] = {u[0], u[2], u[4], u[6]};
+    C o[4] = {u[1], u[3], u[5], u[7]};
+    Butterfly<C, 4>::run(e, nullptr, 0, sign);
+    Butterfly<C, 4>::run(o, nullptr, 0, sign);
+    // W8^1 = (1 + s i)/sqrt2, W8^2 = s i, W8^3 = (-1 + s i)/sqrt2
+    C o1 = o[1], o3 = o[3];
+    C w1o1, w3o3;
+    w1o1.x = h * (o1.x - sign * o1.y);
+    w1o1.y = h * (o1.y + sign * o1.x);
+    w3o3.x = h * (-o3.x - sign * o3.y);
+    w3o3.y = h * (-o3.y + sign * o3.x);
+    C w2o2 = mul_si(o[2], sign);
+    u[0] = cadd(e[0], o[0]);
+    u[4] = csub(e[0], o[0]);
+    u[1] = cadd(e[1], w1o1);
+    u[5] = csub(e[1], w1o1);
+    u[2] = cadd(e[2], w2o2);
+    u[6] = csub(e[2], w2o2);
+    u[3] = cadd(e[3], w3o3);
+    u[7] = csub(e[3], w3o3);
+  }
+};
+
+// generic odd radix (3, 5, 7) from the twiddle table: y_s = sum_q u_q W_r^{qs}
+template <typename C, int R> struct Butterfly {
+  static __device__ __forceinline__ void run(C *u, const C *tw, int n, int sign) {
+    C y[R];
+    const int step = n / R;
+#pragma unroll
+    for (int s = 0; s < R; s++) {
+      C acc = u[0];
+#pragma unroll
+      for (int q = 1; q < R; q++) acc = cadd(acc, cmul(u[q], twid(tw, ((q * s) % R) * step, sign)));
+      y[s] = acc;
+    }
+#pragma unroll
+    for (int s = 0; s < R; s++) u[s] = y[s];
+  }
+};
+
+// One Stockham stage over all lines of the tile.  Element (l, j) of the tile
+// sits at l*ls + j*js.  linefast selects the thread mapping (lines fastest
+// for strided axes, butterflies fastest for the contiguous axis).
+template <typename C, int R>
+__device__ __forceinline__ void stage(const C *in, C *out, int n, int p, int TL, int ls, int js, bool linefast,
+                                      const C *tw, int sign) {
+  const int m = n / R;
+  const int nb = TL * m;
+  const int tstep = n / (p * R);
+  for (int idx = threadIdx.x; idx < nb; idx += blockDim.x) {
+    int l, i;
+    if (linefast) {
+      l = idx % TL;
+      i = idx / TL;
+    } else {
+      i = idx % m;
+      l = idx / m;
+    }
+    const int k = i % p;
+    C u[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) u[q] = in[l * ls + (i + q * m) * js];
+    if (p > 1) {
+#pragma unroll
+      for (int q = 1; q < R; q++) u[q] = cmul(u[q], twid(tw, q * k * tstep, sign));
+    }
+    Butterfly<C, R>::run(u, tw, n, sign);
+    const int j = (i - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; q++) out[l * ls + (j + q * p) * js] = u[q];
+  }
+}
+
+// full transform of the tile: ping-pong between a and b, returns the buffer
+// holding the result
+template <typename C>
+__device__ C *tile_fft(C *a, C *b, const AxisDev &ax, int TL, int ls, int js, bool linefast, const C *tw, int sign) {
+  int p = 1;
+  for (int s = 0; s < ax.nstage; s++) {
+    const int r = ax.radix[s];
+    switch (r) {
+      case 2: stage<C, 2>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
+      case 3: stage<C, 3>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
+      case 4: stage<C, 4>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
+      case 5: stage<C, 5>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
+      case 7: stage<C, 7>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
+      default: stage<C, 8>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
+    }
+    __syncthreads();
+    C *t = a;
+    a = b;
+    b = t;
+    p *= r;
+  }
+  return a;
+}
+
+// Axis kernel.  AXIS 0: lines along x (contiguous tiles); AXIS 1: lines along
+// y, tiles of TL consecutive x at one z; AXIS 2: lines along z, tiles of TL
+// consecutive (x,y) positions.  Op supplies load/store (by linear element
+// index g and batch b) and, when Op::kMid, a k-space hook between a forward
+// and an inverse transform in the same kernel.
+template <typename C, int AXIS, class Op>
+__global__ void __launch_bounds__(256) k_fft_axis(AxisDev ax, Dims3 d, int TL, int sign, const C *__restrict__ twg, Op op) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *tw = reinterpret_cast<C *>(smem_raw);
+  const int n = ax.n;
+  C *bufa = tw + n;
+  C *bufb = bufa + (size_t)TL * n;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = twg[t];
+
+  const int b = blockIdx.y;
+  const int64_t tile = blockIdx.x;
+  int64_t base;       // linear index of element (l=0, j=0)
+  int64_t lstride;    // linear stride between consecutive lines of the tile
+  int64_t jstride;    // linear stride between consecutive elements of a line
+  int nl;             // valid lines in this tile
+  if (AXIS == 0) {
+    const int64_t nlines = (int64_t)d.n1 * d.n2;
+    const int64_t l0 = tile * TL;
+    nl = (int)min((int64_t)TL, nlines - l0);
+    base = l0 * d.n0;
+    lstride = d.n0;
+    jstride = 1;
+  } else if (AXIS == 1) {
+    const int tpz = (d.n0 + TL - 1) / TL;
+    const int z = (int)(tile / tpz);
+    const int x0 = (int)(tile % tpz) * TL;
+    nl = min(TL, d.n0 - x0);
+    base = x0 + (int64_t)d.n0 * d.n1 * z;
+    lstride = 1;
+    jstride = d.n0;
+  } else {
+    const int64_t nlines = (int64_t)d.n0 * d.n1;
+    const int64_t t0 = tile * TL;
+    nl = (int)min((int64_t)TL, nlines - t0);
+    base = t0;
+    lstride = 1;
+    jstride = (int64_t)d.n0 * d.n1;
+  }
+  const bool linefast = (AXIS != 0);
+  const int ls = linefast ? 1 : n;
+  const int js = linefast ? TL : 1;
+  const int tot = TL * n;
+  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    int l, j;
+    if (linefast) { j = idx / TL; l = idx % TL; } else { l = idx / n; j = idx % n; }
+    C v;
+    if (l < nl) v = op.load(b, base + l * lstride + j * jstride);
+    else { v.x = 0; v.y = 0; }
+    bufa[l * ls + j * js] = v;
+  }
+  __syncthreads();
+  C *res;
+  if (Op::kMid) {
+    res = tile_fft(bufa, bufb, ax, TL, ls, js, linefast, tw, -1);
+    C *other = (res == bufa) ? bufb : bufa;
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+      int l, j;
+      if (linefast) { j = idx / TL; l = idx % TL; } else { l = idx / n; j = idx % n; }
+      if (l < nl) res[l * ls + j * js] = op.mid(b, base + l * lstride + j * jstride, res[l * ls + j * js]);
+    }
+    __syncthreads();
+    res = tile_fft(res, other, ax, TL, ls, js, linefast, tw, +1);
+  } else {
+    res = tile_fft(bufa, bufb, ax, TL, ls, js, linefast, tw, sign);
+  }
+  for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+    int l, j;
+    if (linefast) { j = idx / TL; l = idx % TL; } else { l = idx / n; j = idx % n; }
+    if (l < nl) op.store(b, base + l * lstride + j * jstride, res[l * ls + j * js]);
+  }
+}
+
+// plain load/store between two batched arrays (may alias)
+template <typename C> struct OpCopy {
+  const C *src;
+  C *dst;
+  int64_t bstride;
+  static constexpr bool kMid = false;
+  __device__ C load(int b, int64_t g) const { return src[b * bstride + g]; }
+  __device__ void store(int b, int64_t g, C v) const { dst[b * bstride + g] = v; }
+  __device__ C mid(int, int64_t, C v) const { return v; }
+};
+
+template <typename C> inline int tile_lines(int axis, int n, int nlines_hint) {
+  const int budget = sizeof(C) == 8 ? 4096 : 2048;  // elements per ping-pong buffer
+  int tl = budget / n;
+  if (tl < 1) tl = 1;
+  if (tl > 32) tl = 32;
+  (void)axis;
+  (void)nlines_hint;
+  return tl;
+}
+
+template <typename C> inline const C *axis_tw(const FFTAxis &a);
+template <> inline const float2 *axis_tw<float2>(const FFTAxis &a) { return a.tw32; }
+template <> inline const double2 *axis_tw<double2>(const FFTAxis &a) { return a.tw64; }
+
+inline AxisDev axis_dev(const FFTAxis &a) {
+  AxisDev d;
+  d.n = a.n;
+  d.nstage = a.nstage;
+  for (int i = 0; i < 16; i++) d.radix[i] = a.radix[i];
+  return d;
+}
+
+// launch one axis pass over `batch` arrays of dims d
+template <typename C, int AXIS, class Op>
+int launch_axis(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op) {
+  const int n = a.n;  // n == 1 runs zero stages: the fused operations still apply
+  const int TL = tile_lines<C>(AXIS, n, 0);
+  int64_t tiles;
+  if (AXIS == 0) tiles = ((int64_t)d.n1 * d.n2 + TL - 1) / TL;
+  else if (AXIS == 1) tiles = (int64_t)((d.n0 + TL - 1) / TL) * d.n2;
+  else tiles = ((int64_t)d.n0 * d.n1 + TL - 1) / TL;
+  size_t smem = sizeof(C) * ((size_t)n + 2 * (size_t)TL * n);
+  auto kern = k_fft_axis<C, AXIS, Op>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error(std::string("fft smem attribute: ") + cudaGetErrorString(e));
+      return OPAW_ERR_CUDA;
+    }
+  }
+  dim3 grid((unsigned)tiles, (unsigned)batch);
+  kern<<<grid, 256, smem, c->stream>>>(axis_dev(a), d, TL, sign, axis_tw<C>(a), op);
+  c->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("fft axis launch: ") + cudaGetErrorString(e));
+    return OPAW_ERR_CUDA;
+  }
+  return OPAW_OK;
+}
+
+}  // namespace opaw

@@ -1,0 +1,390 @@
+// hamiltonian.cu — the OPAW operators on batches of orbitals:
+//   gather   <p|psi> over each atom's projector box       (proj.f90, proj1.f90)
+//   scatter  psi += sum_i p_i coef_i over the box union    (hphi.f90:31-64, snphi.f90:29-46)
+//   h_apply  F^-1[ek F psi] + v_ks psi + sum p D <p|psi>   (hphi.f90:1-66)
+//   sn_apply psi + sum p1 ((1+s)^n - 1) <p1|psi>           (snphi.f90:1-49)
+//   shs      S^-1/2 H S^-1/2                               (shs.f90:3-23)
+// Every reduction runs in a fixed order (one CTA per atom and orbital group
+// for the box sums; one thread per grid point, atoms in order, for the
+// scatter), so FP64 results are bit-reproducible run to run.
+#include "fft.cuh"
+
+namespace opaw {
+
+template <typename R> struct ProjTab;
+template <> struct ProjTab<float> {
+  static const float *get(const opaw_ctx *c, int which) { return which ? c->d_p3d1_f : c->d_p3d_f; }
+};
+template <> struct ProjTab<double> {
+  static const double *get(const opaw_ctx *c, int which) { return which ? c->d_p3d1 : c->d_p3d; }
+};
+
+__device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------- gather --
+// out[o*ns + soff[a] + i] = dv * sum_box P_a[i][b] * psi_o[g(b)]   (p real: Gamma point)
+template <typename R, int MSMAX, int OB>
+__global__ void __launch_bounds__(256) k_gather(const typename Tr<R>::C *__restrict__ psi, int64_t nn, int norb,
+                                                const R *__restrict__ P, const int64_t *__restrict__ poff,
+                                                const int *__restrict__ ir0, const int *__restrict__ nrough,
+                                                const int *__restrict__ ms, const int64_t *__restrict__ soff, int nx,
+                                                int ny, int nz, double dv, double2 *__restrict__ out, int ns) {
+  typedef typename Tr<R>::C C;
+  const int a = blockIdx.x;
+  const int o0 = blockIdx.y * OB;
+  const int m = ms[a];
+  const int n0 = nrough[3 * a], n1 = nrough[3 * a + 1], n2 = nrough[3 * a + 2];
+  const int nbox = n0 * n1 * n2;
+  const int x0 = ir0[3 * a], y0 = ir0[3 * a + 1], z0 = ir0[3 * a + 2];
+  const R *Pa = P + poff[a];
+  R ax[OB][MSMAX], ay[OB][MSMAX];
+#pragma unroll
+  for (int o = 0; o < OB; o++)
+#pragma unroll
+    for (int i = 0; i < MSMAX; i++) ax[o][i] = ay[o][i] = 0;
+  for (int b = threadIdx.x; b < nbox; b += blockDim.x) {
+    const int bx = b % n0, by = (b / n0) % n1, bz = b / (n0 * n1);
+    const int64_t g = wrapi(x0 + bx, nx) + (int64_t)nx * (wrapi(y0 + by, ny) + (int64_t)ny * wrapi(z0 + bz, nz));
+    R p[MSMAX];
+#pragma unroll
+    for (int i = 0; i < MSMAX; i++) p[i] = (i < m) ? Pa[(int64_t)i * nbox + b] : (R)0;
+#pragma unroll
+    for (int o = 0; o < OB; o++) {
+      if (o0 + o < norb) {
+        C v = psi[(int64_t)(o0 + o) * nn + g];
+#pragma unroll
+        for (int i = 0; i < MSMAX; i++) {
+          ax[o][i] += p[i] * v.x;
+          ay[o][i] += p[i] * v.y;
+        }
+      }
+    }
+  }
+  __shared__ R red[8][OB][MSMAX][2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 0; o < OB; o++)
+#pragma unroll
+    for (int i = 0; i < MSMAX; i++) {
+      R sx = warp_sum(ax[o][i]), sy = warp_sum(ay[o][i]);
+      if (lane == 0) {
+        red[warp][o][i][0] = sx;
+        red[warp][o][i][1] = sy;
+      }
+    }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  for (int t = threadIdx.x; t < OB * m; t += blockDim.x) {
+    const int o = t / m, i = t % m;
+    if (o0 + o >= norb) continue;
+    R sx = 0, sy = 0;
+    for (int w = 0; w < nw; w++) {
+      sx += red[w][o][i][0];
+      sy += red[w][o][i][1];
+    }
+    out[(int64_t)(o0 + o) * ns + soff[a] + i] = make_double2((double)sx * dv, (double)sy * dv);
+  }
+}
+
+template <typename R>
+int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, double2 *coef) {
+  if (c->natom == 0) return OPAW_OK;
+  const R *P = ProjTab<R>::get(c, which);
+  if (c->msmax <= 8) {
+    constexpr int OB = sizeof(R) == 4 ? 4 : 2;
+    dim3 grid(c->natom, (norb + OB - 1) / OB);
+    k_gather<R, 8, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_ir0, c->d_nrough, c->d_ms,
+                                                    c->d_soff, c->nx, c->ny, c->nz, c->dv, coef, c->ns);
+  } else if (c->msmax <= 16) {
+    dim3 grid(c->natom, norb);
+    k_gather<R, 16, 1><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_ir0, c->d_nrough, c->d_ms,
+                                                    c->d_soff, c->nx, c->ny, c->nz, c->dv, coef, c->ns);
+  } else {
+    set_error("more than 16 projectors per atom");
+    return OPAW_ERR_ARG;
+  }
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// --------------------------------------------------------------- scatter --
+// out_o[upt[u]] += sum over the (atom, box point) entries of u of
+//                  sum_i P_a[i][b] * coef[o][soff[a] + i]
+template <typename R>
+__global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__restrict__ out, int64_t nn, int nunion,
+                                                       const int *__restrict__ upt, const int *__restrict__ ustart,
+                                                       const int *__restrict__ uatom, const int *__restrict__ ubox,
+                                                       const R *__restrict__ P, const int64_t *__restrict__ poff,
+                                                       const int *__restrict__ nrough, const int *__restrict__ ms,
+                                                       const int64_t *__restrict__ soff,
+                                                       const double2 *__restrict__ coef, int ns) {
+  typedef typename Tr<R>::C C;
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  const int o = blockIdx.y;
+  if (u >= nunion) return;
+  const double2 *co = coef + (int64_t)o * ns;
+  R sx = 0, sy = 0;
+  for (int e = ustart[u]; e < ustart[u + 1]; e++) {
+    const int a = uatom[e], b = ubox[e];
+    const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+    const R *Pa = P + poff[a] + b;
+    const double2 *ca = co + soff[a];
+    const int m = ms[a];
+    for (int i = 0; i < m; i++) {
+      const R p = Pa[(int64_t)i * nbox];
+      const double2 cf = ca[i];
+      sx += p * (R)cf.x;
+      sy += p * (R)cf.y;
+    }
+  }
+  C *dst = out + (int64_t)o * nn + upt[u];
+  C v = *dst;
+  v.x += sx;
+  v.y += sy;
+  *dst = v;
+}
+
+template <typename R>
+int union_scatter(opaw_ctx *c, int which, typename Tr<R>::C *out, int norb, const double2 *coef) {
+  if (c->nunion == 0) return OPAW_OK;
+  const R *P = ProjTab<R>::get(c, which);
+  dim3 grid(grid1(c->nunion, 256), norb);
+  k_union_scatter<R><<<grid, 256, 0, c->stream>>>(out, c->nn, c->nunion, c->d_upt, c->d_ustart, c->d_uatom, c->d_ubox,
+                                                  P, c->d_poff, c->d_nrough, c->d_ms, c->d_soff, coef, c->ns);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// ----------------------------------------------------- coefficient algebra --
+// arr[o][a][i] = sum_j D_a(i,j) c[o][a][j]   (hphi.f90:43-47, FP64)
+__global__ void k_coef_dij(const double2 *__restrict__ cin, double2 *__restrict__ cout, int norb, int ns,
+                           const int *__restrict__ slot_atom, const int64_t *__restrict__ soff,
+                           const int64_t *__restrict__ doff, const int *__restrict__ ms,
+                           const double *__restrict__ dij) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int o = blockIdx.y;
+  if (t >= ns || o >= norb) return;
+  const int a = slot_atom[t];
+  const int m = ms[a];
+  const int i = t - (int)soff[a];
+  const double *D = dij + doff[a];
+  const double2 *ci = cin + (int64_t)o * ns + soff[a];
+  double sx = 0, sy = 0;
+  for (int j = 0; j < m; j++) {
+    const double d = D[i + m * j];
+    sx += d * ci[j].x;
+    sy += d * ci[j].y;
+  }
+  cout[(int64_t)o * ns + t] = make_double2(sx, sy);
+}
+
+// coef[o][t] = sigma[t] * c[o][t]   (snphi.f90:24-28)
+__global__ void k_coef_scale(const double2 *__restrict__ cin, double2 *__restrict__ cout, int norb, int ns,
+                             const double *__restrict__ sigma) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int o = blockIdx.y;
+  if (t >= ns || o >= norb) return;
+  const double s = sigma[t];
+  const double2 v = cin[(int64_t)o * ns + t];
+  cout[(int64_t)o * ns + t] = make_double2(s * v.x, s * v.y);
+}
+
+// ------------------------------------------------------------ FFT ops --
+// kinetic hook on z-lines: v *= min((kx^2 + ky^2 + kz^2)/2, ekcut) / N   (ek.f90:40-50)
+template <typename R> struct OpKin;
+template <> struct OpKin<double> {
+  double2 *buf;
+  int64_t bstride;
+  const double *k2x, *k2y, *k2z;
+  int nx, ny;
+  double ekcut, ntot;
+  static constexpr bool kMid = true;
+  __device__ double2 load(int b, int64_t g) const { return buf[b * bstride + g]; }
+  __device__ void store(int b, int64_t g, double2 v) const { buf[b * bstride + g] = v; }
+  __device__ double2 mid(int, int64_t g, double2 v) const {
+    const int x = (int)(g % nx);
+    const int y = (int)((g / nx) % ny);
+    const int z = (int)(g / ((int64_t)nx * ny));
+    double e = __dadd_rn(__dadd_rn(k2x[x], k2y[y]), k2z[z]) * 0.5;
+    if (ekcut > 0.0 && e > ekcut) e = ekcut;
+    e = __ddiv_rn(e, ntot);
+    return make_double2(v.x * e, v.y * e);
+  }
+};
+template <> struct OpKin<float> {
+  float2 *buf;
+  int64_t bstride;
+  const float *k2x, *k2y, *k2z;
+  int nx, ny;
+  float ekcut, invn;
+  static constexpr bool kMid = true;
+  __device__ float2 load(int b, int64_t g) const { return buf[b * bstride + g]; }
+  __device__ void store(int b, int64_t g, float2 v) const { buf[b * bstride + g] = v; }
+  __device__ float2 mid(int, int64_t g, float2 v) const {
+    const int x = (int)(g % nx);
+    const int y = (int)((g / nx) % ny);
+    const int z = (int)(g / ((int64_t)nx * ny));
+    float e = (k2x[x] + k2y[y] + k2z[z]) * 0.5f;
+    if (ekcut > 0.f && e > ekcut) e = ekcut;
+    e *= invn;
+    return make_float2(v.x * e, v.y * e);
+  }
+};
+
+// last inverse pass of h_phi: hp = F^-1[...] + pin * v_ks   (hphi.f90:21)
+template <typename R> struct OpHFinal {
+  typedef typename Tr<R>::C C;
+  const C *src;
+  const C *pin;
+  const R *vks;
+  C *hp;
+  int64_t bstride;
+  static constexpr bool kMid = false;
+  __device__ C load(int b, int64_t g) const { return src[b * bstride + g]; }
+  __device__ void store(int b, int64_t g, C v) const {
+    const C p = pin[b * bstride + g];
+    const R w = vks[g];
+    C r;
+    r.x = v.x + p.x * w;
+    r.y = v.y + p.y * w;
+    hp[b * bstride + g] = r;
+  }
+  __device__ C mid(int, int64_t, C v) const { return v; }
+};
+
+template <typename R> struct VksOf;
+template <> struct VksOf<float> {
+  static const float *get(const opaw_ctx *c, int set) { return c->d_vks_f[set]; }
+};
+template <> struct VksOf<double> {
+  static const double *get(const opaw_ctx *c, int set) { return c->d_vks[set]; }
+};
+
+template <typename R> static OpKin<R> make_kin(opaw_ctx *c, typename Tr<R>::C *buf);
+template <> OpKin<double> make_kin<double>(opaw_ctx *c, double2 *buf) {
+  OpKin<double> k;
+  k.buf = buf;
+  k.bstride = c->nn;
+  k.k2x = c->d_k2[0];
+  k.k2y = c->d_k2[1];
+  k.k2z = c->d_k2[2];
+  k.nx = c->nx;
+  k.ny = c->ny;
+  k.ekcut = c->ekcut;
+  k.ntot = (double)c->nx * (double)c->ny * (double)c->nz;
+  return k;
+}
+template <> OpKin<float> make_kin<float>(opaw_ctx *c, float2 *buf) {
+  OpKin<float> k;
+  k.buf = buf;
+  k.bstride = c->nn;
+  k.k2x = c->d_k2f[0];
+  k.k2y = c->d_k2f[1];
+  k.k2z = c->d_k2f[2];
+  k.nx = c->nx;
+  k.ny = c->ny;
+  k.ekcut = (float)c->ekcut;
+  k.invn = (float)(1.0 / ((double)c->nx * (double)c->ny * (double)c->nz));
+  return k;
+}
+
+template <typename R>
+int h_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>::C *hp, int norb) {
+  typedef typename Tr<R>::C C;
+  if (norb <= 0) return OPAW_OK;
+  const size_t bytes = sizeof(C) * (size_t)c->nn * norb;
+  OPAW_CHECK(ensure(c->work[0], bytes));
+  OPAW_CHECK(ensure(c->coef[0], sizeof(double2) * (size_t)c->ns * norb + 16));
+  OPAW_CHECK(ensure(c->coef[1], sizeof(double2) * (size_t)c->ns * norb + 16));
+  C *w = (C *)c->work[0].p;
+  double2 *c0 = (double2 *)c->coef[0].p, *c1 = (double2 *)c->coef[1].p;
+  // <p~|psi> and D c (addvnl, hphi.f90:40-47), from the unmodified input
+  OPAW_CHECK(gather<R>(c, 0, pin, norb, c0));
+  if (c->ns > 0) {
+    dim3 g(grid1(c->ns, 128), norb);
+    k_coef_dij<<<g, 128, 0, c->stream>>>(c0, c1, norb, c->ns, c->d_slot_atom, c->d_soff, c->d_doff, c->d_ms,
+                                         c->d_dij[set]);
+    c->launches++;
+    OPAW_CUDA(cudaGetLastError());
+  }
+  // kinetic term through the 3D FFT (hphi.f90:14-18) and v_ks psi (:21)
+  Dims3 d{c->nx, c->ny, c->nz};
+  OpCopy<C> x_in{pin, w, c->nn};
+  OpCopy<C> inplace{w, w, c->nn};
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, -1, x_in)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, -1, inplace)));
+  OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, make_kin<R>(c, w))));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, +1, inplace)));
+  OpHFinal<R> fin{w, pin, VksOf<R>::get(c, set), hp, c->nn};
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, +1, fin)));
+  // nonlocal term (hphi.f90:42-60)
+  OPAW_CHECK(union_scatter<R>(c, 0, hp, norb, c1));
+  return OPAW_OK;
+}
+
+// sigma table for sn_phi's exponent n: cached for n = -1, -1/2, 1/2, 1
+static int sigma_table(opaw_ctx *c, double n, const double **out) {
+  int slot;
+  if (n == -1.0) slot = 0;
+  else if (n == -0.5) slot = 1;
+  else if (n == 0.5) slot = 2;
+  else if (n == 1.0) slot = 3;
+  else {
+    set_error("sn_phi exponent must be -1, -0.5, 0.5 or 1");
+    return OPAW_ERR_ARG;
+  }
+  *out = c->d_sigma[slot];
+  return OPAW_OK;
+}
+
+template <typename R>
+int sn_apply(opaw_ctx *c, double n, const typename Tr<R>::C *pin, typename Tr<R>::C *sp, int norb) {
+  typedef typename Tr<R>::C C;
+  if (norb <= 0) return OPAW_OK;
+  const double *sigma;
+  OPAW_CHECK(sigma_table(c, n, &sigma));
+  OPAW_CHECK(ensure(c->coef[2], sizeof(double2) * (size_t)c->ns * norb + 16));
+  OPAW_CHECK(ensure(c->coef[3], sizeof(double2) * (size_t)c->ns * norb + 16));
+  double2 *c0 = (double2 *)c->coef[2].p, *c1 = (double2 *)c->coef[3].p;
+  OPAW_CHECK(gather<R>(c, 1, pin, norb, c0));  // proj1 of the unmodified input (snphi.f90:23)
+  if (c->ns > 0) {
+    dim3 g(grid1(c->ns, 128), norb);
+    k_coef_scale<<<g, 128, 0, c->stream>>>(c0, c1, norb, c->ns, sigma);
+    c->launches++;
+    OPAW_CUDA(cudaGetLastError());
+  }
+  if (sp != pin) OPAW_CUDA(cudaMemcpyAsync(sp, pin, sizeof(C) * (size_t)c->nn * norb, cudaMemcpyDeviceToDevice, c->stream));
+  OPAW_CHECK(union_scatter<R>(c, 1, sp, norb, c1));
+  return OPAW_OK;
+}
+
+template <typename R>
+int shs_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>::C *pout, int norb) {
+  typedef typename Tr<R>::C C;
+  if (norb <= 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->work[1], sizeof(C) * (size_t)c->nn * norb));
+  C *t = (C *)c->work[1].p;
+  OPAW_CHECK(sn_apply<R>(c, -0.5, pin, t, norb));   // shs.f90:19
+  OPAW_CHECK(h_apply<R>(c, set, t, pout, norb));    // :20
+  OPAW_CHECK(sn_apply<R>(c, -0.5, pout, pout, norb)); // :21-22
+  return OPAW_OK;
+}
+
+#define OPAW_INST(R)                                                                                   \
+  template int gather<R>(opaw_ctx *, int, const Tr<R>::C *, int, double2 *);                        \
+  template int union_scatter<R>(opaw_ctx *, int, Tr<R>::C *, int, const double2 *);                 \
+  template int h_apply<R>(opaw_ctx *, int, const Tr<R>::C *, Tr<R>::C *, int);                      \
+  template int sn_apply<R>(opaw_ctx *, double, const Tr<R>::C *, Tr<R>::C *, int);                  \
+  template int shs_apply<R>(opaw_ctx *, int, const Tr<R>::C *, Tr<R>::C *, int);
+OPAW_INST(float)
+OPAW_INST(double)
+
+}  // namespace opaw

@@ -1,0 +1,504 @@
+// propagate.cu — the delta kick (tddft_excite.f90), the dipole (tddft_plot.f90),
+// the RK4 step with stage-wise rebuild (rk4.f90, tddft_prop.f90) and the
+// TDDFT time loop (tddft.f90:67-91), plus the C ABI of the rebuild chain.
+//
+// Precision modes:
+//   OPAW_PREC_FP64  : everything complex128 / double.
+//   OPAW_PREC_MIXED : S^-1/2 H S^-1/2, the S^-1/2 of the rebuild, the density
+//                     and box sums on complex64 orbitals; psi, the RK4
+//                     accumulation p = p + dt/6 sum_k, the norms, rho_ij,
+//                     potentials, D_ij, S^-1/2 coefficients and the dipole in
+//                     double.
+#include <cmath>
+
+#include "fft.cuh"
+
+namespace opaw {
+
+template <typename R> int rebuild_from(opaw_ctx *c, int set, const typename Tr<R>::C *psibar, int norb);
+template <typename R> int rhoij_density_from(opaw_ctx *c, int set, const typename Tr<R>::C *psit, int norb, int what);
+int nhat_step(opaw_ctx *c, int set);
+int vks_step(opaw_ctx *c, int set);
+int dij_step(opaw_ctx *c, int set);
+
+__device__ __forceinline__ double bsum256(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) r += sh[i];
+  return r;
+}
+
+// --------------------------------------------------------------- kick --
+// pp = p * exp(-i gamma r_ipol), r = (i - n/2) d   (tddft_excite.f90:11-12)
+__global__ void k_excite(const double2 *__restrict__ p, double2 *__restrict__ pp, int64_t nn, int norb, int nx,
+                         int ny, int nz, int ipol, double gamma, double dx, double dy, double dz) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= nn) return;
+  const int x = (int)(g % nx), y = (int)((g / nx) % ny), z = (int)(g / ((int64_t)nx * ny));
+  double r;
+  if (ipol == 1) r = (double)(x - nx / 2) * dx;
+  else if (ipol == 2) r = (double)(y - ny / 2) * dy;
+  else r = (double)(z - nz / 2) * dz;
+  double sn, cs;
+  sincos(-gamma * r, &sn, &cs);
+  for (int o = 0; o < norb; o++) {
+    const double2 v = p[(int64_t)o * nn + g];
+    pp[(int64_t)o * nn + g] = make_double2(v.x * cs - v.y * sn, v.x * sn + v.y * cs);
+  }
+}
+
+// ------------------------------------------------------------- dipole --
+// partial sums of dv * r * rho for both sets, rho = 2 sum |psi|^2
+// (tddft_plot.f90:40-55, 116-147)
+constexpr int kDipBlocks = 512;
+__global__ void k_dipole_part(const double2 *__restrict__ p0, const double2 *__restrict__ p1, int norb, int64_t nn,
+                              int nx, int ny, int nz, double dx, double dy, double dz, double dv,
+                              double *__restrict__ part) {
+  __shared__ double sh[8];
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(g % nx), y = (int)((g / nx) % ny), z = (int)(g / ((int64_t)nx * ny));
+    const double r[3] = {(double)(x - nx / 2) * dx, (double)(y - ny / 2) * dy, (double)(z - nz / 2) * dz};
+    double rho0 = 0, rho1 = 0;
+    for (int o = 0; o < norb; o++) {
+      const double2 a = p0[(int64_t)o * nn + g], b = p1[(int64_t)o * nn + g];
+      rho0 += a.x * a.x + a.y * a.y;
+      rho1 += b.x * b.x + b.y * b.y;
+    }
+    rho0 *= 2.0;
+    rho1 *= 2.0;
+    for (int k = 0; k < 3; k++) {
+      acc[k] += dv * r[k] * rho0;
+      acc[3 + k] += dv * r[k] * rho1;
+    }
+  }
+  for (int k = 0; k < 6; k++) {
+    const double s = bsum256(acc[k], sh);
+    if (threadIdx.x == 0) part[6 * blockIdx.x + k] = s;
+  }
+}
+
+// out[0..2] dip, [3..5] dip_pert, [6..8] d_dip = (dip_pert - dip)/gamma
+__global__ void k_dipole_final(const double *__restrict__ part, int nb, double gamma, double *__restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < nb; b++)
+    for (int k = 0; k < 6; k++) s[k] += part[6 * b + k];
+  for (int k = 0; k < 6; k++) out[k] = s[k];
+  for (int k = 0; k < 3; k++) out[6 + k] = (s[3 + k] - s[k]) / gamma;  // tddft_plot.f90:57
+}
+
+// ----------------------------------------------------------- RK4 pieces --
+constexpr int kNormBlocks = 64;
+template <typename C>
+__global__ void k_norm_part(const C *__restrict__ p, int64_t nn, double *__restrict__ part) {
+  __shared__ double sh[8];
+  const int o = blockIdx.y;
+  const C *q = p + (int64_t)o * nn;
+  double acc = 0;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
+    const C z = q[g];
+    const double x = z.x, y = z.y;
+    acc += x * x + y * y;
+  }
+  acc = bsum256(acc, sh);
+  if (threadIdx.x == 0) part[(int64_t)o * gridDim.x + blockIdx.x] = acc;
+}
+
+// nrm[o] = sqrt(dv * sum |p_o|^2)   (rk4.f90:87, :98)
+__global__ void k_norm_final(const double *__restrict__ part, int nb, int norb, double dv, double *__restrict__ nrm) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= norb) return;
+  double s = 0;
+  for (int b = 0; b < nb; b++) s += part[(int64_t)o * nb + b];
+  nrm[o] = sqrt(dv * s);
+}
+
+template <typename C> static int norms(opaw_ctx *c, const C *p, int norb, double *part, double *nrm) {
+  dim3 g(kNormBlocks, norb);
+  k_norm_part<C><<<g, 256, 0, c->stream>>>(p, c->nn, part);
+  k_norm_final<<<grid1(norb, 128), 128, 0, c->stream>>>(part, kNormBlocks, norb, c->dv, nrm);
+  c->launches += 2;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// stage update (rk4.f90:44-48): k = -i * shs(pin); ksum (+)= w k; y = p + dts k
+template <typename CK, typename CY, typename CS>
+__global__ void k_rk4_stage(const CK *__restrict__ kraw, const double2 *__restrict__ p, CS *__restrict__ ksum,
+                            CY *__restrict__ y, int64_t n, double w, int first, double dts, int write_y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const CK kr = kraw[i];
+  const double kx = (double)kr.y, ky = -(double)kr.x;  // -i*(a + ib) = b - ia
+  CS s;
+  if (first) {
+    s.x = w * kx;
+    s.y = w * ky;
+  } else {
+    s = ksum[i];
+    s.x += w * kx;
+    s.y += w * ky;
+  }
+  ksum[i] = s;
+  if (write_y) {
+    const double2 pv = p[i];
+    CY yv;
+    yv.x = pv.x + dts * kx;
+    yv.y = pv.y + dts * ky;
+    y[i] = yv;
+  }
+}
+
+// p = p + dt/6 ksum  (rk4.f90:22)
+template <typename CS>
+__global__ void k_rk4_final(double2 *__restrict__ p, const CS *__restrict__ ksum, int64_t n, double h6) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const CS s = ksum[i];
+  double2 v = p[i];
+  v.x += h6 * (double)s.x;
+  v.y += h6 * (double)s.y;
+  p[i] = v;
+}
+
+// p_o *= nrm0[o] / nrm1[o]  (rk4.f90:99)
+__global__ void k_rescale(double2 *__restrict__ p, int64_t nn, const double *__restrict__ nrm0,
+                          const double *__restrict__ nrm1) {
+  const int o = blockIdx.y;
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= nn) return;
+  const double f = nrm0[o] / nrm1[o];
+  double2 v = p[(int64_t)o * nn + g];
+  v.x *= f;
+  v.y *= f;
+  p[(int64_t)o * nn + g] = v;
+}
+
+__global__ void k_down(const double2 *__restrict__ a, float2 *__restrict__ b, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+static int scratch_red(opaw_ctx *c, double **part, double **nrm0, double **nrm1, double **dip, int norb) {
+  // norm partials, nrm0, nrm1, dipole partials
+  OPAW_CHECK(ensure(c->work[10], sizeof(double) * ((size_t)norb * kNormBlocks + 2 * (size_t)norb + 6 * kDipBlocks + 16)));
+  double *w = (double *)c->work[10].p;
+  *part = w;
+  *nrm0 = w + (size_t)norb * kNormBlocks;
+  *nrm1 = *nrm0 + norb;
+  *dip = *nrm1 + norb;
+  return OPAW_OK;
+}
+
+// one rk4_prop_shs pass over one set (rk4.f90:15-33)
+template <typename R> static int rk4_set(opaw_ctx *c, int set, double dt) {
+  typedef typename Tr<R>::C C;
+  const int norb = c->norb[set];
+  const int64_t tot = c->nn * (int64_t)norb;
+  double2 *p = c->d_psi[set];
+  OPAW_CHECK(ensure(c->work[7], sizeof(C) * tot));
+  OPAW_CHECK(ensure(c->work[8], sizeof(C) * tot));
+  OPAW_CHECK(ensure(c->work[9], sizeof(C) * tot));
+  C *k = (C *)c->work[7].p, *y = (C *)c->work[8].p, *ks = (C *)c->work[9].p;
+  double *part, *nrm0, *nrm1, *dipw;
+  OPAW_CHECK(scratch_red(c, &part, &nrm0, &nrm1, &dipw, norb));
+  OPAW_CHECK(norms<double2>(c, p, norb, part, nrm0));  // norm0 (rk4.f90:16)
+  const C *pin;
+  if (sizeof(R) == 8) {
+    pin = (const C *)p;
+  } else {
+    k_down<<<grid1(tot, 256), 256, 0, c->stream>>>(p, (float2 *)y, tot);
+    c->launches++;
+    pin = y;
+  }
+  const double wts[4] = {1.0, 2.0, 2.0, 1.0};
+  const double dts[4] = {dt / 2.0, dt / 2.0, dt, dt};
+  for (int st = 0; st < 4; st++) {
+    OPAW_CHECK(shs_apply<R>(c, set, pin, k, norb));
+    k_rk4_stage<C, C, C><<<grid1(tot, 256), 256, 0, c->stream>>>(k, p, ks, y, tot, wts[st], st == 0, dts[st], st < 3);
+    c->launches++;
+    OPAW_CUDA(cudaGetLastError());
+    if (st < 3) OPAW_CHECK(rebuild_from<R>(c, set, y, norb));  // rk4.f90:53-55
+    pin = y;
+  }
+  k_rk4_final<C><<<grid1(tot, 256), 256, 0, c->stream>>>(p, ks, tot, dt / 6.0);
+  c->launches++;
+  OPAW_CHECK(norms<double2>(c, p, norb, part, nrm1));  // norm1 (rk4.f90:98)
+  dim3 g(grid1(c->nn, 256), norb);
+  k_rescale<<<g, 256, 0, c->stream>>>(p, c->nn, nrm0, nrm1);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// rebuild from the resident orbitals of `set` in the given precision
+static int rebuild_resident(opaw_ctx *c, int set, int prec) {
+  const int norb = c->norb[set];
+  if (prec == OPAW_PREC_FP64) return rebuild_from<double>(c, set, c->d_psi[set], norb);
+  const int64_t tot = c->nn * (int64_t)norb;
+  OPAW_CHECK(ensure(c->work[8], sizeof(float2) * tot));
+  float2 *y = (float2 *)c->work[8].p;
+  k_down<<<grid1(tot, 256), 256, 0, c->stream>>>(c->d_psi[set], y, tot);
+  c->launches++;
+  return rebuild_from<float>(c, set, y, norb);
+}
+
+static int dipole_dev(opaw_ctx *c, double gamma, double *out_dev) {
+  double *part, *n0, *n1, *dipw;
+  OPAW_CHECK(scratch_red(c, &part, &n0, &n1, &dipw, c->norb[0]));
+  k_dipole_part<<<kDipBlocks, 256, 0, c->stream>>>(c->d_psi[0], c->d_psi[1], c->norb[0], c->nn, c->nx, c->ny, c->nz,
+                                                   c->dx, c->dy, c->dz, c->dv, dipw);
+  k_dipole_final<<<1, 32, 0, c->stream>>>(dipw, kDipBlocks, gamma, out_dev);
+  c->launches += 2;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+static int need_psi(opaw_ctx *c, int set) {
+  if (!c || c->norb[set] == 0) {
+    set_error("no orbitals uploaded for this set");
+    return OPAW_ERR_STATE;
+  }
+  return OPAW_OK;
+}
+
+int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, double *d_dip_out) {
+  OPAW_CHECK(need_psi(c, 0));
+  OPAW_CHECK(need_psi(c, 1));
+  OPAW_ARG(c->norb[0] == c->norb[1], "both sets must hold the same number of orbitals");
+  OPAW_ARG(prec == OPAW_PREC_FP64 || prec == OPAW_PREC_MIXED, "precision must be OPAW_PREC_FP64 or OPAW_PREC_MIXED");
+  OPAW_ARG(nsteps >= 0, "nsteps must be >= 0");
+  OPAW_CHECK(ensure(c->work[11], sizeof(double) * (9 * (size_t)(nsteps > 0 ? nsteps : 1) + 16)));
+  double *dd = (double *)c->work[11].p;  // 9 values per step: dip, dip_pert, d_dip
+  for (int it = 0; it < nsteps; it++) {
+    OPAW_CHECK(rebuild_resident(c, 0, prec));  // ncpaw_make_hamiltonian_tddft (tddft.f90:75)
+    OPAW_CHECK(rebuild_resident(c, 1, prec));
+    if (prec == OPAW_PREC_FP64) {  // propdt -> rk4_prop_shs (tddft.f90:80)
+      OPAW_CHECK(rk4_set<double>(c, 0, dt));
+      OPAW_CHECK(rk4_set<double>(c, 1, dt));
+    } else {
+      OPAW_CHECK(rk4_set<float>(c, 0, dt));
+      OPAW_CHECK(rk4_set<float>(c, 1, dt));
+    }
+    OPAW_CHECK(dipole_dev(c, gamma, dd + 9 * (size_t)it));  // plot_dip (tddft.f90:84)
+  }
+  if (d_dip_out && nsteps > 0) {
+    std::vector<double> h(9 * (size_t)nsteps);
+    OPAW_CUDA(cudaMemcpyAsync(h.data(), dd, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    OPAW_CUDA(cudaStreamSynchronize(c->stream));
+    for (int it = 0; it < nsteps; it++)
+      for (int k = 0; k < 3; k++) d_dip_out[3 * it + k] = h[9 * (size_t)it + 6 + k];
+  }
+  return OPAW_OK;
+}
+
+}  // namespace opaw
+
+using namespace opaw;
+
+extern "C" {
+
+static int check_cs(opaw_ctx *c, int set) {
+  if (!c) {
+    set_error("null context");
+    return OPAW_ERR_ARG;
+  }
+  if (set != 0 && set != 1) {
+    set_error("set must be 0 or 1");
+    return OPAW_ERR_ARG;
+  }
+  return OPAW_OK;
+}
+
+static int finish(opaw_ctx *c) {
+  OPAW_CUDA(cudaGetLastError());
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  return OPAW_OK;
+}
+
+int opaw_rhoij(opaw_ctx *c, int set, int precision) {
+  OPAW_CHECK(check_cs(c, set));
+  OPAW_CHECK(need_psi(c, set));
+  if (precision == OPAW_PREC_FP64) OPAW_CHECK(rhoij_density_from<double>(c, set, c->d_psi[set], c->norb[set], 0));
+  else {
+    const int64_t tot = c->nn * (int64_t)c->norb[set];
+    OPAW_CHECK(ensure(c->work[8], sizeof(float2) * tot));
+    k_down<<<grid1(tot, 256), 256, 0, c->stream>>>(c->d_psi[set], (float2 *)c->work[8].p, tot);
+    c->launches++;
+    OPAW_CHECK(rhoij_density_from<float>(c, set, (float2 *)c->work[8].p, c->norb[set], 0));
+  }
+  return finish(c);
+}
+
+int opaw_density(opaw_ctx *c, int set, int precision) {
+  OPAW_CHECK(check_cs(c, set));
+  OPAW_CHECK(need_psi(c, set));
+  if (precision == OPAW_PREC_FP64) OPAW_CHECK(rhoij_density_from<double>(c, set, c->d_psi[set], c->norb[set], 1));
+  else {
+    const int64_t tot = c->nn * (int64_t)c->norb[set];
+    OPAW_CHECK(ensure(c->work[8], sizeof(float2) * tot));
+    k_down<<<grid1(tot, 256), 256, 0, c->stream>>>(c->d_psi[set], (float2 *)c->work[8].p, tot);
+    c->launches++;
+    OPAW_CHECK(rhoij_density_from<float>(c, set, (float2 *)c->work[8].p, c->norb[set], 1));
+  }
+  return finish(c);
+}
+
+int opaw_nhat(opaw_ctx *c, int set) {
+  OPAW_CHECK(check_cs(c, set));
+  OPAW_CHECK(nhat_step(c, set));
+  return finish(c);
+}
+
+int opaw_vks(opaw_ctx *c, int set) {
+  OPAW_CHECK(check_cs(c, set));
+  OPAW_CHECK(vks_step(c, set));
+  return finish(c);
+}
+
+int opaw_dij(opaw_ctx *c, int set) {
+  OPAW_CHECK(check_cs(c, set));
+  OPAW_CHECK(dij_step(c, set));
+  return finish(c);
+}
+
+int opaw_rebuild(opaw_ctx *c, int set, int precision) {
+  OPAW_CHECK(check_cs(c, set));
+  OPAW_CHECK(need_psi(c, set));
+  OPAW_ARG(precision == OPAW_PREC_FP64 || precision == OPAW_PREC_MIXED, "bad precision");
+  OPAW_CHECK(rebuild_resident(c, set, precision));
+  return finish(c);
+}
+
+int opaw_vh(opaw_ctx *c, const double *dens, double *vh) {
+  if (!c) {
+    set_error("null context");
+    return OPAW_ERR_ARG;
+  }
+  OPAW_ARG(dens && vh, "null buffers");
+  OPAW_CHECK(ensure(c->work[2], sizeof(double) * c->nn * 2));
+  double *a = (double *)c->work[2].p, *b = a + c->nn;
+  OPAW_CUDA(cudaMemcpyAsync(a, dens, sizeof(double) * c->nn, cudaMemcpyHostToDevice, c->stream));
+  OPAW_CHECK(hartree(c, a, nullptr, b, nullptr));
+  OPAW_CUDA(cudaMemcpyAsync(vh, b, sizeof(double) * c->nn, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+int opaw_vxc_lda(opaw_ctx *c, const double *dens, double *vxc, int64_t n) {
+  if (!c) {
+    set_error("null context");
+    return OPAW_ERR_ARG;
+  }
+  OPAW_ARG(dens && vxc && n >= 0, "null buffers");
+  if (n == 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->work[2], sizeof(double) * (size_t)n * 2));
+  double *a = (double *)c->work[2].p, *b = a + n;
+  OPAW_CUDA(cudaMemcpyAsync(a, dens, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  OPAW_CHECK(vxc_points(c, a, b, n));
+  OPAW_CUDA(cudaMemcpyAsync(vxc, b, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+int opaw_rconv(int n0, int n1, int n2, const double *gin, const double *bk, double *gout) {
+  OPAW_ARG(n0 > 0 && n1 > 0 && n2 > 0 && gin && bk && gout, "bad arguments");
+  opaw_ctx *c = new opaw_ctx();
+  int st = OPAW_OK;
+  const int64_t n = (int64_t)n0 * n1 * n2;
+  double2 *a = nullptr;
+  double *kb = nullptr, *o = nullptr;
+  do {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { st = OPAW_ERR_CUDA; break; }
+    if ((st = fft3_init(c->fft, n0, n1, n2)) != OPAW_OK) break;
+    if (cudaMalloc(&a, sizeof(double2) * n) != cudaSuccess || cudaMalloc(&kb, sizeof(double) * n) != cudaSuccess ||
+        cudaMalloc(&o, sizeof(double) * n) != cudaSuccess) {
+      set_error("device allocation failed");
+      st = OPAW_ERR_NOMEM;
+      break;
+    }
+    std::vector<double2> h(n);
+    for (int64_t i = 0; i < n; i++) h[i] = make_double2(gin[i], 0.0);
+    cudaMemcpy(a, h.data(), sizeof(double2) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(kb, bk, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+      set_error("rconv upload failed");
+      st = OPAW_ERR_CUDA;
+      break;
+    }
+    if ((st = rconv_device(c, a, kb, o, n0, n1, n2)) != OPAW_OK) break;
+    if (cudaMemcpyAsync(gout, o, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+      set_error("rconv copy-out failed");
+      st = OPAW_ERR_CUDA;
+    }
+  } while (0);
+  cudaFree(a);
+  cudaFree(kb);
+  cudaFree(o);
+  fft3_free(c->fft);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return st;
+}
+
+int opaw_excite(opaw_ctx *c, int ipol, double gamma) {
+  OPAW_CHECK(check_cs(c, 0));
+  OPAW_CHECK(need_psi(c, 0));
+  OPAW_ARG(ipol >= 1 && ipol <= 3, "ipol must be 1, 2 or 3");
+  const int norb = c->norb[0];
+  if (c->norb[1] != norb) {
+    cudaFree(c->d_psi[1]);
+    c->d_psi[1] = nullptr;
+    OPAW_CUDA(cudaMalloc(&c->d_psi[1], sizeof(double2) * (size_t)c->nn * norb));
+    c->norb[1] = norb;
+  }
+  k_excite<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_psi[0], c->d_psi[1], c->nn, norb, c->nx, c->ny, c->nz, ipol,
+                                                    gamma, c->dx, c->dy, c->dz);
+  c->launches++;
+  return finish(c);
+}
+
+int opaw_dipole(opaw_ctx *c, double gamma, double *dip, double *dip_pert, double *d_dip) {
+  OPAW_CHECK(check_cs(c, 0));
+  OPAW_CHECK(need_psi(c, 0));
+  OPAW_CHECK(need_psi(c, 1));
+  OPAW_ARG(c->norb[0] == c->norb[1], "both sets must hold the same number of orbitals");
+  OPAW_CHECK(ensure(c->work[11], sizeof(double) * 16));
+  double *out = (double *)c->work[11].p;
+  OPAW_CHECK(dipole_dev(c, gamma, out));
+  double h[9];
+  OPAW_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  OPAW_CHECK(finish(c));
+  for (int k = 0; k < 3; k++) {
+    if (dip) dip[k] = h[k];
+    if (dip_pert) dip_pert[k] = h[3 + k];
+    if (d_dip) d_dip[k] = h[6 + k];
+  }
+  return OPAW_OK;
+}
+
+int opaw_tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int precision, double *d_dip_out) {
+  OPAW_CHECK(check_cs(c, 0));
+  OPAW_CHECK(tddft_steps(c, nsteps, dt, gamma, precision, d_dip_out));
+  return finish(c);
+}
+
+int opaw_tddft_steps_host(opaw_ctx *c, double *psi, double *psi_pert, int norb, int nsteps, double dt, double gamma,
+                          int precision, double *d_dip_out) {
+  OPAW_CHECK(check_cs(c, 0));
+  OPAW_ARG(psi && psi_pert && norb > 0, "bad buffers");
+  OPAW_CHECK(opaw_psi_upload(c, 0, psi, norb));
+  OPAW_CHECK(opaw_psi_upload(c, 1, psi_pert, norb));
+  OPAW_CHECK(tddft_steps(c, nsteps, dt, gamma, precision, d_dip_out));
+  OPAW_CHECK(opaw_psi_download(c, 0, psi, norb));
+  OPAW_CHECK(opaw_psi_download(c, 1, psi_pert, norb));
+  return OPAW_OK;
+}
+
+}  // extern "C"

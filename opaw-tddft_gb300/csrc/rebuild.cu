@@ -1,0 +1,549 @@
+// rebuild.cu — the per-stage Hamiltonian rebuild of the TDDFT loop
+// (ncpaw_make_hamiltonian.f90:213-281): psi~ = S^-1/2 psi_bar, rho_ij,
+// density, compensation charge with the charge renormalisation, LDA v_xc,
+// Martyna-Tuckerman Hartree on the 2x box, v_ks and D_ij; plus the one-time
+// Martyna-Tuckerman kernel (vk_TuMa.f90, vk_scale.f90).
+// All of it is FP64 (the small matrices and potentials); only psi~ and the
+// box sums follow the orbital precision.
+#include <cmath>
+
+#include "fft.cuh"
+
+namespace opaw {
+
+int refresh_vks_f(opaw_ctx *c, int set);  // ctx.cu
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  // fixed-order block reduction (blockDim.x == 256)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) r += sh[i];
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+// ------------------------------------------------------ MT kernel (A14) --
+struct BigBox {
+  int nx, ny, nz;
+  double dx, dy, dz;
+};
+
+__global__ void k_vk_real(double2 *cvk, BigBox b, double aa, double r0x, double r0y, double r0z, double dvb) {
+  const int64_t n = (int64_t)b.nx * b.ny * b.nz;
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const int x = (int)(g % b.nx), y = (int)((g / b.nx) % b.ny), z = (int)(g / ((int64_t)b.nx * b.ny));
+  const double rx = r0x + x * b.dx, ry = r0y + y * b.dy, rz = r0z + z * b.dz;
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz));
+  const double fl = (double)1e-26f;  // single-precision literal of vk_TuMa.f90:51
+  const double rp = sqrt(r2 > fl ? r2 : fl);
+  cvk[g] = make_double2(erf(aa * rp) / rp * dvb, 0.0);  // :52
+}
+
+__global__ void k_vk_finish(const double2 *cvk, double *vk, BigBox b, const double *kx, const double *ky,
+                            const double *kz, double aa, double r0x, double r0y, double r0z, int periodic) {
+  const int64_t n = (int64_t)b.nx * b.ny * b.nz;
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const int x = (int)(g % b.nx), y = (int)((g / b.nx) % b.ny), z = (int)(g / ((int64_t)b.nx * b.ny));
+  const double qx = kx[x], qy = ky[y], qz = kz[z];
+  const double k2 = __dadd_rn(__dadd_rn(__dmul_rn(qx, qx), __dmul_rn(qy, qy)), __dmul_rn(qz, qz));
+  const double pi = 3.14159265358979323846;
+  double re = 0, ct;
+  if (!periodic) {
+    const double ph = __dadd_rn(__dadd_rn(__dmul_rn(r0x, qx), __dmul_rn(r0y, qy)), __dmul_rn(r0z, qz));
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    const double2 v = cvk[g];
+    re = v.x * cs - v.y * sn;  // real part of vk_TuMa.f90:77-78 (vk = real(cvk), :109)
+    const double k2s = k2 / (4.0 * aa * aa);
+    if (k2s > 1e-8) ct = 4.0 * pi / k2 * (1.0 - exp(-k2s));                      // :85
+    else ct = 4.0 * pi / (4.0 * aa * aa) * (1.0 - 0.5 * k2s + k2s * k2s / 6.0);  // :88
+  } else {
+    ct = (k2 > 1e-8) ? 4.0 * pi / k2 : 0.0;  // :93-97
+  }
+  vk[g] = __ddiv_rn(__ddiv_rn(__ddiv_rn(re + ct, (double)b.nx), (double)b.ny), (double)b.nz);  // vk_scale.f90:46
+}
+
+static double kcomp(int i, int n, double d) {
+  const double pi = acos(-1.0);
+  double dk = 2.0 * pi / ((double)n * d);
+  double k = (double)i * dk;
+  if (k > pi / d) k = k - 2.0 * pi / d;
+  return k;
+}
+
+int vk_prep(opaw_ctx *c) {
+  const int64_t nb = c->nnb;
+  OPAW_CUDA(cudaMalloc(&c->d_vk, sizeof(double) * nb));
+  OPAW_CHECK(ensure(c->work[0], sizeof(double2) * nb));
+  double2 *cvk = (double2 *)c->work[0].p;
+  BigBox b{c->nxb, c->nyb, c->nzb, c->dx, c->dy, c->dz};
+  double lmin = std::min(std::min(c->nxb * c->dx, c->nyb * c->dy), c->nzb * c->dz);
+  const double aa = 7.0 / lmin;  // vk_TuMa.f90:25
+  const double r0x = -(c->nxb) / 2.0 * c->dx, r0y = -(c->nyb) / 2.0 * c->dy, r0z = -(c->nzb) / 2.0 * c->dz;
+  if (!c->periodic) {
+    k_vk_real<<<grid1(nb, 256), 256, 0, c->stream>>>(cvk, b, aa, r0x, r0y, r0z, c->dx * c->dy * c->dz);
+    c->launches++;
+    OPAW_CUDA(cudaGetLastError());
+    OPAW_CHECK(fft3d<double>(c, c->fftb, cvk, 1, +1));  // fft3d_general(.,1)
+  } else {
+    OPAW_CUDA(cudaMemsetAsync(cvk, 0, sizeof(double2) * nb, c->stream));
+  }
+  std::vector<double> kt[3];
+  const int nd[3] = {c->nxb, c->nyb, c->nzb};
+  const double dd[3] = {c->dx, c->dy, c->dz};
+  double *dk[3];
+  for (int k = 0; k < 3; k++) {
+    kt[k].resize(nd[k]);
+    for (int i = 0; i < nd[k]; i++) kt[k][i] = kcomp(i, nd[k], dd[k]);
+    OPAW_CUDA(cudaMalloc(&dk[k], sizeof(double) * nd[k]));
+    OPAW_CUDA(cudaMemcpy(dk[k], kt[k].data(), sizeof(double) * nd[k], cudaMemcpyHostToDevice));
+  }
+  OPAW_CUDA(cudaDeviceSynchronize());
+  k_vk_finish<<<grid1(nb, 256), 256, 0, c->stream>>>(cvk, c->d_vk, b, dk[0], dk[1], dk[2], aa, r0x, r0y, r0z,
+                                                     c->periodic);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 3; k++) cudaFree(dk[k]);
+  return OPAW_OK;
+}
+
+// -------------------------------------------------- Hartree (A13) --
+// big-box FFT pipeline: embed (x pass) .. times vk (z pass) .. crop (x pass).
+// Two real densities ride in the real and imaginary parts of one complex
+// transform; vk is real and even, so the two results separate exactly.
+struct Embed {
+  int nx, ny, nz, nxb, nyb, mx, my, mz;
+  __device__ bool inner(int64_t g, int64_t &i) const {
+    const int x = (int)(g % nxb), y = (int)((g / nxb) % nyb), z = (int)(g / ((int64_t)nxb * nyb));
+    const int ix = x - mx, iy = y - my, iz = z - mz;
+    if (ix < 0 || ix >= nx || iy < 0 || iy >= ny || iz < 0 || iz >= nz) return false;
+    i = ix + (int64_t)nx * (iy + (int64_t)ny * iz);
+    return true;
+  }
+};
+
+struct OpEmbed {
+  Embed e;
+  const double *d0, *d1;
+  double2 *wb;
+  static constexpr bool kMid = false;
+  __device__ double2 load(int, int64_t g) const {
+    int64_t i;
+    if (!e.inner(g, i)) return make_double2(0.0, 0.0);
+    return make_double2(d0[i], d1 ? d1[i] : 0.0);
+  }
+  __device__ void store(int, int64_t g, double2 v) const { wb[g] = v; }
+  __device__ double2 mid(int, int64_t, double2 v) const { return v; }
+};
+
+struct OpVk {
+  double2 *wb;
+  const double *vk;
+  static constexpr bool kMid = true;
+  __device__ double2 load(int, int64_t g) const { return wb[g]; }
+  __device__ void store(int, int64_t g, double2 v) const { wb[g] = v; }
+  __device__ double2 mid(int, int64_t g, double2 v) const {
+    const double k = vk[g];
+    return make_double2(v.x * k, v.y * k);
+  }
+};
+
+struct OpCrop {
+  Embed e;
+  const double2 *wb;
+  double *v0, *v1;
+  double cn, nbd;
+  static constexpr bool kMid = false;
+  __device__ double2 load(int, int64_t g) const { return wb[g]; }
+  __device__ void store(int, int64_t g, double2 v) const {
+    int64_t i;
+    if (!e.inner(g, i)) return;
+    v0[i] = (v.x * cn) * nbd;  // rconv :29, get_vcon :20
+    if (v1) v1[i] = (v.y * cn) * nbd;
+  }
+  __device__ double2 mid(int, int64_t, double2 v) const { return v; }
+};
+
+int hartree(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1) {
+  OPAW_CHECK(ensure(c->work[3], sizeof(double2) * c->nnb));
+  double2 *wb = (double2 *)c->work[3].p;
+  Embed e{c->nx, c->ny, c->nz, c->nxb, c->nyb, c->nxb / 2 - c->nx / 2, c->nyb / 2 - c->ny / 2, c->nzb / 2 - c->nz / 2};
+  Dims3 d{c->nxb, c->nyb, c->nzb};
+  const double nbd = (double)c->nxb * (double)c->nyb * (double)c->nzb;
+  OpEmbed emb{e, dens0, dens1, wb};
+  OpCopy<double2> inplace{wb, wb, c->nnb};
+  OpVk vkop{wb, c->d_vk};
+  OpCrop crop{e, wb, vh0, vh1, 1.0 / nbd, nbd};
+  OPAW_CHECK((launch_axis<double2, 0>(c, c->fftb.ax[0], d, 1, -1, emb)));
+  OPAW_CHECK((launch_axis<double2, 1>(c, c->fftb.ax[1], d, 1, -1, inplace)));
+  OPAW_CHECK((launch_axis<double2, 2>(c, c->fftb.ax[2], d, 1, 0, vkop)));
+  OPAW_CHECK((launch_axis<double2, 1>(c, c->fftb.ax[1], d, 1, +1, inplace)));
+  OPAW_CHECK((launch_axis<double2, 0>(c, c->fftb.ax[0], d, 1, +1, crop)));
+  return OPAW_OK;
+}
+
+// ------------------------------------------------------ LDA (A17) --
+// Slater exchange + Perdew-Wang 1992 correlation (PRB 45, 13244, unpolarised
+// parameters of Table I); zero below the density threshold.
+__device__ __forceinline__ double vxc_point(double n) {
+  if (!(n > 1e-15)) return 0.0;
+  const double pi = 3.14159265358979323846;
+  const double vx = -cbrt(3.0 * n / pi);
+  const double A = 0.031091, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382, b4 = 0.49294;
+  const double rs = cbrt(3.0 / (4.0 * pi * n));
+  const double srs = sqrt(rs);
+  const double Q = 2.0 * A * (b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs);
+  const double dQ = 2.0 * A * (0.5 * b1 / srs + b2 + 1.5 * b3 * srs + 2.0 * b4 * rs);
+  const double lg = log(1.0 + 1.0 / Q);
+  const double ec = -2.0 * A * (1.0 + a1 * rs) * lg;
+  const double dec = -2.0 * A * a1 * lg + 2.0 * A * (1.0 + a1 * rs) * dQ / (Q * Q + Q);
+  return vx + (ec - rs / 3.0 * dec);
+}
+
+__global__ void k_vxc(const double *__restrict__ dens, const double *__restrict__ core, double *__restrict__ vxc,
+                      int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) vxc[i] = vxc_point(core ? dens[i] + core[i] : dens[i]);
+}
+
+int vxc_points(opaw_ctx *c, const double *dens, double *vxc, int64_t n) {
+  k_vxc<<<grid1(n, 256), 256, 0, c->stream>>>(dens, nullptr, vxc, n);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// rconv on an arbitrary grid (library_vh_convolution_r8_r2c.f90:13-31): the
+// r2c/c2r pair of the reference equals a complex transform of the real input
+// whose inverse is real when bk(k) = bk(-k)
+struct OpBk {
+  double2 *a;
+  const double *bk;
+  static constexpr bool kMid = true;
+  __device__ double2 load(int, int64_t g) const { return a[g]; }
+  __device__ void store(int, int64_t g, double2 v) const { a[g] = v; }
+  __device__ double2 mid(int, int64_t g, double2 v) const {
+    const double k = bk[g];
+    return make_double2(v.x * k, v.y * k);
+  }
+};
+struct OpReal {
+  const double2 *a;
+  double *out;
+  double cn;
+  static constexpr bool kMid = false;
+  __device__ double2 load(int, int64_t g) const { return a[g]; }
+  __device__ void store(int, int64_t g, double2 v) const { out[g] = v.x * cn; }
+  __device__ double2 mid(int, int64_t, double2 v) const { return v; }
+};
+
+int rconv_device(opaw_ctx *c, double2 *a, const double *bk, double *gout, int n0, int n1, int n2) {
+  Dims3 d{n0, n1, n2};
+  OpCopy<double2> inplace{a, a, (int64_t)n0 * n1 * n2};
+  OpBk mid{a, bk};
+  OpReal fin{a, gout, 1.0 / ((double)n0 * (double)n1 * (double)n2)};
+  OPAW_CHECK((launch_axis<double2, 0>(c, c->fft.ax[0], d, 1, -1, inplace)));
+  OPAW_CHECK((launch_axis<double2, 1>(c, c->fft.ax[1], d, 1, -1, inplace)));
+  OPAW_CHECK((launch_axis<double2, 2>(c, c->fft.ax[2], d, 1, 0, mid)));
+  OPAW_CHECK((launch_axis<double2, 1>(c, c->fft.ax[1], d, 1, +1, inplace)));
+  OPAW_CHECK((launch_axis<double2, 0>(c, c->fft.ax[0], d, 1, +1, fin)));
+  return OPAW_OK;
+}
+
+// v_ks = v_H + v_xc + v_loc (tddft_pot.f90:46-47), FP32 twin alongside
+__global__ void k_vks(const double *__restrict__ vh, const double *__restrict__ vxc, const double *__restrict__ vloc,
+                      const double *__restrict__ vhmean, double *__restrict__ vks, float *__restrict__ vksf, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double h = vh[i];
+  if (vhmean) h -= *vhmean;
+  const double v = h + vxc[i] + vloc[i];
+  vks[i] = v;
+  vksf[i] = (float)v;
+}
+
+// ------------------------------------------------ density (A10) --
+template <typename C>
+__global__ void k_density(const C *__restrict__ psi, int norb, int64_t nn, double *__restrict__ dens) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  double acc = 0;
+  for (int o = 0; o < norb; o++) {
+    const C z = psi[(int64_t)o * nn + i];
+    const double x = z.x, y = z.y;
+    acc += x * x + y * y;
+  }
+  dens[i] = 2.0 * acc;  // tddft_dens.f90:73
+}
+
+// ------------------------------------------------- rho_ij (A8) --
+__global__ void k_rhoij(const double2 *__restrict__ coef, int norb, int ns, int nd, const int *__restrict__ dslot,
+                        const int64_t *__restrict__ soff, const int64_t *__restrict__ doff,
+                        const int *__restrict__ ms, double *__restrict__ rho) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nd) return;
+  const int a = dslot[t];
+  const int m = ms[a];
+  const int loc = t - (int)doff[a];
+  const int i = loc % m, j = loc / m;
+  double acc = 0;
+  for (int o = 0; o < norb; o++) {
+    const double2 ci = coef[(int64_t)o * ns + soff[a] + i], cj = coef[(int64_t)o * ns + soff[a] + j];
+    acc += 2.0 * (ci.x * cj.x + ci.y * cj.y);  // Re(conj(c_i) c_j) * 2, tddft_rhoij.f90:35
+  }
+  rho[t] = acc;
+}
+
+// ---------------------------------------------------- nhat (A11) --
+// w[a][lm] = sum_ij rho_a(i,j) Q_a(lm,i,j)
+__global__ void k_nhat_w(const double *__restrict__ rho, const double *__restrict__ q, const int *__restrict__ ms,
+                         const int *__restrict__ nlm, const int64_t *__restrict__ doff,
+                         const int64_t *__restrict__ qoff, int natom, int nlmmax, double *__restrict__ w) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= natom * nlmmax) return;
+  const int a = t / nlmmax, l = t % nlmmax;
+  const int L = nlm[a], m = ms[a];
+  if (l >= L) {
+    w[t] = 0;
+    return;
+  }
+  const double *R = rho + doff[a];
+  const double *Q = q + qoff[a];
+  double acc = 0;
+  for (int j = 0; j < m; j++)
+    for (int i = 0; i < m; i++) acc += R[i + m * j] * Q[l + L * (i + m * j)];
+  w[t] = acc;
+}
+
+__global__ void k_nhat(const int *__restrict__ cpt, const int *__restrict__ cstart, const int *__restrict__ catom,
+                       const int *__restrict__ cig, int ncu, const double *__restrict__ w, int nlmmax,
+                       const int *__restrict__ ngrid, const int *__restrict__ nlm, const int64_t *__restrict__ g3off,
+                       const double *__restrict__ g3d, double *__restrict__ nhat) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= ncu) return;
+  double acc = 0;
+  for (int e = cstart[u]; e < cstart[u + 1]; e++) {
+    const int a = catom[e], ig = cig[e];
+    const int L = nlm[a], ng = ngrid[a];
+    const double *G = g3d + g3off[a];
+    for (int l = 0; l < L; l++) acc += w[a * nlmmax + l] * G[ig + (int64_t)ng * l];
+  }
+  nhat[cpt[u]] = acc;
+}
+
+// fixed-grid partial sums of two arrays (for the renormalisation)
+constexpr int kRedBlocks = 1024;
+__global__ void k_sum2(const double *__restrict__ a, const double *__restrict__ b, int64_t n, double *__restrict__ part) {
+  __shared__ double sh[8];
+  double sa = 0, sb = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    sa += a[i];
+    if (b) sb += b[i];
+  }
+  sa = block_sum(sa, sh);
+  sb = block_sum(sb, sh);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sa;
+    part[2 * blockIdx.x + 1] = sb;
+  }
+}
+
+// factor = rnel / ((sum nhat + sum dens) * dv)  (nhat.f90:32-37); also the mean of a
+__global__ void k_renorm_factor(const double *__restrict__ part, int nb, double dv, double rnel, int64_t n,
+                                double *__restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double sa = 0, sb = 0;
+  for (int i = 0; i < nb; i++) {
+    sa += part[2 * i];
+    sb += part[2 * i + 1];
+  }
+  out[0] = rnel / (sa * dv + sb * dv);
+  out[1] = sa / (double)n;
+}
+
+__global__ void k_scale2(double *__restrict__ a, double *__restrict__ b, int64_t n, const double *__restrict__ f) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double s = *f;
+  a[i] *= s;
+  b[i] *= s;
+}
+
+// --------------------------------------------------- D_ij (A16) --
+// prod[a][lm] = dv sum_g v_ks(r_g) g_lm(r_g)
+__global__ void k_dhat_prod(const double *__restrict__ vks, const int *__restrict__ gpt,
+                            const int64_t *__restrict__ goff, const int *__restrict__ ngrid,
+                            const int *__restrict__ nlm, const int64_t *__restrict__ g3off,
+                            const double *__restrict__ g3d, int nlmmax, double dv, double *__restrict__ prod) {
+  __shared__ double sh[8];
+  const int a = blockIdx.x;
+  const int L = nlm[a], ng = ngrid[a];
+  const double *G = g3d + g3off[a];
+  const int *pts = gpt + goff[a];
+  for (int l = 0; l < nlmmax; l++) {
+    double acc = 0;
+    if (l < L)
+      for (int ig = threadIdx.x; ig < ng; ig += blockDim.x) acc += vks[pts[ig]] * G[ig + (int64_t)ng * l];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) prod[a * nlmmax + l] = acc * dv;
+  }
+}
+
+__global__ void k_dij(const double *__restrict__ prod, int nlmmax, const double *__restrict__ rho,
+                      const double *__restrict__ q, const double *__restrict__ d0, const double *__restrict__ E,
+                      const int *__restrict__ ms, const int *__restrict__ nlm, const int64_t *__restrict__ doff,
+                      const int64_t *__restrict__ qoff, const int64_t *__restrict__ eoff,
+                      const int *__restrict__ dslot, int nd, double dmax, double *__restrict__ dij) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nd) return;
+  const int a = dslot[t];
+  const int m = ms[a], L = nlm[a];
+  const int loc = t - (int)doff[a];
+  const int i = loc % m, j = loc / m;
+  if (i < j) return;  // lower triangle computed, mirrored (get_dij.f90:140-146)
+  const double *R = rho + doff[a];
+  const double *Ea = E + eoff[a];
+  const double *Q = q + qoff[a];
+  double d = d0[doff[a] + i + m * j];
+  for (int l2 = 0; l2 < m; l2++)
+    for (int k = 0; k < m; k++) d += Ea[i + m * (j + m * (k + m * l2))] * R[k + m * l2];
+  for (int l = 0; l < L; l++) d += prod[a * nlmmax + l] * Q[l + L * (i + m * j)];
+  if (dmax > 0 && fabs(d) > dmax) d = d / fabs(d) * dmax;  // get_dij.f90:144
+  dij[doff[a] + i + m * j] = d;
+  dij[doff[a] + j + m * i] = d;
+}
+
+// ------------------------------------------------------ the chain --
+static int rhoij_from_coef(opaw_ctx *c, int set, const double2 *coef, int norb) {
+  if (c->nd == 0) return OPAW_OK;
+  k_rhoij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(coef, norb, c->ns, c->nd, c->d_dslot_atom, c->d_soff, c->d_doff,
+                                                    c->d_ms, c->d_rhoij[set]);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+template <typename R> static int density_of(opaw_ctx *c, int set, const typename Tr<R>::C *psit, int norb) {
+  k_density<typename Tr<R>::C><<<grid1(c->nn, 256), 256, 0, c->stream>>>(psit, norb, c->nn, c->d_dens[set]);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+static double *red_scratch(opaw_ctx *c) { return (double *)c->red.p; }
+
+int nhat_step(opaw_ctx *c, int set) {
+  OPAW_CHECK(ensure(c->red, sizeof(double) * (2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1) * 2)));
+  double *part = red_scratch(c);
+  double *fac = part + 2 * kRedBlocks;
+  double *w = fac + 64;
+  OPAW_CUDA(cudaMemsetAsync(c->d_nhat[set], 0, sizeof(double) * c->nn, c->stream));
+  if (c->natom > 0 && c->nlmmax > 0) {
+    const int nt = c->natom * c->nlmmax;
+    k_nhat_w<<<grid1(nt, 128), 128, 0, c->stream>>>(c->d_rhoij[set], c->d_qijlm, c->d_ms, c->d_nlm, c->d_doff,
+                                                     c->d_qoff, c->natom, c->nlmmax, w);
+    c->launches++;
+    if (c->ncunion > 0) {
+      k_nhat<<<grid1(c->ncunion, 256), 256, 0, c->stream>>>(c->d_cpt, c->d_cstart, c->d_catom, c->d_cig, c->ncunion,
+                                                            w, c->nlmmax, c->d_ngrid, c->d_nlm, c->d_g3off, c->d_g3d,
+                                                            c->d_nhat[set]);
+      c->launches++;
+    }
+  }
+  k_sum2<<<kRedBlocks, 256, 0, c->stream>>>(c->d_nhat[set], c->d_dens[set], c->nn, part);
+  k_renorm_factor<<<1, 32, 0, c->stream>>>(part, kRedBlocks, c->dv, c->rnel, c->nn, fac);
+  k_scale2<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_nhat[set], c->d_dens[set], c->nn, fac);
+  c->launches += 3;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+__global__ void k_add(const double *a, const double *b, double *o, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) o[i] = a[i] + b[i];
+}
+
+int vks_step(opaw_ctx *c, int set) {
+  OPAW_CHECK(ensure(c->work[2], sizeof(double) * c->nn * 2));
+  double *t = (double *)c->work[2].p;  // n~ + n^ for the Hartree solve
+  k_vxc<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_dens[set], c->d_ncoret, c->d_vxc[set], c->nn);
+  c->launches++;
+  OPAW_CHECK(ensure(c->red, sizeof(double) * (2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1) * 2)));
+  // t = dens + nhat (tddft_pot.f90:39)
+  k_add<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_dens[set], c->d_nhat[set], t, c->nn);
+  c->launches++;
+  OPAW_CHECK(hartree(c, t, nullptr, c->d_vh[set], nullptr));
+  const double *mean = nullptr;
+  if (c->periodic) {
+    double *part = red_scratch(c);
+    double *fac = part + 2 * kRedBlocks;
+    k_sum2<<<kRedBlocks, 256, 0, c->stream>>>(c->d_vh[set], nullptr, c->nn, part);
+    k_renorm_factor<<<1, 32, 0, c->stream>>>(part, kRedBlocks, c->dv, 1.0, c->nn, fac);
+    c->launches += 2;
+    mean = fac + 1;
+  }
+  k_vks<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_vh[set], c->d_vxc[set], c->d_vloc, mean, c->d_vks[set],
+                                                  c->d_vks_f[set], c->nn);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+int dij_step(opaw_ctx *c, int set) {
+  if (c->natom == 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->red, sizeof(double) * (2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1) * 2)));
+  double *prod = red_scratch(c) + 2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1);
+  const int L = c->nlmmax > 0 ? c->nlmmax : 1;
+  k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(c->d_vks[set], c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off,
+                                                c->d_g3d, L, c->dv, prod);
+  k_dij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(prod, L, c->d_rhoij[set], c->d_qijlm, c->d_dij0, c->d_eijkl,
+                                                  c->d_ms, c->d_nlm, c->d_doff, c->d_qoff, c->d_eoff,
+                                                  c->d_dslot_atom, c->nd, c->dij_max, c->d_dij[set]);
+  c->launches += 2;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// rebuild from orbitals psi_bar (device, dtype) of `set`: psi~ = S^-1/2 psi_bar,
+// then rho_ij, density, nhat, v_ks, D_ij
+template <typename R> int rebuild_from(opaw_ctx *c, int set, const typename Tr<R>::C *psibar, int norb) {
+  typedef typename Tr<R>::C C;
+  OPAW_CHECK(ensure(c->work[4], sizeof(C) * (size_t)c->nn * norb));
+  C *pt = (C *)c->work[4].p;
+  OPAW_CHECK(sn_apply<R>(c, -0.5, psibar, pt, norb));  // ncpaw_make_hamiltonian.f90:119-122
+  OPAW_CHECK(ensure(c->coef[0], sizeof(double2) * (size_t)c->ns * norb + 16));
+  double2 *co = (double2 *)c->coef[0].p;
+  OPAW_CHECK(gather<R>(c, 0, pt, norb, co));
+  OPAW_CHECK(rhoij_from_coef(c, set, co, norb));  // :125
+  OPAW_CHECK(density_of<R>(c, set, pt, norb));    // :126
+  OPAW_CHECK(nhat_step(c, set));                  // :127
+  OPAW_CHECK(vks_step(c, set));                   // :128
+  OPAW_CHECK(dij_step(c, set));                   // :129
+  return OPAW_OK;
+}
+template int rebuild_from<float>(opaw_ctx *, int, const float2 *, int);
+template int rebuild_from<double>(opaw_ctx *, int, const double2 *, int);
+
+template <typename R> int rhoij_density_from(opaw_ctx *c, int set, const typename Tr<R>::C *psit, int norb, int what) {
+  OPAW_CHECK(ensure(c->coef[0], sizeof(double2) * (size_t)c->ns * norb + 16));
+  double2 *co = (double2 *)c->coef[0].p;
+  if (what == 0) {
+    OPAW_CHECK(gather<R>(c, 0, psit, norb, co));
+    OPAW_CHECK(rhoij_from_coef(c, set, co, norb));
+  } else {
+    OPAW_CHECK(density_of<R>(c, set, psit, norb));
+  }
+  return OPAW_OK;
+}
+template int rhoij_density_from<float>(opaw_ctx *, int, const float2 *, int, int);
+template int rhoij_density_from<double>(opaw_ctx *, int, const double2 *, int, int);
+
+}  // namespace opaw

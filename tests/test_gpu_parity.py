@@ -1,0 +1,187 @@
+"""GPU parity: every operator of the propagation path through the C ABI,
+against the FP64 oracle on the same seeded inputs.
+
+Tolerances (relative to the largest magnitude of the reference output):
+  FP64 (complex128) operators ........ 1e-12   (rounding-order differences only)
+  FP32 (complex64) operators ......... 2e-6    (single-precision FFT/projector work)
+  FP64 rebuild chain / potentials .... 1e-11
+  FP64 RK4 steps ..................... 1e-10
+  mixed-precision RK4 steps .......... 1e-5
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as orc
+import opaw_tddft_gb300 as pkg
+from opaw_tddft_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL64, TOL32 = 1e-12, 2e-6
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
+
+
+def make(kind, norb=3, seed=5):
+    s = synthetic.small_system(kind, norb=norb)
+    psi = synthetic.orbitals(s, norb, seed=seed).reshape(norb, -1)
+    o = orc.Oracle(s)
+    c = pkg.Context(s)
+    for st, (v, d) in enumerate([(s.vks0, s.dij_init), (s.vks0 * 0.9, s.dij_init * 1.1)]):
+        o.set_vks(st, v)
+        o.set_dij(st, d)
+        c.set_vks(st, v)
+        c.set_dij(st, d)
+    return s, psi, o, c
+
+
+@pytest.fixture(scope="module", params=["tiny", "odd", "edge"])
+def case(request):
+    s, psi, o, c = make(request.param)
+    yield s, psi, o, c
+    c.close()
+
+
+def test_rconv_golden_on_device():
+    """library_rconv_drv.f90:5-95 through opaw_rconv."""
+    f = np.load(os.path.join(GOLDEN, "rconv_8x6x3.npz"))
+    got = pkg.rconv(f["gin"], f["bk"])
+    assert np.abs(got - f["gana"]).sum() < 1e-11 * np.abs(f["gana"]).sum()
+
+
+@pytest.mark.parametrize("set_", [0, 1])
+def test_h_phi(case, set_):
+    s, psi, o, c = case
+    ref = o.h_phi(psi, set_)
+    assert rel(c.h_phi(psi, set_, pkg.OPAW_C128), ref) < TOL64
+    assert rel(c.h_phi(psi, set_, pkg.OPAW_C64), ref) < TOL32
+
+
+@pytest.mark.parametrize("n", [-1.0, -0.5, 0.5, 1.0])
+def test_sn_phi(case, n):
+    s, psi, o, c = case
+    ref = o.sn_phi(psi, n)
+    assert rel(c.sn_phi(psi, n, pkg.OPAW_C128), ref) < TOL64
+    assert rel(c.sn_phi(psi, n, pkg.OPAW_C64), ref) < TOL32
+
+
+@pytest.mark.parametrize("set_", [0, 1])
+def test_shs(case, set_):
+    s, psi, o, c = case
+    ref = o.shs(psi, set_)
+    assert rel(c.shs(psi, set_, pkg.OPAW_C128), ref) < TOL64
+    assert rel(c.shs(psi, set_, pkg.OPAW_C64), ref) < TOL32
+
+
+def test_proj_device_pointers(case):
+    """proj / proj1 on a device buffer (opaw_proj_dev) holding the resident orbitals."""
+    s, psi, o, c = case
+    c.upload(0, psi)
+    ptr = c.psi_device(0)
+    for which in (0, 1):
+        assert rel(c.proj_dev(which, pkg.OPAW_C128, ptr, psi.shape[0]), o.proj(psi, which)) < TOL64
+
+
+def test_h_apply_dev_async_matches_host_twin(case):
+    torch = pytest.importorskip("torch")
+    s, psi, o, c = case
+    dev = torch.from_numpy(psi.copy()).to("cuda")
+    out = torch.empty_like(dev)
+    torch.cuda.synchronize()
+    c.h_apply_dev(0, pkg.OPAW_C128, dev.data_ptr(), out.data_ptr(), psi.shape[0])
+    c.sync()
+    assert rel(out.cpu().numpy(), o.h_phi(psi, 0)) < TOL64
+
+
+def test_rebuild_chain_step_by_step(case):
+    s, psi, o, c = case
+    c.upload(0, psi)
+    # tddft_rhoij_2 / tddft_dens_2 on the orbitals as they are
+    assert rel(c.rhoij(0), o.rhoij(psi, 0)) < 1e-12
+    assert rel(c.density(0), o.density(psi, 0)) < 1e-13
+    c.nhat(0)
+    o.nhat(0)
+    assert rel(c.get_nhat(0), o.get_nhat(0)) < 1e-12
+    assert rel(c.get_density(0), o.get_density(0)) < 1e-12
+    c.vks(0)
+    o.vks(0)
+    assert rel(c.get_vks(0), o.get_vks(0)) < 1e-11
+    c.dij(0)
+    o.dij(0)
+    assert rel(c.get_dij(0), o.get_dij(0)) < 1e-11
+
+
+@pytest.mark.parametrize("prec,tol", [(pkg.PREC_FP64, 1e-11), (pkg.PREC_MIXED, 1e-5)])
+def test_full_rebuild(case, prec, tol):
+    s, psi, o, c = case
+    c.upload(1, psi)
+    c.rebuild(1, prec)
+    o.rebuild(psi, 1)
+    for got, ref in [(c.get_rhoij(1), o.get_rhoij(1)), (c.get_density(1), o.get_density(1)),
+                     (c.get_nhat(1), o.get_nhat(1)), (c.get_vks(1), o.get_vks(1)), (c.get_dij(1), o.get_dij(1))]:
+        assert rel(got, ref) < tol
+
+
+def test_vh_and_vxc(case):
+    s, psi, o, c = case
+    rng = np.random.default_rng(3)
+    dens = np.abs(rng.standard_normal(s.nn)) * 0.1
+    assert rel(c.vh(dens), o.vh(dens)) < 1e-12
+    assert rel(c.vxc_lda(dens), orc.vxc(dens)) < 1e-13
+
+
+def test_kick_and_dipole(case):
+    s, psi, o, c = case
+    c.upload(0, psi)
+    c.excite(1, 1e-3)
+    pp = o.excite(psi, 1, 1e-3)
+    assert rel(c.download(1, psi.shape[0]).reshape(pp.shape), pp) < 1e-15
+    d0, d1, dd = c.dipole(1e-3)
+    r0, r1, rd = o.dipole(psi, pp, 1e-3)
+    assert np.allclose(d0, r0, rtol=1e-12, atol=1e-13) and np.allclose(d1, r1, rtol=1e-12, atol=1e-13)
+    assert np.allclose(dd, rd, rtol=1e-8, atol=1e-9)
+
+
+@pytest.mark.parametrize("kind", ["tiny", "edge"])
+def test_tddft_steps_fp64_and_mixed(kind):
+    s, psi, o, c = make(kind, norb=3)
+    g = 1e-3
+    pp = o.excite(psi, 1, g)
+    p2, pp2, dref = o.tddft_steps(psi, pp, 2, 0.05, g)
+    c.upload(0, psi)
+    c.excite(1, g)
+    d64 = c.tddft_steps(2, 0.05, g, pkg.PREC_FP64)
+    assert rel(c.download(0, 3).reshape(p2.shape), p2) < 1e-10
+    assert rel(c.download(1, 3).reshape(pp2.shape), pp2) < 1e-10
+    assert np.allclose(d64, dref, rtol=1e-7, atol=1e-8)
+    c.upload(0, psi)
+    c.excite(1, g)
+    c.tddft_steps(2, 0.05, g, pkg.PREC_MIXED)
+    assert rel(c.download(0, 3).reshape(p2.shape), p2) < 1e-5
+    # host-buffer boundary (propdt with Fortran-resident arrays)
+    a = psi.copy()
+    b = o.excite(psi, 1, g).copy()
+    dh = c.tddft_steps_host(a, b, 2, 0.05, g, pkg.PREC_FP64)
+    assert rel(a, p2) < 1e-10 and rel(b, pp2) < 1e-10
+    assert np.allclose(dh, dref, rtol=1e-7, atol=1e-8)
+    c.close()
+
+
+def test_fp64_is_deterministic():
+    s, psi, o, c = make("tiny")
+    a = c.shs(psi, 0, pkg.OPAW_C128)
+    b = c.shs(psi, 0, pkg.OPAW_C128)
+    assert np.array_equal(a, b)
+    c.close()
+
+
+def test_launch_counter_counts_kernels():
+    s, psi, o, c = make("tiny")
+    n0 = c.launches
+    c.h_phi(psi, 0)
+    assert c.launches > n0
+    c.close()
