@@ -175,6 +175,58 @@ def cpu_sample(system, psi_full):
     }
 
 
+def fp64_compare(ctx, pkg, torch, stream, fresh, ncmp, dd_mixed, ipol, norb, mixed_ms):
+    """FP64 steps from the same initial state: their speed, and the error of
+    the mixed-precision dipole signal against them."""
+    fresh()
+    ctx.tddft_steps(1, DT, GAMMA, pkg.PREC_FP64, want_dipoles=False)  # allocates the FP64 buffers
+    fresh()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    f0.record(stream)
+    dd64 = ctx.tddft_steps(ncmp, DT, GAMMA, pkg.PREC_FP64)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = f0.elapsed_time(f1) / ncmp
+    dm = np.array(dd_mixed[:ncmp])[:, ipol - 1]
+    d64 = dd64[:, ipol - 1]
+    err = float(np.abs(dm - d64).max() / max(np.abs(d64).max(), 1e-300))
+    return {"orbital_steps_per_s": 2.0 * norb / (fp64_ms / 1e3), "ms_per_step": fp64_ms,
+            "mixed_speedup": fp64_ms / mixed_ms, "dipole_rel_err_mixed_vs_fp64": err, "compared_steps": ncmp}
+
+
+def roofline(ctx, pkg, torch, stream, s, psi0, norb):
+    """The batched FFT axis kernel on the complex64 orbital batch, timed
+    alone with CUDA events on the library's stream."""
+    peak, peak_kind = load_peaks()
+    batch = torch.empty((norb, s.nn), dtype=torch.complex64, device="cuda")
+    batch.copy_(torch.from_numpy(psi0.astype(np.complex64)).to("cuda"))
+    torch.cuda.synchronize()
+    for _ in range(2):
+        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, -1)
+        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, +1)
+    ctx.sync()
+    reps = 5
+    r0 = torch.cuda.Event(enable_timing=True)
+    r1 = torch.cuda.Event(enable_timing=True)
+    l1 = ctx.launches
+    r0.record(stream)
+    for _ in range(reps):
+        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, -1)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    nl = ctx.launches - l1
+    per_launch_s = r0.elapsed_time(r1) / 1e3 / nl
+    alg_bytes = 2.0 * norb * s.nn * 8  # read + write the complex64 batch once per axis pass
+    achieved = alg_bytes / per_launch_s / 1e9
+    del batch
+    return {"kernel": f"k_fft_axis<float2> (batched 3D FFT axis pass, {norb} x 96^3 complex64)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": peak_kind, "traffic": None, "alg_bytes_per_launch": alg_bytes,
+            "avg_launch_ms": per_launch_s * 1e3}
+
+
 def run_reference(args):
     """--impl reference: the reference path's CPU implementation (the FP64
     oracle port: the Fortran reference needs gfortran/MPI/FFTW3/libxc, absent
@@ -225,6 +277,8 @@ def main():
     ap.add_argument("--norb", type=int, default=NORB)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--no-roofline", action="store_true", help="skip the standalone FFT timing")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -282,44 +336,12 @@ def main():
 
     # FP64 path from the same initial state: speed and dipole error of the mixed run
     ncmp = min(args.steps, 3)
-    fresh()
-    ctx.tddft_steps(1, DT, GAMMA, pkg.PREC_FP64, want_dipoles=False)  # allocates the FP64 buffers
-    fresh()
-    f0 = torch.cuda.Event(enable_timing=True)
-    f1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    f0.record(stream)
-    dd64 = ctx.tddft_steps(ncmp, DT, GAMMA, pkg.PREC_FP64)
-    f1.record(stream)
-    torch.cuda.synchronize()
-    fp64_ms = f0.elapsed_time(f1) / ncmp
-    dm = np.array(dd_mixed[:ncmp])[:, ipol - 1]
-    d64 = dd64[:, ipol - 1]
-    dip_err = float(np.abs(dm - d64).max() / max(np.abs(d64).max(), 1e-300))
-
-    # roofline: the batched FFT axis kernel on the complex64 orbital batch
-    peak, peak_kind = load_peaks()
-    batch = torch.empty((norb, s.nn), dtype=torch.complex64, device="cuda")
-    batch.copy_(torch.from_numpy(psi0.astype(np.complex64)).to("cuda"))
-    torch.cuda.synchronize()
-    for _ in range(2):
-        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, -1)
-        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, +1)
-    ctx.sync()
-    reps = 5
-    r0 = torch.cuda.Event(enable_timing=True)
-    r1 = torch.cuda.Event(enable_timing=True)
-    l1 = ctx.launches
-    r0.record(stream)
-    for _ in range(reps):
-        ctx.fft3d_dev(pkg.OPAW_C64, batch.data_ptr(), norb, -1)
-    r1.record(stream)
-    torch.cuda.synchronize()
-    nl = ctx.launches - l1
-    per_launch_s = r0.elapsed_time(r1) / 1e3 / nl
-    alg_bytes = 2.0 * norb * s.nn * 8  # read + write the complex64 batch once per axis pass
-    achieved = alg_bytes / per_launch_s / 1e9
-    del batch
+    fp64 = None
+    if not args.skip_fp64:
+        fp64 = fp64_compare(ctx, pkg, torch, stream, fresh, ncmp, dd_mixed, ipol, norb, el_max / args.steps)
+    roof = None
+    if not args.no_roofline:
+        roof = roofline(ctx, pkg, torch, stream, s, psi0, norb)
 
     e2e = None
     if not args.no_e2e:
@@ -353,13 +375,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "mixed: c64 FFT/v_ks/projectors, f64 RK4 sum/D_ij/dipole",
             "data": "synthetic (seeded)", "config": workload_config(norb),
             "parallelism": "replicas" if world > 1 else "single GPU",
-            "fp64": {"orbital_steps_per_s": 2.0 * norb / (fp64_ms / 1e3), "ms_per_step": fp64_ms,
-                     "mixed_speedup": (2.0 * norb / (el_max / 1e3 / args.steps)) / (2.0 * norb / (fp64_ms / 1e3)),
-                     "dipole_rel_err_mixed_vs_fp64": dip_err, "compared_steps": ncmp},
-            "roofline": {"kernel": "k_fft_axis<float2> (batched 3D FFT axis pass, 128 x 96^3 complex64)",
-                         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                         "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": per_launch_s * 1e3},
+            "fp64": fp64,
+            "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,

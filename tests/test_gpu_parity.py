@@ -3,7 +3,9 @@ against the FP64 oracle on the same seeded inputs.
 
 Tolerances (relative to the largest magnitude of the reference output):
   FP64 (complex128) operators ........ 1e-12   (rounding-order differences only)
-  FP32 (complex64) operators ......... 2e-6    (single-precision FFT/projector work)
+  FP32 (complex64) operators ......... 1e-5    (single-precision FFT/projector work; the FFT's
+                                                rounding grows with log N and the kinetic and
+                                                potential terms partially cancel)
   FP64 rebuild chain / potentials .... 1e-11
   FP64 RK4 steps ..................... 1e-10
   mixed-precision RK4 steps .......... 1e-5
@@ -19,7 +21,7 @@ from opaw_tddft_gb300 import synthetic
 
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-TOL64, TOL32 = 1e-12, 2e-6
+TOL64, TOL32 = 1e-12, 1e-5
 
 
 def rel(a, b):
