@@ -144,6 +144,7 @@ struct opaw_ctx {
   // potentials
   double *d_vloc = nullptr, *d_ncoret = nullptr;
   double *d_vk = nullptr;        // MT kernel on the big box, 1/Nb folded in
+  float *d_vk_f = nullptr;       // its FP32 copy for the mixed-precision Hartree solve
   double *d_vks[2] = {nullptr, nullptr};
   float *d_vks_f[2] = {nullptr, nullptr};
   double *d_dij[2] = {nullptr, nullptr};

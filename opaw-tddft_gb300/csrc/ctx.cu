@@ -268,7 +268,7 @@ static void destroy(opaw_ctx *c) {
                   c->d_p3d_f, c->d_p3d1_f, c->d_s, c->d_sinv, c->d_slot_atom, c->d_dslot_atom, c->d_upt,
                   c->d_ustart, c->d_uatom, c->d_ubox, c->d_ngrid, c->d_nlm, c->d_goff, c->d_g3off, c->d_qoff,
                   c->d_eoff, c->d_gpt, c->d_g3d, c->d_qijlm, c->d_dij0, c->d_eijkl, c->d_cpt, c->d_cstart,
-                  c->d_catom, c->d_cig, c->d_vloc, c->d_ncoret, c->d_vk};
+                  c->d_catom, c->d_cig, c->d_vloc, c->d_ncoret, c->d_vk, c->d_vk_f};
   for (void *p : ptrs) cudaFree(p);
   for (int k = 0; k < 4; k++) cudaFree(c->d_sigma[k]);
   for (int k = 0; k < 3; k++) {

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256) k_fft_axis(AxisDev ax, Dims3 d, int TL, i
     for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
       int l, j;
       if (linefast) { j = idx / TL; l = idx % TL; } else { l = idx / n; j = idx % n; }
-      if (l < nl) res[l * ls + j * js] = op.mid(b, base + l * lstride + j * jstride, res[l * ls + j * js]);
+      if (l < nl) res[l * ls + j * js] = op.mid(b, base + l * lstride + j * jstride, op.line(base + l * lstride), j, res[l * ls + j * js]);
     }
     __syncthreads();
     res = tile_fft(res, other, ax, TL, ls, js, linefast, tw, +1);
@@ -250,7 +250,8 @@ template <typename C> struct OpCopy {
   static constexpr bool kMid = false;
   __device__ C load(int b, int64_t g) const { return src[b * bstride + g]; }
   __device__ void store(int b, int64_t g, C v) const { dst[b * bstride + g] = v; }
-  __device__ C mid(int, int64_t, C v) const { return v; }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
 
 template <typename C> inline int tile_lines(int axis, int n, int nlines_hint) {
@@ -275,10 +276,195 @@ inline AxisDev axis_dev(const FFTAxis &a) {
   return d;
 }
 
+// ------------------------------------------------------------------------
+// Specialised transform: the line length N, its radix plan and the tile
+// width TL are compile-time constants, so every index of the butterfly loops
+// is a multiply/shift and the stages unroll.  All axes stage the tile as
+// [element][line] with an odd line stride TL+1: threads of a warp take
+// consecutive lines of the same butterfly, which keeps shared memory free of
+// bank conflicts for every stage and every axis.
+// ------------------------------------------------------------------------
+constexpr int kRadixPref[6] = {8, 4, 2, 3, 5, 7};
+constexpr int ct_nstage(int n) {
+  int c = 0;
+  for (int k = 0; k < 6; k++)
+    while (n % kRadixPref[k] == 0) { n /= kRadixPref[k]; c++; }
+  return n == 1 ? c : -1;
+}
+constexpr int ct_radix(int n, int s) {
+  int c = 0;
+  for (int k = 0; k < 6; k++)
+    while (n % kRadixPref[k] == 0) {
+      if (c == s) return kRadixPref[k];
+      n /= kRadixPref[k];
+      c++;
+    }
+  return 1;
+}
+constexpr int ct_pre(int n, int s) {  // product of the radices before stage s
+  int p = 1;
+  for (int t = 0; t < s; t++) p *= ct_radix(n, t);
+  return p;
+}
+
+template <typename C, int N, int TL, int NT, int S>
+__device__ __forceinline__ void ct_stage(const C *__restrict__ in, C *__restrict__ out, const C *tw, int sign) {
+  constexpr int R = ct_radix(N, S);
+  constexpr int P = ct_pre(N, S);
+  constexpr int M = N / R;
+  constexpr int NB = TL * M;
+  constexpr int TSTEP = N / (P * R);
+  constexpr int LS = TL + 1;
+#pragma unroll 1
+  for (int idx = threadIdx.x; idx < NB; idx += NT) {
+    const int l = idx % TL;
+    const int i = idx / TL;
+    const int k = i % P;
+    C u[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) u[q] = in[(i + q * M) * LS + l];
+    if (P > 1) {
+#pragma unroll
+      for (int q = 1; q < R; q++) u[q] = cmul(u[q], twid(tw, q * k * TSTEP, sign));
+    }
+    Butterfly<C, R>::run(u, tw, N, sign);
+    const int j = (i - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; q++) out[(j + q * P) * LS + l] = u[q];
+  }
+}
+
+template <typename C, int N, int TL, int NT, int S> struct CtStages {
+  // runs stages S.. and returns the buffer holding the result
+  static __device__ __forceinline__ C *run(C *a, C *b, const C *tw, int sign) {
+    if constexpr (S >= ct_nstage(N)) {
+      return a;
+    } else {
+      ct_stage<C, N, TL, NT, S>(a, b, tw, sign);
+      __syncthreads();
+      return CtStages<C, N, TL, NT, S + 1>::run(b, a, tw, sign);
+    }
+  }
+};
+
+template <typename C, int N, int TL, int AXIS, class Op>
+__global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, int sign, const C *__restrict__ twg, Op op) {
+  constexpr int NT = 256;
+  constexpr int LS = TL + 1;
+  static_assert(ct_nstage(N) > 0, "unsupported length");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *tw = reinterpret_cast<C *>(smem_raw);
+  C *bufa = tw + N;
+  C *bufb = bufa + N * LS;
+  for (int t = threadIdx.x; t < N; t += NT) tw[t] = twg[t];
+  const int b = blockIdx.y;
+  const int tile = blockIdx.x;
+  int64_t base;
+  int lstride, jstride, nl;
+  if (AXIS == 0) {
+    const int nlines = d.n1 * d.n2;
+    const int l0 = tile * TL;
+    nl = min(TL, nlines - l0);
+    base = (int64_t)l0 * N;
+    lstride = N;
+    jstride = 1;
+  } else if (AXIS == 1) {
+    const int tpz = (d.n0 + TL - 1) / TL;
+    const int z = tile / tpz;
+    const int x0 = (tile - z * tpz) * TL;
+    nl = min(TL, d.n0 - x0);
+    base = x0 + (int64_t)d.n0 * d.n1 * z;
+    lstride = 1;
+    jstride = d.n0;
+  } else {
+    const int nlines = d.n0 * d.n1;
+    const int t0 = tile * TL;
+    nl = min(TL, nlines - t0);
+    base = t0;
+    lstride = 1;
+    jstride = d.n0 * d.n1;
+  }
+  constexpr int TOT = TL * N;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < TOT; e += NT) {
+    int l, j;
+    if (AXIS == 0) { l = e / N; j = e - l * N; } else { j = e / TL; l = e - j * TL; }
+    C v;
+    if (l < nl) v = op.load(b, base + l * lstride + j * jstride);
+    else { v.x = 0; v.y = 0; }
+    bufa[j * LS + l] = v;
+  }
+  __syncthreads();
+  C *res;
+  if constexpr (Op::kMid) {
+    // per-line value of the k-space hook (e.g. kx^2 + ky^2 of a z-line)
+    __shared__ decltype(op.line(0)) lvs[TL];
+    if (threadIdx.x < nl) lvs[threadIdx.x] = op.line(base + threadIdx.x * lstride);
+    res = CtStages<C, N, TL, NT, 0>::run(bufa, bufb, tw, -1);
+#pragma unroll 4
+    for (int e = threadIdx.x; e < TOT; e += NT) {
+      const int j = e / TL, l = e - j * TL;
+      if (l < nl) res[j * LS + l] = op.mid(b, base + l * lstride + j * jstride, lvs[l], j, res[j * LS + l]);
+    }
+    __syncthreads();
+    res = CtStages<C, N, TL, NT, 0>::run(res, res == bufa ? bufb : bufa, tw, +1);
+  } else {
+    res = CtStages<C, N, TL, NT, 0>::run(bufa, bufb, tw, sign);
+  }
+#pragma unroll 4
+  for (int e = threadIdx.x; e < TOT; e += NT) {
+    int l, j;
+    if (AXIS == 0) { l = e / N; j = e - l * N; } else { j = e / TL; l = e - j * TL; }
+    if (l < nl) op.store(b, base + l * lstride + j * jstride, res[j * LS + l]);
+  }
+}
+
+template <typename C, int N> constexpr int ct_tile() {
+  // ~24 KB per ping-pong buffer, power of two, at most 32 lines
+  constexpr int budget = (sizeof(C) == 8 ? 3072 : 1536);
+  return budget / N >= 32 ? 32 : (budget / N >= 16 ? 16 : (budget / N >= 8 ? 8 : 4));
+}
+
+template <typename C, int N, int AXIS, class Op>
+int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op) {
+  constexpr int TL = ct_tile<C, N>();
+  int64_t tiles;
+  if (AXIS == 0) tiles = ((int64_t)d.n1 * d.n2 + TL - 1) / TL;
+  else if (AXIS == 1) tiles = (int64_t)((d.n0 + TL - 1) / TL) * d.n2;
+  else tiles = ((int64_t)d.n0 * d.n1 + TL - 1) / TL;
+  const size_t smem = sizeof(C) * ((size_t)N + 2 * (size_t)N * (TL + 1));
+  auto kern = k_fft_ct<C, N, TL, AXIS, Op>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error(std::string("fft smem attribute: ") + cudaGetErrorString(e));
+      return OPAW_ERR_CUDA;
+    }
+  }
+  dim3 grid((unsigned)tiles, (unsigned)batch);
+  kern<<<grid, 256, smem, c->stream>>>(d, sign, axis_tw<C>(a), op);
+  c->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("fft axis launch: ") + cudaGetErrorString(e));
+    return OPAW_ERR_CUDA;
+  }
+  return OPAW_OK;
+}
+
 // launch one axis pass over `batch` arrays of dims d
 template <typename C, int AXIS, class Op>
 int launch_axis(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op) {
   const int n = a.n;  // n == 1 runs zero stages: the fused operations still apply
+  switch (n) {  // specialised lengths of the production grids and their 2x boxes
+    case 32: return launch_ct<C, 32, AXIS>(c, a, d, batch, sign, op);
+    case 48: return launch_ct<C, 48, AXIS>(c, a, d, batch, sign, op);
+    case 64: return launch_ct<C, 64, AXIS>(c, a, d, batch, sign, op);
+    case 96: return launch_ct<C, 96, AXIS>(c, a, d, batch, sign, op);
+    case 128: return launch_ct<C, 128, AXIS>(c, a, d, batch, sign, op);
+    case 192: return launch_ct<C, 192, AXIS>(c, a, d, batch, sign, op);
+    default: break;
+  }
   const int TL = tile_lines<C>(AXIS, n, 0);
   int64_t tiles;
   if (AXIS == 0) tiles = ((int64_t)d.n1 * d.n2 + TL - 1) / TL;

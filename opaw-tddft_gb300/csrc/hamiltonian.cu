@@ -117,47 +117,98 @@ int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, doubl
 // --------------------------------------------------------------- scatter --
 // out_o[upt[u]] += sum over the (atom, box point) entries of u of
 //                  sum_i P_a[i][b] * coef[o][soff[a] + i]
-template <typename R>
+// One thread per grid point of the box union: the projector values of the
+// point are loaded once into registers and reused for every orbital; the
+// entries of a point are summed in atom order (deterministic).
+template <typename R, int EMAX, int MSMAX>
 __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__restrict__ out, int64_t nn, int nunion,
-                                                       const int *__restrict__ upt, const int *__restrict__ ustart,
-                                                       const int *__restrict__ uatom, const int *__restrict__ ubox,
-                                                       const R *__restrict__ P, const int64_t *__restrict__ poff,
+                                                       int norb, const int *__restrict__ upt,
+                                                       const int *__restrict__ ustart, const int *__restrict__ uatom,
+                                                       const int *__restrict__ ubox, const R *__restrict__ P,
+                                                       const int64_t *__restrict__ poff,
                                                        const int *__restrict__ nrough, const int *__restrict__ ms,
                                                        const int64_t *__restrict__ soff,
                                                        const double2 *__restrict__ coef, int ns) {
   typedef typename Tr<R>::C C;
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  const int o = blockIdx.y;
   if (u >= nunion) return;
-  const double2 *co = coef + (int64_t)o * ns;
-  R sx = 0, sy = 0;
-  for (int e = ustart[u]; e < ustart[u + 1]; e++) {
-    const int a = uatom[e], b = ubox[e];
-    const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
-    const R *Pa = P + poff[a] + b;
-    const double2 *ca = co + soff[a];
-    const int m = ms[a];
-    for (int i = 0; i < m; i++) {
-      const R p = Pa[(int64_t)i * nbox];
-      const double2 cf = ca[i];
-      sx += p * (R)cf.x;
-      sy += p * (R)cf.y;
+  const int e0 = ustart[u], ne = ustart[u + 1] - e0;
+  C *dst = out + upt[u];
+  if (ne <= EMAX) {
+    R pv[EMAX][MSMAX];
+    int so[EMAX], mm[EMAX];
+#pragma unroll
+    for (int e = 0; e < EMAX; e++) {
+      mm[e] = 0;
+      so[e] = 0;
+      if (e < ne) {
+        const int a = uatom[e0 + e], b = ubox[e0 + e];
+        const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+        mm[e] = ms[a];
+        so[e] = (int)soff[a];
+        const R *Pa = P + poff[a] + b;
+#pragma unroll
+        for (int i = 0; i < MSMAX; i++) pv[e][i] = (i < mm[e]) ? Pa[(int64_t)i * nbox] : (R)0;
+      }
     }
+    for (int o = 0; o < norb; o++) {
+      const double2 *co = coef + (int64_t)o * ns;
+      R sx = 0, sy = 0;
+#pragma unroll
+      for (int e = 0; e < EMAX; e++) {
+        if (e < ne) {
+#pragma unroll
+          for (int i = 0; i < MSMAX; i++) {
+            if (i < mm[e]) {
+              const double2 cf = co[so[e] + i];
+              sx += pv[e][i] * (R)cf.x;
+              sy += pv[e][i] * (R)cf.y;
+            }
+          }
+        }
+      }
+      C v = dst[(int64_t)o * nn];
+      v.x += sx;
+      v.y += sy;
+      dst[(int64_t)o * nn] = v;
+    }
+    return;
   }
-  C *dst = out + (int64_t)o * nn + upt[u];
-  C v = *dst;
-  v.x += sx;
-  v.y += sy;
-  *dst = v;
+  for (int o = 0; o < norb; o++) {
+    const double2 *co = coef + (int64_t)o * ns;
+    R sx = 0, sy = 0;
+    for (int e = e0; e < e0 + ne; e++) {
+      const int a = uatom[e], b = ubox[e];
+      const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+      const R *Pa = P + poff[a] + b;
+      const double2 *ca = co + soff[a];
+      const int m = ms[a];
+      for (int i = 0; i < m; i++) {
+        const R p = Pa[(int64_t)i * nbox];
+        sx += p * (R)ca[i].x;
+        sy += p * (R)ca[i].y;
+      }
+    }
+    C v = dst[(int64_t)o * nn];
+    v.x += sx;
+    v.y += sy;
+    dst[(int64_t)o * nn] = v;
+  }
 }
 
 template <typename R>
 int union_scatter(opaw_ctx *c, int which, typename Tr<R>::C *out, int norb, const double2 *coef) {
   if (c->nunion == 0) return OPAW_OK;
   const R *P = ProjTab<R>::get(c, which);
-  dim3 grid(grid1(c->nunion, 256), norb);
-  k_union_scatter<R><<<grid, 256, 0, c->stream>>>(out, c->nn, c->nunion, c->d_upt, c->d_ustart, c->d_uatom, c->d_ubox,
-                                                  P, c->d_poff, c->d_nrough, c->d_ms, c->d_soff, coef, c->ns);
+  const int grid = grid1(c->nunion, 128);
+  if (c->msmax <= 8)
+    k_union_scatter<R, 2, 8><<<grid, 128, 0, c->stream>>>(out, c->nn, c->nunion, norb, c->d_upt, c->d_ustart,
+                                                          c->d_uatom, c->d_ubox, P, c->d_poff, c->d_nrough, c->d_ms,
+                                                          c->d_soff, coef, c->ns);
+  else
+    k_union_scatter<R, 1, 16><<<grid, 128, 0, c->stream>>>(out, c->nn, c->nunion, norb, c->d_upt, c->d_ustart,
+                                                           c->d_uatom, c->d_ubox, P, c->d_poff, c->d_nrough, c->d_ms,
+                                                           c->d_soff, coef, c->ns);
   c->launches++;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
@@ -209,11 +260,13 @@ template <> struct OpKin<double> {
   static constexpr bool kMid = true;
   __device__ double2 load(int b, int64_t g) const { return buf[b * bstride + g]; }
   __device__ void store(int b, int64_t g, double2 v) const { buf[b * bstride + g] = v; }
-  __device__ double2 mid(int, int64_t g, double2 v) const {
-    const int x = (int)(g % nx);
-    const int y = (int)((g / nx) % ny);
-    const int z = (int)(g / ((int64_t)nx * ny));
-    double e = __dadd_rn(__dadd_rn(k2x[x], k2y[y]), k2z[z]) * 0.5;
+  // z-lines: the line index is the (x, y) position
+  __device__ double line(int64_t gl) const {
+    const int t = (int)gl;
+    return __dadd_rn(k2x[t % nx], k2y[t / nx]);
+  }
+  __device__ double2 mid(int, int64_t, double kxy, int z, double2 v) const {
+    double e = __dadd_rn(kxy, k2z[z]) * 0.5;
     if (ekcut > 0.0 && e > ekcut) e = ekcut;
     e = __ddiv_rn(e, ntot);
     return make_double2(v.x * e, v.y * e);
@@ -228,11 +281,12 @@ template <> struct OpKin<float> {
   static constexpr bool kMid = true;
   __device__ float2 load(int b, int64_t g) const { return buf[b * bstride + g]; }
   __device__ void store(int b, int64_t g, float2 v) const { buf[b * bstride + g] = v; }
-  __device__ float2 mid(int, int64_t g, float2 v) const {
-    const int x = (int)(g % nx);
-    const int y = (int)((g / nx) % ny);
-    const int z = (int)(g / ((int64_t)nx * ny));
-    float e = (k2x[x] + k2y[y] + k2z[z]) * 0.5f;
+  __device__ float line(int64_t gl) const {
+    const int t = (int)gl;
+    return k2x[t % nx] + k2y[t / nx];
+  }
+  __device__ float2 mid(int, int64_t, float kxy, int z, float2 v) const {
+    float e = (kxy + k2z[z]) * 0.5f;
     if (ekcut > 0.f && e > ekcut) e = ekcut;
     e *= invn;
     return make_float2(v.x * e, v.y * e);
@@ -257,7 +311,8 @@ template <typename R> struct OpHFinal {
     r.y = v.y + p.y * w;
     hp[b * bstride + g] = r;
   }
-  __device__ C mid(int, int64_t, C v) const { return v; }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
 
 template <typename R> struct VksOf;

@@ -18,7 +18,7 @@ namespace opaw {
 template <typename R> int rebuild_from(opaw_ctx *c, int set, const typename Tr<R>::C *psibar, int norb);
 template <typename R> int rhoij_density_from(opaw_ctx *c, int set, const typename Tr<R>::C *psit, int norb, int what);
 int nhat_step(opaw_ctx *c, int set);
-int vks_step(opaw_ctx *c, int set);
+int vks_step(opaw_ctx *c, int set, int fp32_hartree);
 int dij_step(opaw_ctx *c, int set);
 
 __device__ __forceinline__ double bsum256(double v, double *sh) {
@@ -129,15 +129,19 @@ template <typename C> static int norms(opaw_ctx *c, const C *p, int norb, double
   return OPAW_OK;
 }
 
-// stage update (rk4.f90:44-48): k = -i * shs(pin); ksum (+)= w k; y = p + dts k
-template <typename CK, typename CY, typename CS>
-__global__ void k_rk4_stage(const CK *__restrict__ kraw, const double2 *__restrict__ p, CS *__restrict__ ksum,
-                            CY *__restrict__ y, int64_t n, double w, int first, double dts, int write_y) {
+// stage update (rk4.f90:44-48): k = -i * shs(pin); ksum (+)= w k; y = p + dts k.
+// Arithmetic in the precision of the stage vectors: FP64 for the FP64 path,
+// FP32 for the mixed path (p is read as FP64 and rounded once).
+template <typename R>
+__global__ void k_rk4_stage(const typename Tr<R>::C *__restrict__ kraw, const double2 *__restrict__ p,
+                            typename Tr<R>::C *__restrict__ ksum, typename Tr<R>::C *__restrict__ y, int64_t n,
+                            R w, int first, R dts, int write_y) {
+  typedef typename Tr<R>::C C;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const CK kr = kraw[i];
-  const double kx = (double)kr.y, ky = -(double)kr.x;  // -i*(a + ib) = b - ia
-  CS s;
+  const C kr = kraw[i];
+  const R kx = kr.y, ky = -kr.x;  // -i*(a + ib) = b - ia
+  C s;
   if (first) {
     s.x = w * kx;
     s.y = w * ky;
@@ -149,9 +153,9 @@ __global__ void k_rk4_stage(const CK *__restrict__ kraw, const double2 *__restri
   ksum[i] = s;
   if (write_y) {
     const double2 pv = p[i];
-    CY yv;
-    yv.x = pv.x + dts * kx;
-    yv.y = pv.y + dts * ky;
+    C yv;
+    yv.x = (R)pv.x + dts * kx;
+    yv.y = (R)pv.y + dts * ky;
     y[i] = yv;
   }
 }
@@ -168,16 +172,19 @@ __global__ void k_rk4_final(double2 *__restrict__ p, const CS *__restrict__ ksum
   p[i] = v;
 }
 
-// p_o *= nrm0[o] / nrm1[o]  (rk4.f90:99)
-__global__ void k_rescale(double2 *__restrict__ p, int64_t nn, const double *__restrict__ nrm0,
-                          const double *__restrict__ nrm1) {
+// f[o] = nrm0[o] / nrm1[o], then p_o *= f[o]  (rk4.f90:99)
+__global__ void k_rescale_factor(const double *__restrict__ nrm0, double *__restrict__ nrm1, int norb) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < norb) nrm1[o] = nrm0[o] / nrm1[o];
+}
+__global__ void k_rescale(double2 *__restrict__ p, int64_t nn, const double *__restrict__ f) {
   const int o = blockIdx.y;
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (g >= nn) return;
-  const double f = nrm0[o] / nrm1[o];
+  const double s = f[o];
   double2 v = p[(int64_t)o * nn + g];
-  v.x *= f;
-  v.y *= f;
+  v.x *= s;
+  v.y *= s;
   p[(int64_t)o * nn + g] = v;
 }
 
@@ -222,7 +229,8 @@ template <typename R> static int rk4_set(opaw_ctx *c, int set, double dt) {
   const double dts[4] = {dt / 2.0, dt / 2.0, dt, dt};
   for (int st = 0; st < 4; st++) {
     OPAW_CHECK(shs_apply<R>(c, set, pin, k, norb));
-    k_rk4_stage<C, C, C><<<grid1(tot, 256), 256, 0, c->stream>>>(k, p, ks, y, tot, wts[st], st == 0, dts[st], st < 3);
+    k_rk4_stage<R><<<grid1(tot, 256), 256, 0, c->stream>>>(k, p, ks, y, tot, (R)wts[st], st == 0, (R)dts[st],
+                                                          st < 3);
     c->launches++;
     OPAW_CUDA(cudaGetLastError());
     if (st < 3) OPAW_CHECK(rebuild_from<R>(c, set, y, norb));  // rk4.f90:53-55
@@ -231,9 +239,10 @@ template <typename R> static int rk4_set(opaw_ctx *c, int set, double dt) {
   k_rk4_final<C><<<grid1(tot, 256), 256, 0, c->stream>>>(p, ks, tot, dt / 6.0);
   c->launches++;
   OPAW_CHECK(norms<double2>(c, p, norb, part, nrm1));  // norm1 (rk4.f90:98)
+  k_rescale_factor<<<grid1(norb, 128), 128, 0, c->stream>>>(nrm0, nrm1, norb);
   dim3 g(grid1(c->nn, 256), norb);
-  k_rescale<<<g, 256, 0, c->stream>>>(p, c->nn, nrm0, nrm1);
-  c->launches++;
+  k_rescale<<<g, 256, 0, c->stream>>>(p, c->nn, nrm1);
+  c->launches += 2;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
 }
@@ -359,7 +368,7 @@ int opaw_nhat(opaw_ctx *c, int set) {
 
 int opaw_vks(opaw_ctx *c, int set) {
   OPAW_CHECK(check_cs(c, set));
-  OPAW_CHECK(vks_step(c, set));
+  OPAW_CHECK(vks_step(c, set, 0));
   return finish(c);
 }
 

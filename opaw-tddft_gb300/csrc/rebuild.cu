@@ -6,6 +6,7 @@
 // All of it is FP64 (the small matrices and potentials); only psi~ and the
 // box sums follow the orbital precision.
 #include <cmath>
+#include <type_traits>
 
 #include "fft.cuh"
 
@@ -70,6 +71,11 @@ __global__ void k_vk_finish(const double2 *cvk, double *vk, BigBox b, const doub
   vk[g] = __ddiv_rn(__ddiv_rn(__ddiv_rn(re + ct, (double)b.nx), (double)b.ny), (double)b.nz);  // vk_scale.f90:46
 }
 
+__global__ void k_vk_to_float(const double *a, float *b, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
 static double kcomp(int i, int n, double d) {
   const double pi = acos(-1.0);
   double dk = 2.0 * pi / ((double)n * d);
@@ -110,6 +116,9 @@ int vk_prep(opaw_ctx *c) {
                                                      c->periodic);
   c->launches++;
   OPAW_CUDA(cudaGetLastError());
+  OPAW_CUDA(cudaMalloc(&c->d_vk_f, sizeof(float) * nb));
+  k_vk_to_float<<<grid1(nb, 256), 256, 0, c->stream>>>(c->d_vk, c->d_vk_f, nb);
+  c->launches++;
   OPAW_CUDA(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < 3; k++) cudaFree(dk[k]);
   return OPAW_OK;
@@ -130,64 +139,91 @@ struct Embed {
   }
 };
 
-struct OpEmbed {
+template <typename R> struct OpEmbed {
+  typedef typename Tr<R>::C C;
   Embed e;
   const double *d0, *d1;
-  double2 *wb;
+  C *wb;
   static constexpr bool kMid = false;
-  __device__ double2 load(int, int64_t g) const {
+  __device__ C load(int, int64_t g) const {
     int64_t i;
-    if (!e.inner(g, i)) return make_double2(0.0, 0.0);
-    return make_double2(d0[i], d1 ? d1[i] : 0.0);
+    C v;
+    v.x = 0;
+    v.y = 0;
+    if (!e.inner(g, i)) return v;
+    v.x = (R)d0[i];
+    v.y = d1 ? (R)d1[i] : (R)0;
+    return v;
   }
-  __device__ void store(int, int64_t g, double2 v) const { wb[g] = v; }
-  __device__ double2 mid(int, int64_t, double2 v) const { return v; }
+  __device__ void store(int, int64_t g, C v) const { wb[g] = v; }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
 
-struct OpVk {
-  double2 *wb;
-  const double *vk;
+template <typename R> struct OpVk {
+  typedef typename Tr<R>::C C;
+  C *wb;
+  const R *vk;
   static constexpr bool kMid = true;
-  __device__ double2 load(int, int64_t g) const { return wb[g]; }
-  __device__ void store(int, int64_t g, double2 v) const { wb[g] = v; }
-  __device__ double2 mid(int, int64_t g, double2 v) const {
-    const double k = vk[g];
-    return make_double2(v.x * k, v.y * k);
+  __device__ C load(int, int64_t g) const { return wb[g]; }
+  __device__ void store(int, int64_t g, C v) const { wb[g] = v; }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ C mid(int, int64_t g, double, int, C v) const {
+    const R k = vk[g];
+    v.x *= k;
+    v.y *= k;
+    return v;
   }
 };
 
-struct OpCrop {
+template <typename R> struct OpCrop {
+  typedef typename Tr<R>::C C;
   Embed e;
-  const double2 *wb;
+  const C *wb;
   double *v0, *v1;
   double cn, nbd;
   static constexpr bool kMid = false;
-  __device__ double2 load(int, int64_t g) const { return wb[g]; }
-  __device__ void store(int, int64_t g, double2 v) const {
+  __device__ C load(int, int64_t g) const { return wb[g]; }
+  __device__ void store(int, int64_t g, C v) const {
     int64_t i;
     if (!e.inner(g, i)) return;
-    v0[i] = (v.x * cn) * nbd;  // rconv :29, get_vcon :20
-    if (v1) v1[i] = (v.y * cn) * nbd;
+    v0[i] = ((double)v.x * cn) * nbd;  // rconv :29, get_vcon :20
+    if (v1) v1[i] = ((double)v.y * cn) * nbd;
   }
-  __device__ double2 mid(int, int64_t, double2 v) const { return v; }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
 
-int hartree(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1) {
-  OPAW_CHECK(ensure(c->work[3], sizeof(double2) * c->nnb));
-  double2 *wb = (double2 *)c->work[3].p;
+template <typename R> struct VkOf;
+template <> struct VkOf<double> {
+  static const double *get(const opaw_ctx *c) { return c->d_vk; }
+};
+template <> struct VkOf<float> {
+  static const float *get(const opaw_ctx *c) { return c->d_vk_f; }
+};
+
+template <typename R>
+int hartree_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1) {
+  typedef typename Tr<R>::C C;
+  OPAW_CHECK(ensure(c->work[3], sizeof(C) * c->nnb));
+  C *wb = (C *)c->work[3].p;
   Embed e{c->nx, c->ny, c->nz, c->nxb, c->nyb, c->nxb / 2 - c->nx / 2, c->nyb / 2 - c->ny / 2, c->nzb / 2 - c->nz / 2};
   Dims3 d{c->nxb, c->nyb, c->nzb};
   const double nbd = (double)c->nxb * (double)c->nyb * (double)c->nzb;
-  OpEmbed emb{e, dens0, dens1, wb};
-  OpCopy<double2> inplace{wb, wb, c->nnb};
-  OpVk vkop{wb, c->d_vk};
-  OpCrop crop{e, wb, vh0, vh1, 1.0 / nbd, nbd};
-  OPAW_CHECK((launch_axis<double2, 0>(c, c->fftb.ax[0], d, 1, -1, emb)));
-  OPAW_CHECK((launch_axis<double2, 1>(c, c->fftb.ax[1], d, 1, -1, inplace)));
-  OPAW_CHECK((launch_axis<double2, 2>(c, c->fftb.ax[2], d, 1, 0, vkop)));
-  OPAW_CHECK((launch_axis<double2, 1>(c, c->fftb.ax[1], d, 1, +1, inplace)));
-  OPAW_CHECK((launch_axis<double2, 0>(c, c->fftb.ax[0], d, 1, +1, crop)));
+  OpEmbed<R> emb{e, dens0, dens1, wb};
+  OpCopy<C> inplace{wb, wb, c->nnb};
+  OpVk<R> vkop{wb, VkOf<R>::get(c)};
+  OpCrop<R> crop{e, wb, vh0, vh1, 1.0 / nbd, nbd};
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 1, -1, emb)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, 1, -1, inplace)));
+  OPAW_CHECK((launch_axis<C, 2>(c, c->fftb.ax[2], d, 1, 0, vkop)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, 1, +1, inplace)));
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 1, +1, crop)));
   return OPAW_OK;
+}
+
+int hartree(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1) {
+  return hartree_t<double>(c, dens0, dens1, vh0, vh1);
 }
 
 // ------------------------------------------------------ LDA (A17) --
@@ -230,7 +266,8 @@ struct OpBk {
   static constexpr bool kMid = true;
   __device__ double2 load(int, int64_t g) const { return a[g]; }
   __device__ void store(int, int64_t g, double2 v) const { a[g] = v; }
-  __device__ double2 mid(int, int64_t g, double2 v) const {
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ double2 mid(int, int64_t g, double, int, double2 v) const {
     const double k = bk[g];
     return make_double2(v.x * k, v.y * k);
   }
@@ -242,7 +279,8 @@ struct OpReal {
   static constexpr bool kMid = false;
   __device__ double2 load(int, int64_t g) const { return a[g]; }
   __device__ void store(int, int64_t g, double2 v) const { out[g] = v.x * cn; }
-  __device__ double2 mid(int, int64_t, double2 v) const { return v; }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ double2 mid(int, int64_t, double, int, double2 v) const { return v; }
 };
 
 int rconv_device(opaw_ctx *c, double2 *a, const double *bk, double *gout, int n0, int n1, int n2) {
@@ -275,11 +313,18 @@ template <typename C>
 __global__ void k_density(const C *__restrict__ psi, int norb, int64_t nn, double *__restrict__ dens) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nn) return;
+  typedef decltype(psi[0].x) RR;
+  typedef typename std::remove_const<typename std::remove_reference<RR>::type>::type R;
   double acc = 0;
-  for (int o = 0; o < norb; o++) {
-    const C z = psi[(int64_t)o * nn + i];
-    const double x = z.x, y = z.y;
-    acc += x * x + y * y;
+  // sums of up to 16 orbitals in the orbital precision, added in FP64
+  for (int o0 = 0; o0 < norb; o0 += 16) {
+    R part = 0;
+    const int o1 = min(norb, o0 + 16);
+    for (int o = o0; o < o1; o++) {
+      const C z = psi[(int64_t)o * nn + i];
+      part += z.x * z.x + z.y * z.y;
+    }
+    acc += (double)part;
   }
   dens[i] = 2.0 * acc;  // tddft_dens.f90:73
 }
@@ -471,7 +516,7 @@ __global__ void k_add(const double *a, const double *b, double *o, int64_t n) {
   if (i < n) o[i] = a[i] + b[i];
 }
 
-int vks_step(opaw_ctx *c, int set) {
+int vks_step(opaw_ctx *c, int set, int fp32_hartree) {
   OPAW_CHECK(ensure(c->work[2], sizeof(double) * c->nn * 2));
   double *t = (double *)c->work[2].p;  // n~ + n^ for the Hartree solve
   k_vxc<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_dens[set], c->d_ncoret, c->d_vxc[set], c->nn);
@@ -480,7 +525,8 @@ int vks_step(opaw_ctx *c, int set) {
   // t = dens + nhat (tddft_pot.f90:39)
   k_add<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_dens[set], c->d_nhat[set], t, c->nn);
   c->launches++;
-  OPAW_CHECK(hartree(c, t, nullptr, c->d_vh[set], nullptr));
+  if (fp32_hartree) OPAW_CHECK(hartree_t<float>(c, t, nullptr, c->d_vh[set], nullptr));
+  else OPAW_CHECK(hartree_t<double>(c, t, nullptr, c->d_vh[set], nullptr));
   const double *mean = nullptr;
   if (c->periodic) {
     double *part = red_scratch(c);
@@ -525,7 +571,7 @@ template <typename R> int rebuild_from(opaw_ctx *c, int set, const typename Tr<R
   OPAW_CHECK(rhoij_from_coef(c, set, co, norb));  // :125
   OPAW_CHECK(density_of<R>(c, set, pt, norb));    // :126
   OPAW_CHECK(nhat_step(c, set));                  // :127
-  OPAW_CHECK(vks_step(c, set));                   // :128
+  OPAW_CHECK(vks_step(c, set, sizeof(R) == 4));    // :128 (FP32 Hartree on the mixed path)
   OPAW_CHECK(dij_step(c, set));                   // :129
   return OPAW_OK;
 }

@@ -335,7 +335,9 @@ def hamiltonian_microbench(norb=128, seed=2024):
 
 def small_system(kind="tiny", seed=7, norb=4):
     """Test-sized systems.  'tiny' 24x20x16; 'odd' exercises radices 3,5,7;
-    'edge' is periodic with boxes that wrap around the faces."""
+    'edge' is periodic with boxes that wrap around the faces; 'spec' uses
+    extents with compile-time specialised FFT kernels (32, 48, 64 and the
+    64, 96, 128 Hartree box)."""
     if kind == "tiny":
         return build_system(n=(24, 20, 16), h=0.5, natom=3, seed=seed, rc=0.8, norb=norb)
     if kind == "odd":
@@ -344,6 +346,8 @@ def small_system(kind="tiny", seed=7, norb=4):
         coords = np.array([[5.9, 0.3, -0.2], [-1.0, -4.8, 3.7], [0.5, 1.5, 0.1]])
         return build_system(n=(24, 20, 16), h=0.5, natom=3, seed=seed, rc=0.8, norb=norb,
                             periodic=1, coords=coords)
+    if kind == "spec":
+        return build_system(n=(32, 48, 64), h=0.5, natom=4, seed=seed, rc=0.8, norb=norb)
     if kind == "medium":
         return build_system(n=(48, 48, 32), h=0.5, natom=10, seed=seed, rc=1.0, norb=norb)
     raise ValueError(kind)

@@ -41,7 +41,7 @@ def make(kind, norb=3, seed=5):
     return s, psi, o, c
 
 
-@pytest.fixture(scope="module", params=["tiny", "odd", "edge"])
+@pytest.fixture(scope="module", params=["tiny", "odd", "edge", "spec"])
 def case(request):
     s, psi, o, c = make(request.param)
     yield s, psi, o, c
@@ -148,7 +148,7 @@ def test_kick_and_dipole(case):
     assert np.allclose(dd, rd, rtol=1e-8, atol=1e-9)
 
 
-@pytest.mark.parametrize("kind", ["tiny", "edge"])
+@pytest.mark.parametrize("kind", ["tiny", "edge", "spec"])
 def test_tddft_steps_fp64_and_mixed(kind):
     s, psi, o, c = make(kind, norb=3)
     g = 1e-3
