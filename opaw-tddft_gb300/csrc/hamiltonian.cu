@@ -28,6 +28,27 @@ template <typename T> __device__ __forceinline__ T warp_sum(T v) {
 }
 
 // ---------------------------------------------------------------- gather --
+// Warp reduction of NV register values by recursive halving: at each level a
+// lane keeps one half of its values and receives the partner's sums for that
+// half, so NV values cost NV-1 shuffles in total instead of 5 NV.  Afterwards
+// lane L holds the warp sums of values L*(NV/32) .. L*(NV/32) + NV/32 - 1.
+template <int NV, int LEVEL = 0> struct Halve {
+  template <typename T> static __device__ __forceinline__ void run(T *v, int lane) {
+    constexpr int OFF = 16 >> LEVEL;
+    constexpr int HALF = (NV >> LEVEL) / 2;
+    if constexpr (OFF >= 1 && HALF >= 1) {
+      const bool up = (lane & OFF) != 0;
+#pragma unroll
+      for (int k = 0; k < HALF; k++) {
+        const T send = up ? v[k] : v[k + HALF];
+        const T keep = up ? v[k + HALF] : v[k];
+        v[k] = keep + __shfl_xor_sync(0xffffffffu, send, OFF);
+      }
+      Halve<NV, LEVEL + 1>::run(v, lane);
+    }
+  }
+};
+
 // out[o*ns + soff[a] + i] = dv * sum_box P_a[i][b] * psi_o[g(b)]   (p real: Gamma point)
 template <typename R, int MSMAX, int OB>
 __global__ void __launch_bounds__(256) k_gather(const typename Tr<R>::C *__restrict__ psi, int64_t nn, int norb,
@@ -36,6 +57,8 @@ __global__ void __launch_bounds__(256) k_gather(const typename Tr<R>::C *__restr
                                                 const int *__restrict__ ms, const int64_t *__restrict__ soff, int nx,
                                                 int ny, int nz, double dv, double2 *__restrict__ out, int ns) {
   typedef typename Tr<R>::C C;
+  constexpr int NV = OB * MSMAX * 2;  // value index (o * MSMAX + i) * 2 + re/im
+  static_assert(NV >= 32 && (NV & (NV - 1)) == 0, "NV must be a power of two >= 32");
   const int a = blockIdx.x;
   const int o0 = blockIdx.y * OB;
   const int m = ms[a];
@@ -43,11 +66,9 @@ __global__ void __launch_bounds__(256) k_gather(const typename Tr<R>::C *__restr
   const int nbox = n0 * n1 * n2;
   const int x0 = ir0[3 * a], y0 = ir0[3 * a + 1], z0 = ir0[3 * a + 2];
   const R *Pa = P + poff[a];
-  R ax[OB][MSMAX], ay[OB][MSMAX];
+  R v[NV];
 #pragma unroll
-  for (int o = 0; o < OB; o++)
-#pragma unroll
-    for (int i = 0; i < MSMAX; i++) ax[o][i] = ay[o][i] = 0;
+  for (int k = 0; k < NV; k++) v[k] = 0;
   for (int b = threadIdx.x; b < nbox; b += blockDim.x) {
     const int bx = b % n0, by = (b / n0) % n1, bz = b / (n0 * n1);
     const int64_t g = wrapi(x0 + bx, nx) + (int64_t)nx * (wrapi(y0 + by, ny) + (int64_t)ny * wrapi(z0 + bz, nz));
@@ -57,27 +78,21 @@ __global__ void __launch_bounds__(256) k_gather(const typename Tr<R>::C *__restr
 #pragma unroll
     for (int o = 0; o < OB; o++) {
       if (o0 + o < norb) {
-        C v = psi[(int64_t)(o0 + o) * nn + g];
+        const C z = psi[(int64_t)(o0 + o) * nn + g];
 #pragma unroll
         for (int i = 0; i < MSMAX; i++) {
-          ax[o][i] += p[i] * v.x;
-          ay[o][i] += p[i] * v.y;
+          v[(o * MSMAX + i) * 2] += p[i] * z.x;
+          v[(o * MSMAX + i) * 2 + 1] += p[i] * z.y;
         }
       }
     }
   }
-  __shared__ R red[8][OB][MSMAX][2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Halve<NV>::run(v, lane);
+  constexpr int PER = NV / 32;
+  __shared__ R red[8][NV];
 #pragma unroll
-  for (int o = 0; o < OB; o++)
-#pragma unroll
-    for (int i = 0; i < MSMAX; i++) {
-      R sx = warp_sum(ax[o][i]), sy = warp_sum(ay[o][i]);
-      if (lane == 0) {
-        red[warp][o][i][0] = sx;
-        red[warp][o][i][1] = sy;
-      }
-    }
+  for (int k = 0; k < PER; k++) red[warp][lane * PER + k] = v[k];
   __syncthreads();
   const int nw = blockDim.x >> 5;
   for (int t = threadIdx.x; t < OB * m; t += blockDim.x) {
@@ -85,8 +100,8 @@ __global__ void __launch_bounds__(256) k_gather(const typename Tr<R>::C *__restr
     if (o0 + o >= norb) continue;
     R sx = 0, sy = 0;
     for (int w = 0; w < nw; w++) {
-      sx += red[w][o][i][0];
-      sy += red[w][o][i][1];
+      sx += red[w][(o * MSMAX + i) * 2];
+      sy += red[w][(o * MSMAX + i) * 2 + 1];
     }
     out[(int64_t)(o0 + o) * ns + soff[a] + i] = make_double2((double)sx * dv, (double)sy * dv);
   }
@@ -102,8 +117,9 @@ int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, doubl
     k_gather<R, 8, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_ir0, c->d_nrough, c->d_ms,
                                                     c->d_soff, c->nx, c->ny, c->nz, c->dv, coef, c->ns);
   } else if (c->msmax <= 16) {
-    dim3 grid(c->natom, norb);
-    k_gather<R, 16, 1><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_ir0, c->d_nrough, c->d_ms,
+    constexpr int OB = sizeof(R) == 4 ? 2 : 1;
+    dim3 grid(c->natom, (norb + OB - 1) / OB);
+    k_gather<R, 16, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_ir0, c->d_nrough, c->d_ms,
                                                     c->d_soff, c->nx, c->ny, c->nz, c->dv, coef, c->ns);
   } else {
     set_error("more than 16 projectors per atom");
@@ -120,6 +136,8 @@ int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, doubl
 // One thread per grid point of the box union: the projector values of the
 // point are loaded once into registers and reused for every orbital; the
 // entries of a point are summed in atom order (deterministic).
+constexpr int kScatterOrb = 16;  // orbitals per thread of the box scatter
+
 template <typename R, int EMAX, int MSMAX>
 __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__restrict__ out, int64_t nn, int nunion,
                                                        int norb, const int *__restrict__ upt,
@@ -151,30 +169,41 @@ __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__rest
         for (int i = 0; i < MSMAX; i++) pv[e][i] = (i < mm[e]) ? Pa[(int64_t)i * nbox] : (R)0;
       }
     }
-    for (int o = 0; o < norb; o++) {
-      const double2 *co = coef + (int64_t)o * ns;
-      R sx = 0, sy = 0;
+    const int oa = blockIdx.y * kScatterOrb, ob = min(norb, oa + kScatterOrb);
+    for (int o0 = oa; o0 < ob; o0 += 4) {
+      C cur[4];
 #pragma unroll
-      for (int e = 0; e < EMAX; e++) {
-        if (e < ne) {
+      for (int q = 0; q < 4; q++)
+        if (o0 + q < ob) cur[q] = dst[(int64_t)(o0 + q) * nn];
 #pragma unroll
-          for (int i = 0; i < MSMAX; i++) {
-            if (i < mm[e]) {
-              const double2 cf = co[so[e] + i];
-              sx += pv[e][i] * (R)cf.x;
-              sy += pv[e][i] * (R)cf.y;
+      for (int q = 0; q < 4; q++) {
+        if (o0 + q < ob) {
+          const double2 *co = coef + (int64_t)(o0 + q) * ns;
+          R sx = 0, sy = 0;
+#pragma unroll
+          for (int e = 0; e < EMAX; e++) {
+            if (e < ne) {
+#pragma unroll
+              for (int i = 0; i < MSMAX; i++) {
+                if (i < mm[e]) {
+                  const double2 cf = co[so[e] + i];
+                  sx += pv[e][i] * (R)cf.x;
+                  sy += pv[e][i] * (R)cf.y;
+                }
+              }
             }
           }
+          cur[q].x += sx;
+          cur[q].y += sy;
         }
       }
-      C v = dst[(int64_t)o * nn];
-      v.x += sx;
-      v.y += sy;
-      dst[(int64_t)o * nn] = v;
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        if (o0 + q < ob) dst[(int64_t)(o0 + q) * nn] = cur[q];
     }
     return;
   }
-  for (int o = 0; o < norb; o++) {
+  for (int o = blockIdx.y * kScatterOrb; o < min(norb, (int)(blockIdx.y + 1) * kScatterOrb); o++) {
     const double2 *co = coef + (int64_t)o * ns;
     R sx = 0, sy = 0;
     for (int e = e0; e < e0 + ne; e++) {
@@ -200,7 +229,7 @@ template <typename R>
 int union_scatter(opaw_ctx *c, int which, typename Tr<R>::C *out, int norb, const double2 *coef) {
   if (c->nunion == 0) return OPAW_OK;
   const R *P = ProjTab<R>::get(c, which);
-  const int grid = grid1(c->nunion, 128);
+  const dim3 grid(grid1(c->nunion, 128), (norb + kScatterOrb - 1) / kScatterOrb);
   if (c->msmax <= 8)
     k_union_scatter<R, 2, 8><<<grid, 128, 0, c->stream>>>(out, c->nn, c->nunion, norb, c->d_upt, c->d_ustart,
                                                           c->d_uatom, c->d_ubox, P, c->d_poff, c->d_nrough, c->d_ms,
