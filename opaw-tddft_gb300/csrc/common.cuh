@@ -166,6 +166,7 @@ struct opaw_ctx {
   // 4 rebuild psi~, 5-6 host-twin staging, 7 RK4 k, 8 RK4 y, 9 RK4 ksum
   opaw::DeviceBuf work[12];
   opaw::DeviceBuf coef[4];       // [norb][ns] double2
+  opaw::DeviceBuf mix[12];       // buffers of the mixed-precision difference step
   opaw::DeviceBuf red;           // reductions
   double *h_red = nullptr;       // pinned host mirror of small reductions
 };
@@ -189,12 +190,28 @@ int sn_apply(opaw_ctx *c, double n, const typename Tr<R>::C *pin, typename Tr<R>
 template <typename R>
 int shs_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>::C *pout, int norb);
 
+template <typename R>
+int h_apply_ex(opaw_ctx *c, const R *vks, const double *dij, const typename Tr<R>::C *pin, typename Tr<R>::C *hp,
+               int norb, const double2 *cpre, const typename Tr<R>::C *t0, const R *dv, const double2 *c0,
+               const double *ddij);
+
 // (fft.cu) batched 3D FFT of `batch` arrays; sign -1 forward, +1 backward
 template <typename R>
 int fft3d(opaw_ctx *c, const FFT3 &f, typename Tr<R>::C *data, int batch, int sign);
 
 // (rebuild.cu)
 int hartree(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1);
+template <typename R>
+int hartree_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1);
+int rhoij_of(opaw_ctx *c, const double2 *coef, int norb, double *out);
+template <typename R> int density_raw(opaw_ctx *c, const typename Tr<R>::C *psit, int norb, double *out);
+int nhat_raw_of(opaw_ctx *c, const double *rhoij, double *out);
+int sums2(opaw_ctx *c, const double *a, const double *b, double *part);
+constexpr int kRedBlocks = 1024;
+int vxc_of(opaw_ctx *c, const double *dens, const double *core, double *out);
+int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, double *out);
+// (mixed.cu) nsteps mixed-precision TDDFT steps; 9 doubles per step into dd_dev
+int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev);
 // LDA potential of n points (device arrays)
 int vxc_points(opaw_ctx *c, const double *dens, double *vxc, int64_t n);
 // gout = 1/N ifft(bk fft(a)) on the context's main FFT plan; a is overwritten

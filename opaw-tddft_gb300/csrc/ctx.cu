@@ -282,6 +282,7 @@ static void destroy(opaw_ctx *c) {
   }
   for (auto &b : c->work) cudaFree(b.p);
   for (auto &b : c->coef) cudaFree(b.p);
+  for (auto &b : c->mix) cudaFree(b.p);
   cudaFree(c->red.p);
   if (c->h_red) cudaFreeHost(c->h_red);
   fft3_free(c->fft);

@@ -266,6 +266,32 @@ __global__ void k_coef_dij(const double2 *__restrict__ cin, double2 *__restrict_
   cout[(int64_t)o * ns + t] = make_double2(sx, sy);
 }
 
+// arr = D c + dD c0: the nonlocal coefficients of H' applied to the
+// difference plus those of (H' - H) applied to the unperturbed vector
+__global__ void k_coef_dij2(const double2 *__restrict__ cin, const double2 *__restrict__ c0,
+                            double2 *__restrict__ cout, int norb, int ns, const int *__restrict__ slot_atom,
+                            const int64_t *__restrict__ soff, const int64_t *__restrict__ doff,
+                            const int *__restrict__ ms, const double *__restrict__ dij,
+                            const double *__restrict__ ddij) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int o = blockIdx.y;
+  if (t >= ns || o >= norb) return;
+  const int a = slot_atom[t];
+  const int m = ms[a];
+  const int i = t - (int)soff[a];
+  const double *D = dij + doff[a];
+  const double *dD = ddij + doff[a];
+  const double2 *ci = cin + (int64_t)o * ns + soff[a];
+  const double2 *c0i = c0 + (int64_t)o * ns + soff[a];
+  double sx = 0, sy = 0;
+  for (int j = 0; j < m; j++) {
+    const double d = D[i + m * j], e = dD[i + m * j];
+    sx += d * ci[j].x + e * c0i[j].x;
+    sy += d * ci[j].y + e * c0i[j].y;
+  }
+  cout[(int64_t)o * ns + t] = make_double2(sx, sy);
+}
+
 // coef[o][t] = sigma[t] * c[o][t]   (snphi.f90:24-28)
 __global__ void k_coef_scale(const double2 *__restrict__ cin, double2 *__restrict__ cout, int norb, int ns,
                              const double *__restrict__ sigma) {
@@ -322,7 +348,9 @@ template <> struct OpKin<float> {
   }
 };
 
-// last inverse pass of h_phi: hp = F^-1[...] + pin * v_ks   (hphi.f90:21)
+// last inverse pass of h_phi: hp = F^-1[...] + pin * v_ks   (hphi.f90:21);
+// with t0/dv set it also adds the local part of (H' - H) t0 = dv * t0 (the
+// source term of the perturbation-difference propagation)
 template <typename R> struct OpHFinal {
   typedef typename Tr<R>::C C;
   const C *src;
@@ -330,6 +358,8 @@ template <typename R> struct OpHFinal {
   const R *vks;
   C *hp;
   int64_t bstride;
+  const C *t0;
+  const R *dv;
   static constexpr bool kMid = false;
   __device__ C load(int b, int64_t g) const { return src[b * bstride + g]; }
   __device__ void store(int b, int64_t g, C v) const {
@@ -338,6 +368,12 @@ template <typename R> struct OpHFinal {
     C r;
     r.x = v.x + p.x * w;
     r.y = v.y + p.y * w;
+    if (t0) {
+      const C t = t0[b * bstride + g];
+      const R d = dv[g];
+      r.x += t.x * d;
+      r.y += t.y * d;
+    }
     hp[b * bstride + g] = r;
   }
   __device__ double line(int64_t) const { return 0.0; }
@@ -407,9 +443,51 @@ int h_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>::
   OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, -1, inplace)));
   OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, make_kin<R>(c, w))));
   OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, +1, inplace)));
-  OpHFinal<R> fin{w, pin, VksOf<R>::get(c, set), hp, c->nn};
+  OpHFinal<R> fin{w, pin, VksOf<R>::get(c, set), hp, c->nn, nullptr, nullptr};
   OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, +1, fin)));
   // nonlocal term (hphi.f90:42-60)
+  OPAW_CHECK(union_scatter<R>(c, 0, hp, norb, c1));
+  return OPAW_OK;
+}
+
+// H applied with explicit potential / D_ij, optionally with the projections
+// <p~|pin> already known (cpre) and with the perturbation-difference extras
+// (t0, dv, c0, ddij): hp = H[vks, dij] pin + dv t0 + sum p~ ddij c0
+template <typename R>
+int h_apply_ex(opaw_ctx *c, const R *vks, const double *dij, const typename Tr<R>::C *pin, typename Tr<R>::C *hp,
+               int norb, const double2 *cpre, const typename Tr<R>::C *t0, const R *dv, const double2 *c0,
+               const double *ddij) {
+  typedef typename Tr<R>::C C;
+  if (norb <= 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->work[0], sizeof(C) * (size_t)c->nn * norb));
+  OPAW_CHECK(ensure(c->coef[0], sizeof(double2) * (size_t)c->ns * norb + 16));
+  OPAW_CHECK(ensure(c->coef[1], sizeof(double2) * (size_t)c->ns * norb + 16));
+  C *w = (C *)c->work[0].p;
+  const double2 *cp = cpre;
+  if (!cp) {
+    OPAW_CHECK(gather<R>(c, 0, pin, norb, (double2 *)c->coef[0].p));
+    cp = (const double2 *)c->coef[0].p;
+  }
+  double2 *c1 = (double2 *)c->coef[1].p;
+  if (c->ns > 0) {
+    dim3 g(grid1(c->ns, 128), norb);
+    if (t0)
+      k_coef_dij2<<<g, 128, 0, c->stream>>>(cp, c0, c1, norb, c->ns, c->d_slot_atom, c->d_soff, c->d_doff, c->d_ms,
+                                            dij, ddij);
+    else
+      k_coef_dij<<<g, 128, 0, c->stream>>>(cp, c1, norb, c->ns, c->d_slot_atom, c->d_soff, c->d_doff, c->d_ms, dij);
+    c->launches++;
+    OPAW_CUDA(cudaGetLastError());
+  }
+  Dims3 d{c->nx, c->ny, c->nz};
+  OpCopy<C> x_in{pin, w, c->nn};
+  OpCopy<C> inplace{w, w, c->nn};
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, -1, x_in)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, -1, inplace)));
+  OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, make_kin<R>(c, w))));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, +1, inplace)));
+  OpHFinal<R> fin{w, pin, vks, hp, c->nn, t0, dv};
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, +1, fin)));
   OPAW_CHECK(union_scatter<R>(c, 0, hp, norb, c1));
   return OPAW_OK;
 }
@@ -467,7 +545,9 @@ int shs_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>
   template int union_scatter<R>(opaw_ctx *, int, Tr<R>::C *, int, const double2 *);                 \
   template int h_apply<R>(opaw_ctx *, int, const Tr<R>::C *, Tr<R>::C *, int);                      \
   template int sn_apply<R>(opaw_ctx *, double, const Tr<R>::C *, Tr<R>::C *, int);                  \
-  template int shs_apply<R>(opaw_ctx *, int, const Tr<R>::C *, Tr<R>::C *, int);
+  template int shs_apply<R>(opaw_ctx *, int, const Tr<R>::C *, Tr<R>::C *, int);                    \
+  template int h_apply_ex<R>(opaw_ctx *, const R *, const double *, const Tr<R>::C *, Tr<R>::C *, int,  \
+                             const double2 *, const Tr<R>::C *, const R *, const double2 *, const double *);
 OPAW_INST(float)
 OPAW_INST(double)
 

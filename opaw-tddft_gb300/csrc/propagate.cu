@@ -204,9 +204,12 @@ static int scratch_red(opaw_ctx *c, double **part, double **nrm0, double **nrm1,
   return OPAW_OK;
 }
 
-// one rk4_prop_shs pass over one set (rk4.f90:15-33)
-template <typename R> static int rk4_set(opaw_ctx *c, int set, double dt) {
-  typedef typename Tr<R>::C C;
+// one rk4_prop_shs pass over one set (rk4.f90:15-33), FP64.  Each stage's
+// shs starts from S^-1/2 y and <p~|S^-1/2 y>, which the rebuild that precedes
+// it (the loop-top rebuild for stage 1, rk4.f90:53-55 for the others) has
+// just computed from the same y: the identical values are reused.
+static int rk4_set64(opaw_ctx *c, int set, double dt) {
+  typedef double2 C;
   const int norb = c->norb[set];
   const int64_t tot = c->nn * (int64_t)norb;
   double2 *p = c->d_psi[set];
@@ -217,24 +220,17 @@ template <typename R> static int rk4_set(opaw_ctx *c, int set, double dt) {
   double *part, *nrm0, *nrm1, *dipw;
   OPAW_CHECK(scratch_red(c, &part, &nrm0, &nrm1, &dipw, norb));
   OPAW_CHECK(norms<double2>(c, p, norb, part, nrm0));  // norm0 (rk4.f90:16)
-  const C *pin;
-  if (sizeof(R) == 8) {
-    pin = (const C *)p;
-  } else {
-    k_down<<<grid1(tot, 256), 256, 0, c->stream>>>(p, (float2 *)y, tot);
-    c->launches++;
-    pin = y;
-  }
   const double wts[4] = {1.0, 2.0, 2.0, 1.0};
   const double dts[4] = {dt / 2.0, dt / 2.0, dt, dt};
   for (int st = 0; st < 4; st++) {
-    OPAW_CHECK(shs_apply<R>(c, set, pin, k, norb));
-    k_rk4_stage<R><<<grid1(tot, 256), 256, 0, c->stream>>>(k, p, ks, y, tot, (R)wts[st], st == 0, (R)dts[st],
-                                                          st < 3);
+    // shs (shs.f90:19-22) from the rebuild's S^-1/2 y (work[4]) and projections (coef[0])
+    OPAW_CHECK(h_apply_ex<double>(c, c->d_vks[set], c->d_dij[set], (const C *)c->work[4].p, k, norb,
+                                  (const double2 *)c->coef[0].p, nullptr, nullptr, nullptr, nullptr));
+    OPAW_CHECK(sn_apply<double>(c, -0.5, k, k, norb));
+    k_rk4_stage<double><<<grid1(tot, 256), 256, 0, c->stream>>>(k, p, ks, y, tot, wts[st], st == 0, dts[st], st < 3);
     c->launches++;
     OPAW_CUDA(cudaGetLastError());
-    if (st < 3) OPAW_CHECK(rebuild_from<R>(c, set, y, norb));  // rk4.f90:53-55
-    pin = y;
+    if (st < 3) OPAW_CHECK(rebuild_from<double>(c, set, y, norb));  // rk4.f90:53-55
   }
   k_rk4_final<C><<<grid1(tot, 256), 256, 0, c->stream>>>(p, ks, tot, dt / 6.0);
   c->launches++;
@@ -286,15 +282,16 @@ int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, doub
   OPAW_ARG(nsteps >= 0, "nsteps must be >= 0");
   OPAW_CHECK(ensure(c->work[11], sizeof(double) * (9 * (size_t)(nsteps > 0 ? nsteps : 1) + 16)));
   double *dd = (double *)c->work[11].p;  // 9 values per step: dip, dip_pert, d_dip
-  for (int it = 0; it < nsteps; it++) {
-    OPAW_CHECK(rebuild_resident(c, 0, prec));  // ncpaw_make_hamiltonian_tddft (tddft.f90:75)
-    OPAW_CHECK(rebuild_resident(c, 1, prec));
-    if (prec == OPAW_PREC_FP64) {  // propdt -> rk4_prop_shs (tddft.f90:80)
-      OPAW_CHECK(rk4_set<double>(c, 0, dt));
-      OPAW_CHECK(rk4_set<double>(c, 1, dt));
-    } else {
-      OPAW_CHECK(rk4_set<float>(c, 0, dt));
-      OPAW_CHECK(rk4_set<float>(c, 1, dt));
+  if (prec == OPAW_PREC_MIXED) {
+    OPAW_CHECK(mixed_steps(c, nsteps, dt, gamma, dd));
+  }
+  for (int it = 0; it < nsteps && prec == OPAW_PREC_FP64; it++) {
+    // ncpaw_make_hamiltonian_tddft (tddft.f90:75) and propdt (:80), one set
+    // after the other: the two sets never interact, so this equals the
+    // reference's order (both rebuilds, then both propagations)
+    for (int set = 0; set < 2; set++) {
+      OPAW_CHECK(rebuild_resident(c, set, prec));
+      OPAW_CHECK(rk4_set64(c, set, dt));
     }
     OPAW_CHECK(dipole_dev(c, gamma, dd + 9 * (size_t)it));  // plot_dip (tddft.f90:84)
   }

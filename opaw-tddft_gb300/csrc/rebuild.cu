@@ -385,7 +385,6 @@ __global__ void k_nhat(const int *__restrict__ cpt, const int *__restrict__ csta
 }
 
 // fixed-grid partial sums of two arrays (for the renormalisation)
-constexpr int kRedBlocks = 1024;
 __global__ void k_sum2(const double *__restrict__ a, const double *__restrict__ b, int64_t n, double *__restrict__ part) {
   __shared__ double sh[8];
   double sa = 0, sb = 0;
@@ -557,6 +556,79 @@ int dij_step(opaw_ctx *c, int set) {
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
 }
+
+// ---- pointer-based pieces (used by the perturbation-difference propagation)
+int rhoij_of(opaw_ctx *c, const double2 *coef, int norb, double *out) {
+  if (c->nd == 0) return OPAW_OK;
+  k_rhoij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(coef, norb, c->ns, c->nd, c->d_dslot_atom, c->d_soff, c->d_doff,
+                                                    c->d_ms, out);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+template <typename R> int density_raw(opaw_ctx *c, const typename Tr<R>::C *psit, int norb, double *out) {
+  k_density<typename Tr<R>::C><<<grid1(c->nn, 256), 256, 0, c->stream>>>(psit, norb, c->nn, out);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+template int density_raw<float>(opaw_ctx *, const float2 *, int, double *);
+template int density_raw<double>(opaw_ctx *, const double2 *, int, double *);
+
+// compensation charge of rho_ij without the renormalisation (nhat.f90:13-28)
+int nhat_raw_of(opaw_ctx *c, const double *rhoij, double *out) {
+  OPAW_CHECK(ensure(c->red, sizeof(double) * (2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1) * 2)));
+  double *w = red_scratch(c) + 2 * kRedBlocks + 64;
+  OPAW_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * c->nn, c->stream));
+  if (c->natom > 0 && c->nlmmax > 0) {
+    const int nt = c->natom * c->nlmmax;
+    k_nhat_w<<<grid1(nt, 128), 128, 0, c->stream>>>(rhoij, c->d_qijlm, c->d_ms, c->d_nlm, c->d_doff, c->d_qoff,
+                                                     c->natom, c->nlmmax, w);
+    c->launches++;
+    if (c->ncunion > 0) {
+      k_nhat<<<grid1(c->ncunion, 256), 256, 0, c->stream>>>(c->d_cpt, c->d_cstart, c->d_catom, c->d_cig, c->ncunion,
+                                                            w, c->nlmmax, c->d_ngrid, c->d_nlm, c->d_g3off, c->d_g3d,
+                                                            out);
+      c->launches++;
+    }
+  }
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// partial sums of a and b (kRedBlocks x 2 doubles)
+int sums2(opaw_ctx *c, const double *a, const double *b, double *part) {
+  k_sum2<<<kRedBlocks, 256, 0, c->stream>>>(a, b, c->nn, part);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+int vxc_of(opaw_ctx *c, const double *dens, const double *core, double *out) {
+  k_vxc<<<grid1(c->nn, 256), 256, 0, c->stream>>>(dens, core, out, c->nn);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, double *out) {
+  if (c->natom == 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->red, sizeof(double) * (2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1) * 2)));
+  double *prod = red_scratch(c) + 2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1);
+  const int L = c->nlmmax > 0 ? c->nlmmax : 1;
+  k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(vks, c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off, c->d_g3d, L,
+                                                c->dv, prod);
+  k_dij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(prod, L, rhoij, c->d_qijlm, c->d_dij0, c->d_eijkl, c->d_ms, c->d_nlm,
+                                                  c->d_doff, c->d_qoff, c->d_eoff, c->d_dslot_atom, c->nd, c->dij_max,
+                                                  out);
+  c->launches += 2;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+template int hartree_t<float>(opaw_ctx *, const double *, const double *, double *, double *);
+template int hartree_t<double>(opaw_ctx *, const double *, const double *, double *, double *);
 
 // rebuild from orbitals psi_bar (device, dtype) of `set`: psi~ = S^-1/2 psi_bar,
 // then rho_ij, density, nhat, v_ks, D_ij
