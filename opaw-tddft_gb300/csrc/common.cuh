@@ -64,6 +64,46 @@ template <typename C> __host__ __device__ inline C cmul(C a, C b) {
 template <typename C, typename R> __host__ __device__ inline C cscale(C a, R s) { C r; r.x = a.x * s; r.y = a.y * s; return r; }
 template <typename C> __host__ __device__ inline C cconj(C a) { C r; r.x = a.x; r.y = -a.y; return r; }
 
+#ifdef __CUDACC__
+// IEEE double -> float with round-to-nearest-even done on the integer pipe.
+// GB300 runs 64-bit type conversions at its (low) FP64 rate; the bulk
+// kernels of the mixed path convert every grid point, so they use these.
+// Magnitudes below 2^-126 flush to a signed zero, above FLT_MAX give inf;
+// NaN stays NaN.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned ex = (hi >> 20) & 0x7ffu;
+  if (ex == 0x7ffu) return __uint_as_float(sign | 0x7f800000u | (((hi & 0xfffffu) | lo) ? 0x400000u : 0u));
+  const int e = (int)ex - 1023 + 127;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rest = lo & 0x1fffffffu;
+  unsigned r = sign | ((unsigned)e << 23) | m;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) r += 1u;  // a carry rolls into the exponent
+  return __uint_as_float(r);
+}
+// exact float -> double on the integer pipe (subnormal floats flush to zero)
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  unsigned hi, lo;
+  if (e == 0) {
+    hi = sign;
+    lo = 0;
+  } else if (e == 0xffu) {
+    hi = sign | 0x7ff00000u | (m >> 3);
+    lo = m << 29;
+  } else {
+    hi = sign | ((e + 896u) << 20) | (m >> 3);
+    lo = m << 29;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+#endif
+
 // ---------------------------------------------------------- FFT planning --
 struct FFTAxis {
   int n = 0;
@@ -122,6 +162,8 @@ struct opaw_ctx {
   // union of projector boxes: CSR over grid points
   int nunion = 0, nuent = 0;
   int *d_upt = nullptr, *d_ustart = nullptr, *d_uatom = nullptr, *d_ubox = nullptr;
+  int *d_boxg = nullptr;         // per atom and box point: the wrapped linear grid index
+  int64_t *d_boff = nullptr;     // per atom offset into d_boxg
 
   // compensation charge tables
   int ncomp = 0;             // total sphere points
@@ -166,6 +208,7 @@ struct opaw_ctx {
   // 4 rebuild psi~, 5-6 host-twin staging, 7 RK4 k, 8 RK4 y, 9 RK4 ksum
   opaw::DeviceBuf work[12];
   opaw::DeviceBuf coef[4];       // [norb][ns] double2
+  opaw::DeviceBuf coefr;         // single-precision copy of the scatter coefficients
   opaw::DeviceBuf mix[12];       // buffers of the mixed-precision difference step
   opaw::DeviceBuf red;           // reductions
   double *h_red = nullptr;       // pinned host mirror of small reductions

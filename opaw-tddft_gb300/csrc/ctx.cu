@@ -149,6 +149,13 @@ static int build(opaw_ctx *c, const opaw_system *s) {
           }
     }
     std::stable_sort(ents.begin(), ents.end(), [](const Ent &x, const Ent &y) { return x.g < y.g; });
+    std::vector<int> boxg(ents.size());
+    std::vector<int64_t> boff(na + 1, 0);
+    for (int a = 0; a < na; a++)
+      boff[a + 1] = boff[a] + (int64_t)s->nrough[3 * a] * s->nrough[3 * a + 1] * s->nrough[3 * a + 2];
+    for (const Ent &e : ents) boxg[boff[e.a] + e.b] = (int)e.g;
+    OPAW_CHECK(upload(&c->d_boxg, boxg.data(), boxg.size()));
+    OPAW_CHECK(upload(&c->d_boff, boff.data(), boff.size()));
     std::vector<int> upt, ustart, uatom, ubox;
     for (size_t i = 0; i < ents.size(); i++) {
       if (i == 0 || ents[i].g != ents[i - 1].g) {
@@ -282,6 +289,9 @@ static void destroy(opaw_ctx *c) {
   }
   for (auto &b : c->work) cudaFree(b.p);
   for (auto &b : c->coef) cudaFree(b.p);
+  cudaFree(c->coefr.p);
+  cudaFree(c->d_boxg);
+  cudaFree(c->d_boff);
   for (auto &b : c->mix) cudaFree(b.p);
   cudaFree(c->red.p);
   if (c->h_red) cudaFreeHost(c->h_red);

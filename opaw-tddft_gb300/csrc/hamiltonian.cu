@@ -53,25 +53,24 @@ template <int NV, int LEVEL = 0> struct Halve {
 template <typename R, int MSMAX, int OB>
 __global__ void __launch_bounds__(256) k_gather(const typename Tr<R>::C *__restrict__ psi, int64_t nn, int norb,
                                                 const R *__restrict__ P, const int64_t *__restrict__ poff,
-                                                const int *__restrict__ ir0, const int *__restrict__ nrough,
-                                                const int *__restrict__ ms, const int64_t *__restrict__ soff, int nx,
-                                                int ny, int nz, double dv, double2 *__restrict__ out, int ns) {
+                                                const int *__restrict__ boxg, const int64_t *__restrict__ boff,
+                                                const int *__restrict__ nrough, const int *__restrict__ ms,
+                                                const int64_t *__restrict__ soff, double dv,
+                                                double2 *__restrict__ out, int ns) {
   typedef typename Tr<R>::C C;
   constexpr int NV = OB * MSMAX * 2;  // value index (o * MSMAX + i) * 2 + re/im
   static_assert(NV >= 32 && (NV & (NV - 1)) == 0, "NV must be a power of two >= 32");
   const int a = blockIdx.x;
   const int o0 = blockIdx.y * OB;
   const int m = ms[a];
-  const int n0 = nrough[3 * a], n1 = nrough[3 * a + 1], n2 = nrough[3 * a + 2];
-  const int nbox = n0 * n1 * n2;
-  const int x0 = ir0[3 * a], y0 = ir0[3 * a + 1], z0 = ir0[3 * a + 2];
+  const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+  const int *bg = boxg + boff[a];  // wrapped grid index of each box point (proj.f90:27-37)
   const R *Pa = P + poff[a];
   R v[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) v[k] = 0;
   for (int b = threadIdx.x; b < nbox; b += blockDim.x) {
-    const int bx = b % n0, by = (b / n0) % n1, bz = b / (n0 * n1);
-    const int64_t g = wrapi(x0 + bx, nx) + (int64_t)nx * (wrapi(y0 + by, ny) + (int64_t)ny * wrapi(z0 + bz, nz));
+    const int64_t g = bg[b];
     R p[MSMAX];
 #pragma unroll
     for (int i = 0; i < MSMAX; i++) p[i] = (i < m) ? Pa[(int64_t)i * nbox + b] : (R)0;
@@ -112,15 +111,15 @@ int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, doubl
   if (c->natom == 0) return OPAW_OK;
   const R *P = ProjTab<R>::get(c, which);
   if (c->msmax <= 8) {
-    constexpr int OB = sizeof(R) == 4 ? 4 : 2;
+    constexpr int OB = 2;
     dim3 grid(c->natom, (norb + OB - 1) / OB);
-    k_gather<R, 8, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_ir0, c->d_nrough, c->d_ms,
-                                                    c->d_soff, c->nx, c->ny, c->nz, c->dv, coef, c->ns);
+    k_gather<R, 8, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_boxg, c->d_boff, c->d_nrough,
+                                                    c->d_ms, c->d_soff, c->dv, coef, c->ns);
   } else if (c->msmax <= 16) {
     constexpr int OB = sizeof(R) == 4 ? 2 : 1;
     dim3 grid(c->natom, (norb + OB - 1) / OB);
-    k_gather<R, 16, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_ir0, c->d_nrough, c->d_ms,
-                                                    c->d_soff, c->nx, c->ny, c->nz, c->dv, coef, c->ns);
+    k_gather<R, 16, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_boxg, c->d_boff,
+                                                     c->d_nrough, c->d_ms, c->d_soff, c->dv, coef, c->ns);
   } else {
     set_error("more than 16 projectors per atom");
     return OPAW_ERR_ARG;
@@ -146,7 +145,7 @@ __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__rest
                                                        const int64_t *__restrict__ poff,
                                                        const int *__restrict__ nrough, const int *__restrict__ ms,
                                                        const int64_t *__restrict__ soff,
-                                                       const double2 *__restrict__ coef, int ns) {
+                                                       const typename Tr<R>::C *__restrict__ coef, int ns) {
   typedef typename Tr<R>::C C;
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= nunion) return;
@@ -178,7 +177,7 @@ __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__rest
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         if (o0 + q < ob) {
-          const double2 *co = coef + (int64_t)(o0 + q) * ns;
+          const C *co = coef + (int64_t)(o0 + q) * ns;
           R sx = 0, sy = 0;
 #pragma unroll
           for (int e = 0; e < EMAX; e++) {
@@ -186,9 +185,9 @@ __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__rest
 #pragma unroll
               for (int i = 0; i < MSMAX; i++) {
                 if (i < mm[e]) {
-                  const double2 cf = co[so[e] + i];
-                  sx += pv[e][i] * (R)cf.x;
-                  sy += pv[e][i] * (R)cf.y;
+                  const C cf = co[so[e] + i];
+                  sx += pv[e][i] * cf.x;
+                  sy += pv[e][i] * cf.y;
                 }
               }
             }
@@ -204,18 +203,18 @@ __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__rest
     return;
   }
   for (int o = blockIdx.y * kScatterOrb; o < min(norb, (int)(blockIdx.y + 1) * kScatterOrb); o++) {
-    const double2 *co = coef + (int64_t)o * ns;
+    const C *co = coef + (int64_t)o * ns;
     R sx = 0, sy = 0;
     for (int e = e0; e < e0 + ne; e++) {
       const int a = uatom[e], b = ubox[e];
       const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
       const R *Pa = P + poff[a] + b;
-      const double2 *ca = co + soff[a];
+      const C *ca = co + soff[a];
       const int m = ms[a];
       for (int i = 0; i < m; i++) {
         const R p = Pa[(int64_t)i * nbox];
-        sx += p * (R)ca[i].x;
-        sy += p * (R)ca[i].y;
+        sx += p * ca[i].x;
+        sy += p * ca[i].y;
       }
     }
     C v = dst[(int64_t)o * nn];
@@ -225,19 +224,40 @@ __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__rest
   }
 }
 
+template <typename R> struct CoefIn;
+template <> struct CoefIn<double> {
+  static const double2 *get(opaw_ctx *, const double2 *coef, int) { return coef; }
+};
+__global__ void k_coef_to_f(const double2 *__restrict__ a, float2 *__restrict__ b, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = make_float2(d2f(a[i].x), d2f(a[i].y));
+}
+template <> struct CoefIn<float> {
+  // the scatter's coefficients in single precision, converted once
+  static const float2 *get(opaw_ctx *c, const double2 *coef, int norb) {
+    const int64_t n = (int64_t)c->ns * norb;
+    if (ensure(c->coefr, sizeof(float2) * n + 16) != OPAW_OK) return nullptr;
+    k_coef_to_f<<<grid1(n, 256), 256, 0, c->stream>>>(coef, (float2 *)c->coefr.p, n);
+    c->launches++;
+    return (const float2 *)c->coefr.p;
+  }
+};
+
 template <typename R>
 int union_scatter(opaw_ctx *c, int which, typename Tr<R>::C *out, int norb, const double2 *coef) {
   if (c->nunion == 0) return OPAW_OK;
   const R *P = ProjTab<R>::get(c, which);
+  const typename Tr<R>::C *cf = CoefIn<R>::get(c, coef, norb);
+  if (!cf) return OPAW_ERR_NOMEM;
   const dim3 grid(grid1(c->nunion, 128), (norb + kScatterOrb - 1) / kScatterOrb);
   if (c->msmax <= 8)
     k_union_scatter<R, 2, 8><<<grid, 128, 0, c->stream>>>(out, c->nn, c->nunion, norb, c->d_upt, c->d_ustart,
                                                           c->d_uatom, c->d_ubox, P, c->d_poff, c->d_nrough, c->d_ms,
-                                                          c->d_soff, coef, c->ns);
+                                                          c->d_soff, cf, c->ns);
   else
     k_union_scatter<R, 1, 16><<<grid, 128, 0, c->stream>>>(out, c->nn, c->nunion, norb, c->d_upt, c->d_ustart,
                                                            c->d_uatom, c->d_ubox, P, c->d_poff, c->d_nrough, c->d_ms,
-                                                           c->d_soff, coef, c->ns);
+                                                           c->d_soff, cf, c->ns);
   c->launches++;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;

@@ -50,8 +50,9 @@ __global__ void k_mix_down2(const double2 *__restrict__ p0, const double2 *__res
                             float2 *__restrict__ yd, int64_t n) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  y0[i] = make_float2((float)p0[i].x, (float)p0[i].y);
-  yd[i] = make_float2((float)d[i].x, (float)d[i].y);
+  const double2 a = p0[i], b = d[i];
+  y0[i] = make_float2(d2f(a.x), d2f(a.y));
+  yd[i] = make_float2(d2f(b.x), d2f(b.y));
 }
 
 // difference of rho_ij: 2 sum_occ Re(conj(c0_i) cd_j + conj(cd_i) c0_j + conj(cd_i) cd_j)
@@ -222,8 +223,8 @@ __global__ void k_mix_stage(const float2 *__restrict__ k0r, const float2 *__rest
   ksd[i] = sd;
   if (write_y) {
     const double2 pv = p0[i], dvv = d[i];
-    y0[i] = make_float2((float)pv.x + dts * ax, (float)pv.y + dts * ay);
-    yd[i] = make_float2((float)dvv.x + dts * bx, (float)dvv.y + dts * by);
+    y0[i] = make_float2(d2f(pv.x) + dts * ax, d2f(pv.y) + dts * ay);
+    yd[i] = make_float2(d2f(dvv.x) + dts * bx, d2f(dvv.y) + dts * by);
   }
 }
 
@@ -260,10 +261,10 @@ __global__ void k_mix_final(double2 *__restrict__ p0, double2 *__restrict__ d, c
     const int64_t i = (int64_t)o * nn + g;
     const float2 s0 = ks0[i], sd = ksd[i];
     double2 x = p0[i], y = d[i];
-    x.x += h6 * (double)s0.x;
-    x.y += h6 * (double)s0.y;
-    y.x += h6 * (double)sd.x;
-    y.y += h6 * (double)sd.y;
+    x.x += h6 * f2d(s0.x);
+    x.y += h6 * f2d(s0.y);
+    y.x += h6 * f2d(sd.x);
+    y.y += h6 * f2d(sd.y);
     p0[i] = x;
     d[i] = y;
     A += x.x * x.x + x.y * x.y;

@@ -190,7 +190,10 @@ __global__ void k_rescale(double2 *__restrict__ p, int64_t nn, const double *__r
 
 __global__ void k_down(const double2 *__restrict__ a, float2 *__restrict__ b, int64_t n) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) b[i] = make_float2((float)a[i].x, (float)a[i].y);
+  if (i < n) {
+    const double2 v = a[i];
+    b[i] = make_float2(d2f(v.x), d2f(v.y));
+  }
 }
 
 static int scratch_red(opaw_ctx *c, double **part, double **nrm0, double **nrm1, double **dip, int norb) {
