@@ -209,7 +209,7 @@ struct opaw_ctx {
   opaw::DeviceBuf work[12];
   opaw::DeviceBuf coef[4];       // [norb][ns] double2
   opaw::DeviceBuf coefr;         // single-precision copy of the scatter coefficients
-  opaw::DeviceBuf mix[12];       // buffers of the mixed-precision difference step
+  opaw::DeviceBuf mix[14];       // buffers of the mixed-precision difference step
   opaw::DeviceBuf red;           // reductions
   double *h_red = nullptr;       // pinned host mirror of small reductions
 };

@@ -60,6 +60,19 @@ int fft3d(opaw_ctx *c, const FFT3 &f, typename Tr<R>::C *data, int batch, int si
   typedef typename Tr<R>::C C;
   Dims3 d{f.n[0], f.n[1], f.n[2]};
   OpCopy<C> op{data, data, (int64_t)d.n0 * d.n1 * d.n2};
+  int st;
+  if (sign < 0 && launch_xy_if<C>(c, f, batch, sign, op, &st)) {
+    OPAW_CHECK(st);
+    OPAW_CHECK((launch_axis<C, 2>(c, f.ax[2], d, batch, sign, op)));
+    return OPAW_OK;
+  }
+  if (sign > 0) {
+    OPAW_CHECK((launch_axis<C, 2>(c, f.ax[2], d, batch, sign, op)));
+    if (launch_xy_if<C>(c, f, batch, sign, op, &st)) return st;
+    OPAW_CHECK((launch_axis<C, 1>(c, f.ax[1], d, batch, sign, op)));
+    OPAW_CHECK((launch_axis<C, 0>(c, f.ax[0], d, batch, sign, op)));
+    return OPAW_OK;
+  }
   OPAW_CHECK((launch_axis<C, 0>(c, f.ax[0], d, batch, sign, op)));
   OPAW_CHECK((launch_axis<C, 1>(c, f.ax[1], d, batch, sign, op)));
   OPAW_CHECK((launch_axis<C, 2>(c, f.ax[2], d, batch, sign, op)));

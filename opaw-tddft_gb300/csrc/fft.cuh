@@ -452,6 +452,134 @@ int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const
   return OPAW_OK;
 }
 
+// ------------------------------------------------------------------------
+// XY-plane kernel: one CTA transforms a whole z-plane (nx x ny) of one
+// orbital in shared memory, x lines then y lines (inverse: y then x), so a 3D
+// transform needs this pass plus one z pass instead of three axis passes.
+// The plane is stored [y][x] with an odd row stride; every stage keeps its
+// butterfly inputs in registers between two barriers and writes in place.
+// ------------------------------------------------------------------------
+template <typename C, int N, int NLINES, int LSL, int LSE, int NT, int S>
+__device__ __forceinline__ void xy_stage(C *__restrict__ buf, const C *tw, int sign) {
+  constexpr int R = ct_radix(N, S);
+  constexpr int P = ct_pre(N, S);
+  constexpr int M = N / R;
+  constexpr int TOT = NLINES * M;
+  constexpr int B = (TOT + NT - 1) / NT;
+  constexpr int TSTEP = N / (P * R);
+  C u[B][R];
+#pragma unroll
+  for (int k = 0; k < B; k++) {
+    const int bf = threadIdx.x + k * NT;
+    if (bf < TOT) {
+      const int line = bf % NLINES, i = bf / NLINES;
+#pragma unroll
+      for (int q = 0; q < R; q++) u[k][q] = buf[line * LSL + (i + q * M) * LSE];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < B; k++) {
+    const int bf = threadIdx.x + k * NT;
+    if (bf < TOT) {
+      const int line = bf % NLINES, i = bf / NLINES;
+      const int kk = i % P;
+      if (P > 1) {
+#pragma unroll
+        for (int q = 1; q < R; q++) u[k][q] = cmul(u[k][q], twid(tw, q * kk * TSTEP, sign));
+      }
+      Butterfly<C, R>::run(u[k], tw, N, sign);
+      const int j = (i - kk) * R + kk;
+#pragma unroll
+      for (int q = 0; q < R; q++) buf[line * LSL + (j + q * P) * LSE] = u[k][q];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename C, int N, int NLINES, int LSL, int LSE, int NT, int S> struct XyStages {
+  static __device__ __forceinline__ void run(C *buf, const C *tw, int sign) {
+    if constexpr (S < ct_nstage(N)) {
+      xy_stage<C, N, NLINES, LSL, LSE, NT, S>(buf, tw, sign);
+      XyStages<C, N, NLINES, LSL, LSE, NT, S + 1>::run(buf, tw, sign);
+    }
+  }
+};
+
+template <typename C, int NX, int NY, class Op>
+__global__ void __launch_bounds__(384, 2) k_fft_xy(int sign, const C *__restrict__ twx, const C *__restrict__ twy, Op op) {
+  constexpr int NT = 384;
+  constexpr int LX = NX + 1;  // odd row stride
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *tx = reinterpret_cast<C *>(smem_raw);
+  C *ty = tx + NX;
+  C *pl = ty + NY;
+  for (int t = threadIdx.x; t < NX; t += NT) tx[t] = twx[t];
+  for (int t = threadIdx.x; t < NY; t += NT) ty[t] = twy[t];
+  const int b = blockIdx.y;
+  const int64_t base = (int64_t)blockIdx.x * NX * NY;
+  constexpr int TOT = NX * NY;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < TOT; e += NT) {
+    const int y = e / NX, x = e - y * NX;
+    pl[y * LX + x] = op.load(b, base + e);
+  }
+  __syncthreads();
+  if (sign < 0) {
+    XyStages<C, NX, NY, LX, 1, NT, 0>::run(pl, tx, sign);   // x lines (rows)
+    XyStages<C, NY, NX, 1, LX, NT, 0>::run(pl, ty, sign);   // y lines (columns)
+  } else {
+    XyStages<C, NY, NX, 1, LX, NT, 0>::run(pl, ty, sign);
+    XyStages<C, NX, NY, LX, 1, NT, 0>::run(pl, tx, sign);
+  }
+#pragma unroll 4
+  for (int e = threadIdx.x; e < TOT; e += NT) {
+    const int y = e / NX, x = e - y * NX;
+    op.store(b, base + e, pl[y * LX + x]);
+  }
+}
+
+template <typename C, int NX, int NY, class Op>
+int launch_xy(opaw_ctx *c, const FFTAxis &ax, const FFTAxis &ay, int nz, int batch, int sign, const Op &op) {
+  const size_t smem = sizeof(C) * ((size_t)NX + NY + (size_t)NY * (NX + 1));
+  auto kern = k_fft_xy<C, NX, NY, Op>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error(std::string("xy smem attribute: ") + cudaGetErrorString(e));
+      return OPAW_ERR_CUDA;
+    }
+  }
+  dim3 grid((unsigned)nz, (unsigned)batch);
+  kern<<<grid, 384, smem, c->stream>>>(sign, axis_tw<C>(ax), axis_tw<C>(ay), op);
+  c->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("xy launch: ") + cudaGetErrorString(e));
+    return OPAW_ERR_CUDA;
+  }
+  return OPAW_OK;
+}
+
+// both x and y transforms of every z-plane in one pass when the plane has a
+// specialised kernel (complex64 planes that fit shared memory); returns 1 if
+// it ran, 0 if the caller must run the two axis passes
+template <typename C, class Op>
+int launch_xy_if(opaw_ctx *c, const FFT3 &f, int batch, int sign, const Op &op, int *st) {
+  *st = OPAW_OK;
+  if constexpr (sizeof(C) != 8) {
+    return 0;
+  } else {
+    const int nx = f.n[0], ny = f.n[1], nz = f.n[2];
+    if (nx == 96 && ny == 96) { *st = launch_xy<C, 96, 96>(c, f.ax[0], f.ax[1], nz, batch, sign, op); return 1; }
+    if (nx == 48 && ny == 48) { *st = launch_xy<C, 48, 48>(c, f.ax[0], f.ax[1], nz, batch, sign, op); return 1; }
+    if (nx == 96 && ny == 64) { *st = launch_xy<C, 96, 64>(c, f.ax[0], f.ax[1], nz, batch, sign, op); return 1; }
+    if (nx == 64 && ny == 48) { *st = launch_xy<C, 64, 48>(c, f.ax[0], f.ax[1], nz, batch, sign, op); return 1; }
+    if (nx == 32 && ny == 48) { *st = launch_xy<C, 32, 48>(c, f.ax[0], f.ax[1], nz, batch, sign, op); return 1; }
+    return 0;
+  }
+}
+
 // launch one axis pass over `batch` arrays of dims d
 template <typename C, int AXIS, class Op>
 int launch_axis(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op) {

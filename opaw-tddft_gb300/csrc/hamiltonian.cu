@@ -502,12 +502,21 @@ int h_apply_ex(opaw_ctx *c, const R *vks, const double *dij, const typename Tr<R
   Dims3 d{c->nx, c->ny, c->nz};
   OpCopy<C> x_in{pin, w, c->nn};
   OpCopy<C> inplace{w, w, c->nn};
-  OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, -1, x_in)));
-  OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, -1, inplace)));
-  OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, make_kin<R>(c, w))));
-  OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, +1, inplace)));
   OpHFinal<R> fin{w, pin, vks, hp, c->nn, t0, dv};
-  OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, +1, fin)));
+  int st;
+  if (launch_xy_if<C>(c, c->fft, norb, -1, x_in, &st)) {
+    // three passes: xy planes, z lines with the kinetic factor, xy planes + v_ks psi
+    OPAW_CHECK(st);
+    OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, make_kin<R>(c, w))));
+    launch_xy_if<C>(c, c->fft, norb, +1, fin, &st);
+    OPAW_CHECK(st);
+  } else {
+    OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, -1, x_in)));
+    OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, -1, inplace)));
+    OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, make_kin<R>(c, w))));
+    OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, +1, inplace)));
+    OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, +1, fin)));
+  }
   OPAW_CHECK(union_scatter<R>(c, 0, hp, norb, c1));
   return OPAW_OK;
 }

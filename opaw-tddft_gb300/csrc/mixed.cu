@@ -40,20 +40,7 @@ static __device__ __forceinline__ double bsum(double v, double *sh) {
 }
 
 // ---------------------------------------------------------------- kernels --
-__global__ void k_mix_sub(const double2 *__restrict__ a, const double2 *__restrict__ b, double2 *__restrict__ o,
-                          int64_t n) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) o[i] = make_double2(a[i].x - b[i].x, a[i].y - b[i].y);
-}
 
-__global__ void k_mix_down2(const double2 *__restrict__ p0, const double2 *__restrict__ d, float2 *__restrict__ y0,
-                            float2 *__restrict__ yd, int64_t n) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double2 a = p0[i], b = d[i];
-  y0[i] = make_float2(d2f(a.x), d2f(a.y));
-  yd[i] = make_float2(d2f(b.x), d2f(b.y));
-}
 
 // difference of rho_ij: 2 sum_occ Re(conj(c0_i) cd_j + conj(cd_i) c0_j + conj(cd_i) cd_j)
 __global__ void k_mix_drhoij(const double2 *__restrict__ c0, const double2 *__restrict__ cd, int norb, int ns, int nd,
@@ -200,7 +187,7 @@ __global__ void k_mix_ddij(const double *__restrict__ d0, const double *__restri
 
 // RK4 stage of both sets (rk4.f90:44-48): k = -i shs(y); ksum (+)= w k; y = p + dts k
 __global__ void k_mix_stage(const float2 *__restrict__ k0r, const float2 *__restrict__ kdr,
-                            const double2 *__restrict__ p0, const double2 *__restrict__ d,
+                            const float2 *__restrict__ p0, const float2 *__restrict__ d,
                             float2 *__restrict__ ks0, float2 *__restrict__ ksd, float2 *__restrict__ y0,
                             float2 *__restrict__ yd, int64_t n, float w, int first, float dts, int write_y) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -222,28 +209,55 @@ __global__ void k_mix_stage(const float2 *__restrict__ k0r, const float2 *__rest
   ks0[i] = s0;
   ksd[i] = sd;
   if (write_y) {
-    const double2 pv = p0[i], dvv = d[i];
-    y0[i] = make_float2(d2f(pv.x) + dts * ax, d2f(pv.y) + dts * ay);
-    yd[i] = make_float2(d2f(dvv.x) + dts * bx, d2f(dvv.y) + dts * by);
+    const float2 pv = p0[i], dvv = d[i];
+    y0[i] = make_float2(pv.x + dts * ax, pv.y + dts * ay);
+    yd[i] = make_float2(dvv.x + dts * bx, dvv.y + dts * by);
   }
 }
 
-// norms of both sets in difference form: A = |p0|^2, B = |p0 + d|^2 - |p0|^2
+// Tail of the step.  FP64 arithmetic only where psi and delta are updated;
+// the norms and the dipole take FP32 products of the rounded values, summed
+// in FP32 over chunks of 32 points and in FP64 across chunks (their relative
+// rounding is ~1e-9, far below the FP32 work of the step).
 constexpr int kMixNormBlocks = 64;
-__global__ void k_mix_norm_part(const double2 *__restrict__ p0, const double2 *__restrict__ d, int64_t nn,
-                                double *__restrict__ part) {
+constexpr int kChunk = 32;
+
+struct NormAcc {
+  double A = 0, B = 0;
+  float a = 0.f, b = 0.f;
+  int n = 0;
+  __device__ __forceinline__ void add(float2 x, float2 y) {
+    a += x.x * x.x + x.y * x.y;
+    b += 2.f * (x.x * y.x + x.y * y.y) + y.x * y.x + y.y * y.y;
+    if (++n == kChunk) flush();
+  }
+  __device__ __forceinline__ void flush() {
+    A += f2d(a);
+    B += f2d(b);
+    a = b = 0.f;
+    n = 0;
+  }
+};
+
+// start of a call: delta = psi' - psi, their complex64 copies, norm partials
+__global__ void k_mix_start(const double2 *__restrict__ p0, const double2 *__restrict__ p1, double2 *__restrict__ d,
+                            float2 *__restrict__ pf0, float2 *__restrict__ pfd, int64_t nn,
+                            double *__restrict__ part) {
   __shared__ double sh[8];
   const int o = blockIdx.y;
-  const double2 *a = p0 + (int64_t)o * nn;
-  const double2 *b = d + (int64_t)o * nn;
-  double A = 0, B = 0;
+  NormAcc acc;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
-    const double2 x = a[g], y = b[g];
-    A += x.x * x.x + x.y * x.y;
-    B += 2.0 * (x.x * y.x + x.y * y.y) + y.x * y.x + y.y * y.y;
+    const int64_t i = (int64_t)o * nn + g;
+    const double2 x = p0[i], y1 = p1[i];
+    const double2 y = make_double2(y1.x - x.x, y1.y - x.y);
+    d[i] = y;
+    const float2 xf = make_float2(d2f(x.x), d2f(x.y)), yf = make_float2(d2f(y.x), d2f(y.y));
+    pf0[i] = xf;
+    pfd[i] = yf;
+    acc.add(xf, yf);
   }
-  A = bsum(A, sh);
-  B = bsum(B, sh);
+  acc.flush();
+  const double A = bsum(acc.A, sh), B = bsum(acc.B, sh);
   if (threadIdx.x == 0) {
     part[((int64_t)o * gridDim.x + blockIdx.x) * 2] = A;
     part[((int64_t)o * gridDim.x + blockIdx.x) * 2 + 1] = B;
@@ -256,7 +270,7 @@ __global__ void k_mix_final(double2 *__restrict__ p0, double2 *__restrict__ d, c
                             const float2 *__restrict__ ksd, int64_t nn, double h6, double *__restrict__ part) {
   __shared__ double sh[8];
   const int o = blockIdx.y;
-  double A = 0, B = 0;
+  NormAcc acc;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = (int64_t)o * nn + g;
     const float2 s0 = ks0[i], sd = ksd[i];
@@ -267,11 +281,10 @@ __global__ void k_mix_final(double2 *__restrict__ p0, double2 *__restrict__ d, c
     y.y += h6 * f2d(sd.y);
     p0[i] = x;
     d[i] = y;
-    A += x.x * x.x + x.y * x.y;
-    B += 2.0 * (x.x * y.x + x.y * y.y) + y.x * y.x + y.y * y.y;
+    acc.add(make_float2(d2f(x.x), d2f(x.y)), make_float2(d2f(y.x), d2f(y.y)));
   }
-  A = bsum(A, sh);
-  B = bsum(B, sh);
+  acc.flush();
+  const double A = bsum(acc.A, sh), B = bsum(acc.B, sh);
   if (threadIdx.x == 0) {
     part[((int64_t)o * gridDim.x + blockIdx.x) * 2] = A;
     part[((int64_t)o * gridDim.x + blockIdx.x) * 2 + 1] = B;
@@ -301,69 +314,92 @@ __global__ void k_mix_nfac(const double *__restrict__ part0, const double *__res
   fac[3 * o + 2] = df;
 }
 
-// p0 = f0 p0u; delta = df p0u + f1 du; p1 = p0 + delta
-__global__ void k_mix_rescale(double2 *__restrict__ p0, double2 *__restrict__ d, double2 *__restrict__ p1,
-                              const double *__restrict__ fac, int64_t nn) {
-  const int o = blockIdx.y;
-  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (g >= nn) return;
-  const double f0 = fac[3 * o], f1 = fac[3 * o + 1], df = fac[3 * o + 2];
-  const int64_t i = (int64_t)o * nn + g;
-  const double2 x = p0[i], y = d[i];
-  const double2 a = make_double2(f0 * x.x, f0 * x.y);
-  const double2 b = make_double2(df * x.x + f1 * y.x, df * x.y + f1 * y.y);
-  p0[i] = a;
-  d[i] = b;
-  p1[i] = make_double2(a.x + b.x, a.y + b.y);
-}
-
-// dipole of the unperturbed set and of the density difference
-// (tddft_plot.f90:40-57): dip = sum r rho0 dv, dip' - dip = sum r drho dv
-constexpr int kMixDipBlocks = 512;
-__global__ void k_mix_dip_part(const double2 *__restrict__ p0, const double2 *__restrict__ d, int norb, int64_t nn,
-                               int nx, int ny, int nz, double dx, double dy, double dz, double dv,
-                               double *__restrict__ part) {
+// norm restore p0 = f0 p0u, delta = df p0u + f1 du, fused with what the next
+// step reads first: complex64 copies, norm partials, and the dipole partials
+// of this step (tddft_plot.f90:40-57: dip = sum r rho0 dv, dip' - dip = sum r drho dv)
+__global__ void k_mix_rescale(double2 *__restrict__ p0, double2 *__restrict__ d, float2 *__restrict__ pf0,
+                              float2 *__restrict__ pfd, const double *__restrict__ fac, int64_t nn, int nx, int ny,
+                              int nz, float dx, float dy, float dz, double *__restrict__ npart,
+                              double *__restrict__ dpart) {
   __shared__ double sh[8];
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  const int o = blockIdx.y;
+  const double f0 = fac[3 * o], f1 = fac[3 * o + 1], df = fac[3 * o + 2];
+  NormAcc acc;
+  double D[6] = {0, 0, 0, 0, 0, 0};
+  float Df[6] = {0, 0, 0, 0, 0, 0};
+  int nd = 0;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
-    const int x = (int)(g % nx), y = (int)((g / nx) % ny), z = (int)(g / ((int64_t)nx * ny));
-    const double r[3] = {(double)(x - nx / 2) * dx, (double)(y - ny / 2) * dy, (double)(z - nz / 2) * dz};
-    double rho0 = 0, drho = 0;
-    for (int o = 0; o < norb; o++) {
-      const double2 a = p0[(int64_t)o * nn + g], b = d[(int64_t)o * nn + g];
-      rho0 += a.x * a.x + a.y * a.y;
-      drho += 2.0 * (a.x * b.x + a.y * b.y) + b.x * b.x + b.y * b.y;
-    }
-    rho0 *= 2.0;
-    drho *= 2.0;
+    const int64_t i = (int64_t)o * nn + g;
+    const double2 x = p0[i], y = d[i];
+    const double2 a = make_double2(f0 * x.x, f0 * x.y);
+    const double2 b = make_double2(df * x.x + f1 * y.x, df * x.y + f1 * y.y);
+    p0[i] = a;
+    d[i] = b;
+    const float2 af = make_float2(d2f(a.x), d2f(a.y)), bf = make_float2(d2f(b.x), d2f(b.y));
+    pf0[i] = af;
+    pfd[i] = bf;
+    const float rho = af.x * af.x + af.y * af.y;
+    const float drho = 2.f * (af.x * bf.x + af.y * bf.y) + bf.x * bf.x + bf.y * bf.y;
+    acc.add(af, bf);
+    const int gi = (int)g, gxy = gi / nx;
+    const int gx = gi - gxy * nx, gz = gxy / ny, gy = gxy - gz * ny;
+    const float r[3] = {(float)(gx - nx / 2) * dx, (float)(gy - ny / 2) * dy, (float)(gz - nz / 2) * dz};
+#pragma unroll
     for (int k = 0; k < 3; k++) {
-      acc[k] += dv * r[k] * rho0;
-      acc[3 + k] += dv * r[k] * drho;
+      Df[k] += r[k] * rho;
+      Df[3 + k] += r[k] * drho;
+    }
+    if (++nd == kChunk) {
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        D[k] += f2d(Df[k]);
+        Df[k] = 0.f;
+      }
+      nd = 0;
     }
   }
+  acc.flush();
+#pragma unroll
+  for (int k = 0; k < 6; k++) D[k] += f2d(Df[k]);
+  const double A = bsum(acc.A, sh), B = bsum(acc.B, sh);
+  if (threadIdx.x == 0) {
+    npart[((int64_t)o * gridDim.x + blockIdx.x) * 2] = A;
+    npart[((int64_t)o * gridDim.x + blockIdx.x) * 2 + 1] = B;
+  }
+#pragma unroll
   for (int k = 0; k < 6; k++) {
-    const double s = bsum(acc[k], sh);
-    if (threadIdx.x == 0) part[6 * blockIdx.x + k] = s;
+    const double v = bsum(D[k], sh);
+    if (threadIdx.x == 0) dpart[((int64_t)o * gridDim.x + blockIdx.x) * 6 + k] = v;
   }
 }
 
-__global__ void k_mix_dip_final(const double *__restrict__ part, int nb, double gamma, double *__restrict__ out) {
+// dipoles from the (orbital, block) partials: out[0..2] dip, [3..5] dip', [6..8] d_dip
+__global__ void k_mix_dip_final(const double *__restrict__ part, int nparts, double gamma, double dv,
+                                double *__restrict__ out) {
   if (threadIdx.x != 0) return;
   double s[6] = {0, 0, 0, 0, 0, 0};
-  for (int b = 0; b < nb; b++)
-    for (int k = 0; k < 6; k++) s[k] += part[6 * b + k];
+  for (int b = 0; b < nparts; b++)
+    for (int k = 0; k < 6; k++) s[k] += part[6 * (int64_t)b + k];
   for (int k = 0; k < 3; k++) {
-    out[k] = s[k];
-    out[3 + k] = s[k] + s[3 + k];
-    out[6 + k] = s[3 + k] / gamma;
+    const double dip = 2.0 * dv * s[k], ddip = 2.0 * dv * s[3 + k];  // rho = 2 sum |psi|^2
+    out[k] = dip;
+    out[3 + k] = dip + ddip;
+    out[6 + k] = ddip / gamma;
   }
+}
+
+// psi' = psi + delta (once at the end of a call)
+__global__ void k_mix_p1(const double2 *__restrict__ p0, const double2 *__restrict__ d, double2 *__restrict__ p1,
+                         int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) p1[i] = make_double2(p0[i].x + d[i].x, p0[i].y + d[i].y);
 }
 
 // ----------------------------------------------------------------- driver --
 struct Mix {
   int norb;
   int64_t tot;
-  float2 *y0, *yd, *k0, *kd, *ks0, *ksd, *t0, *td;
+  float2 *y0, *yd, *k0, *kd, *ks0, *ksd, *t0, *td, *pf0, *pfd;
   double2 *d;
   double2 *c0, *cd;
   double *r0raw, *h0raw, *drraw, *dhraw, *src0, *srcd, *ddens, *vh0, *dvh;
@@ -375,25 +411,25 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
   m.norb = norb;
   m.tot = c->nn * (int64_t)norb;
   const size_t cb = sizeof(float2) * (size_t)m.tot;
-  float2 **cs[8] = {&m.y0, &m.yd, &m.k0, &m.kd, &m.ks0, &m.ksd, &m.t0, &m.td};
-  for (int i = 0; i < 8; i++) {
+  float2 **cs[10] = {&m.y0, &m.yd, &m.k0, &m.kd, &m.ks0, &m.ksd, &m.t0, &m.td, &m.pf0, &m.pfd};
+  for (int i = 0; i < 10; i++) {
     OPAW_CHECK(ensure(c->mix[i], cb));
     *cs[i] = (float2 *)c->mix[i].p;
   }
-  OPAW_CHECK(ensure(c->mix[8], sizeof(double2) * (size_t)m.tot));
-  m.d = (double2 *)c->mix[8].p;
-  OPAW_CHECK(ensure(c->mix[9], sizeof(double2) * (size_t)c->ns * norb * 2 + 32));
-  m.c0 = (double2 *)c->mix[9].p;
+  OPAW_CHECK(ensure(c->mix[10], sizeof(double2) * (size_t)m.tot));
+  m.d = (double2 *)c->mix[10].p;
+  OPAW_CHECK(ensure(c->mix[11], sizeof(double2) * (size_t)c->ns * norb * 2 + 32));
+  m.c0 = (double2 *)c->mix[11].p;
   m.cd = m.c0 + (size_t)c->ns * norb;
-  OPAW_CHECK(ensure(c->mix[10], sizeof(double) * (size_t)c->nn * 9 + sizeof(float) * (size_t)c->nn + 64));
-  double *r = (double *)c->mix[10].p;
+  OPAW_CHECK(ensure(c->mix[12], sizeof(double) * (size_t)c->nn * 9 + sizeof(float) * (size_t)c->nn + 64));
+  double *r = (double *)c->mix[12].p;
   double **rs[9] = {&m.r0raw, &m.h0raw, &m.drraw, &m.dhraw, &m.src0, &m.srcd, &m.ddens, &m.vh0, &m.dvh};
   for (int i = 0; i < 9; i++) *rs[i] = r + (size_t)i * c->nn;
   m.dvf = (float *)(r + (size_t)9 * c->nn);
-  const size_t small = 2 * (size_t)c->nd + 16 + 4 * kRedBlocks + 16 + 4 * (size_t)norb * kMixNormBlocks +
-                       3 * (size_t)norb + 6 * kMixDipBlocks + 64;
-  OPAW_CHECK(ensure(c->mix[11], sizeof(double) * small));
-  double *q = (double *)c->mix[11].p;
+  const size_t nparts = (size_t)norb * kMixNormBlocks;
+  const size_t small = 2 * (size_t)c->nd + 16 + 4 * kRedBlocks + 16 + 4 * nparts + 3 * (size_t)norb + 6 * nparts + 64;
+  OPAW_CHECK(ensure(c->mix[13], sizeof(double) * small));
+  double *q = (double *)c->mix[13].p;
   m.drhoij = q;
   m.ddij = m.drhoij + c->nd;
   m.fac = m.ddij + c->nd;
@@ -401,8 +437,8 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
   m.partd = m.part0 + 2 * kRedBlocks;
   m.mean = m.partd + 2 * kRedBlocks;
   m.npart0 = m.mean + 16;
-  m.npart1 = m.npart0 + 2 * (size_t)norb * kMixNormBlocks;
-  m.nfac = m.npart1 + 2 * (size_t)norb * kMixNormBlocks;
+  m.npart1 = m.npart0 + 2 * nparts;
+  m.nfac = m.npart1 + 2 * nparts;
   m.dpart = m.nfac + 3 * (size_t)norb;
   return OPAW_OK;
 }
@@ -415,17 +451,17 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
 
 // rebuild of both sets from y0 and the difference yd: leaves t0 = S^-1/2 y0,
 // td = S^-1/2 yd and their projections c0, cd for the following shs
-static int mix_rebuild(opaw_ctx *c, Mix &m) {
+static int mix_rebuild(opaw_ctx *c, Mix &m, const float2 *y0, const float2 *yd) {
   const int norb = m.norb;
   const int nb = grid1(c->nn, 256);
   // unperturbed set (ncpaw_make_hamiltonian.f90:119-129)
-  OPAW_CHECK(sn_apply<float>(c, -0.5, m.y0, m.t0, norb));
+  OPAW_CHECK(sn_apply<float>(c, -0.5, y0, m.t0, norb));
   OPAW_CHECK(gather<float>(c, 0, m.t0, norb, m.c0));
   OPAW_CHECK(rhoij_of(c, m.c0, norb, c->d_rhoij[0]));
   OPAW_CHECK(density_raw<float>(c, m.t0, norb, m.r0raw));
   OPAW_CHECK(nhat_raw_of(c, c->d_rhoij[0], m.h0raw));
   // differences
-  OPAW_CHECK(sn_apply<float>(c, -0.5, m.yd, m.td, norb));
+  OPAW_CHECK(sn_apply<float>(c, -0.5, yd, m.td, norb));
   OPAW_CHECK(gather<float>(c, 0, m.td, norb, m.cd));
   if (c->nd > 0) {
     k_mix_drhoij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(m.c0, m.cd, norb, c->ns, c->nd, c->d_dslot_atom,
@@ -486,42 +522,33 @@ int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev
   OPAW_CHECK(mix_bufs(c, norb, m));
   const int nb = grid1(m.tot, 256);
   double2 *p0 = c->d_psi[0], *p1 = c->d_psi[1];
-  k_mix_sub<<<nb, 256, 0, c->stream>>>(p1, p0, m.d, m.tot);  // delta = psi' - psi
+  const dim3 gn(kMixNormBlocks, norb);
+  // delta = psi' - psi, complex64 copies, norms of the step start (rk4.f90:16)
+  k_mix_start<<<gn, 256, 0, c->stream>>>(p0, p1, m.d, m.pf0, m.pfd, c->nn, m.npart0);
   MIX_LAUNCHED();
   const float wts[4] = {1.f, 2.f, 2.f, 1.f};
   const double dts[4] = {dt / 2.0, dt / 2.0, dt, dt};
   for (int it = 0; it < nsteps; it++) {
-    k_mix_down2<<<nb, 256, 0, c->stream>>>(p0, m.d, m.y0, m.yd, m.tot);
-    MIX_LAUNCHED();
-    OPAW_CHECK(mix_rebuild(c, m));  // ncpaw_make_hamiltonian_tddft (tddft.f90:75)
-    {
-      dim3 g(kMixNormBlocks, norb);
-      k_mix_norm_part<<<g, 256, 0, c->stream>>>(p0, m.d, c->nn, m.npart0);  // norm0 (rk4.f90:16)
-      MIX_LAUNCHED();
-    }
+    OPAW_CHECK(mix_rebuild(c, m, m.pf0, m.pfd));  // ncpaw_make_hamiltonian_tddft (tddft.f90:75)
     for (int st = 0; st < 4; st++) {
       OPAW_CHECK(mix_shs(c, m));
-      k_mix_stage<<<nb, 256, 0, c->stream>>>(m.k0, m.kd, p0, m.d, m.ks0, m.ksd, m.y0, m.yd, m.tot, wts[st], st == 0,
-                                             (float)dts[st], st < 3);
+      k_mix_stage<<<nb, 256, 0, c->stream>>>(m.k0, m.kd, m.pf0, m.pfd, m.ks0, m.ksd, m.y0, m.yd, m.tot, wts[st],
+                                             st == 0, (float)dts[st], st < 3);
       MIX_LAUNCHED();
-      if (st < 3) OPAW_CHECK(mix_rebuild(c, m));  // rk4.f90:53-55
+      if (st < 3) OPAW_CHECK(mix_rebuild(c, m, m.y0, m.yd));  // rk4.f90:53-55
     }
-    {
-      dim3 g(kMixNormBlocks, norb);
-      k_mix_final<<<g, 256, 0, c->stream>>>(p0, m.d, m.ks0, m.ksd, c->nn, dt / 6.0, m.npart1);
-      MIX_LAUNCHED();
-      k_mix_nfac<<<grid1(norb, 128), 128, 0, c->stream>>>(m.npart0, m.npart1, kMixNormBlocks, norb, m.nfac);
-      MIX_LAUNCHED();
-      dim3 g2(grid1(c->nn, 256), norb);
-      k_mix_rescale<<<g2, 256, 0, c->stream>>>(p0, m.d, p1, m.nfac, c->nn);
-      MIX_LAUNCHED();
-    }
-    k_mix_dip_part<<<kMixDipBlocks, 256, 0, c->stream>>>(p0, m.d, norb, c->nn, c->nx, c->ny, c->nz, c->dx, c->dy,
-                                                         c->dz, c->dv, m.dpart);
+    k_mix_final<<<gn, 256, 0, c->stream>>>(p0, m.d, m.ks0, m.ksd, c->nn, dt / 6.0, m.npart1);
     MIX_LAUNCHED();
-    k_mix_dip_final<<<1, 32, 0, c->stream>>>(m.dpart, kMixDipBlocks, gamma, dd_dev + 9 * (size_t)it);
+    k_mix_nfac<<<grid1(norb, 128), 128, 0, c->stream>>>(m.npart0, m.npart1, kMixNormBlocks, norb, m.nfac);
+    MIX_LAUNCHED();
+    k_mix_rescale<<<gn, 256, 0, c->stream>>>(p0, m.d, m.pf0, m.pfd, m.nfac, c->nn, c->nx, c->ny, c->nz, (float)c->dx,
+                                             (float)c->dy, (float)c->dz, m.npart0, m.dpart);
+    MIX_LAUNCHED();
+    k_mix_dip_final<<<1, 32, 0, c->stream>>>(m.dpart, norb * kMixNormBlocks, gamma, c->dv, dd_dev + 9 * (size_t)it);
     MIX_LAUNCHED();
   }
+  k_mix_p1<<<nb, 256, 0, c->stream>>>(p0, m.d, p1, m.tot);  // psi' = psi + delta
+  MIX_LAUNCHED();
   return OPAW_OK;
 }
 
