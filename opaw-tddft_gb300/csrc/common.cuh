@@ -85,6 +85,24 @@ __device__ __forceinline__ float d2f(double x) {
   if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) r += 1u;  // a carry rolls into the exponent
   return __uint_as_float(r);
 }
+// Fixed-order sum over a block of 256 threads: thread t adds elements
+// t, t+256, ... of a strided sequence, then a shuffle/shared-memory tree.
+// Returns the total in thread 0 (deterministic for a given n).
+__device__ __forceinline__ double block_sum_seq(const double *__restrict__ v, int n, int stride, double *sh) {
+  double acc = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += v[(int64_t)i * stride];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = acc;
+  __syncthreads();
+  double r = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) r += sh[i];
+  return r;
+}
+
 // exact float -> double on the integer pipe (subnormal floats flush to zero)
 __device__ __forceinline__ double f2d(float f) {
   const unsigned u = __float_as_uint(f);

@@ -86,14 +86,12 @@ __global__ void k_mix_drho(const float2 *__restrict__ t0, const float2 *__restri
 // f0 = rnel / S0, f1 = rnel / (S0 + dS), df = f1 - f0 = -rnel dS / (S0 (S0 + dS))
 __global__ void k_mix_factors(const double *__restrict__ p0, const double *__restrict__ pd, int nb, double dv,
                               double rnel, double *__restrict__ fac) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double a = 0, b = 0, c = 0, d = 0;
-  for (int i = 0; i < nb; i++) {
-    a += p0[2 * i];
-    b += p0[2 * i + 1];
-    c += pd[2 * i];
-    d += pd[2 * i + 1];
-  }
+  __shared__ double sh[8];
+  const double a = block_sum_seq(p0, nb, 2, sh);
+  const double b = block_sum_seq(p0 + 1, nb, 2, sh);
+  const double c = block_sum_seq(pd, nb, 2, sh);
+  const double d = block_sum_seq(pd + 1, nb, 2, sh);
+  if (threadIdx.x != 0) return;
   const double S0 = a * dv + b * dv, dS = c * dv + d * dv;
   fac[0] = rnel / S0;
   fac[1] = rnel / (S0 + dS);
@@ -169,12 +167,10 @@ __global__ void k_mix_pot(const double *__restrict__ dens0, const double *__rest
 
 __global__ void k_mix_mean(const double *__restrict__ pa, const double *__restrict__ pb, int nb, int64_t n,
                            double *__restrict__ mean) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double a = 0, b = 0;
-  for (int i = 0; i < nb; i++) {
-    a += pa[2 * i];
-    b += pb[2 * i];
-  }
+  __shared__ double sh[8];
+  const double a = block_sum_seq(pa, nb, 2, sh);
+  const double b = block_sum_seq(pb, nb, 2, sh);
+  if (threadIdx.x != 0) return;
   mean[0] = a / (double)n;
   mean[1] = b / (double)n;
 }
@@ -376,10 +372,10 @@ __global__ void k_mix_rescale(double2 *__restrict__ p0, double2 *__restrict__ d,
 // dipoles from the (orbital, block) partials: out[0..2] dip, [3..5] dip', [6..8] d_dip
 __global__ void k_mix_dip_final(const double *__restrict__ part, int nparts, double gamma, double dv,
                                 double *__restrict__ out) {
+  __shared__ double sh[8];
+  double s[6];
+  for (int k = 0; k < 6; k++) s[k] = block_sum_seq(part + k, nparts, 6, sh);
   if (threadIdx.x != 0) return;
-  double s[6] = {0, 0, 0, 0, 0, 0};
-  for (int b = 0; b < nparts; b++)
-    for (int k = 0; k < 6; k++) s[k] += part[6 * (int64_t)b + k];
   for (int k = 0; k < 3; k++) {
     const double dip = 2.0 * dv * s[k], ddip = 2.0 * dv * s[3 + k];  // rho = 2 sum |psi|^2
     out[k] = dip;
@@ -475,7 +471,7 @@ static int mix_rebuild(opaw_ctx *c, Mix &m, const float2 *y0, const float2 *yd) 
   // charge renormalisation of both sets
   OPAW_CHECK(sums2(c, m.h0raw, m.r0raw, m.part0));
   OPAW_CHECK(sums2(c, m.dhraw, m.drraw, m.partd));
-  k_mix_factors<<<1, 32, 0, c->stream>>>(m.part0, m.partd, kRedBlocks, c->dv, c->rnel, m.fac);
+  k_mix_factors<<<1, 256, 0, c->stream>>>(m.part0, m.partd, kRedBlocks, c->dv, c->rnel, m.fac);
   MIX_LAUNCHED();
   k_mix_renorm<<<nb, 256, 0, c->stream>>>(m.r0raw, m.h0raw, m.drraw, m.dhraw, m.fac, c->d_dens[0], c->d_nhat[0],
                                           c->d_dens[1], c->d_nhat[1], m.src0, m.srcd, m.ddens, c->nn);
@@ -486,7 +482,7 @@ static int mix_rebuild(opaw_ctx *c, Mix &m, const float2 *y0, const float2 *yd) 
   if (c->periodic) {  // tddft_pot.f90:42-45
     OPAW_CHECK(sums2(c, m.vh0, nullptr, m.part0));
     OPAW_CHECK(sums2(c, m.dvh, nullptr, m.partd));
-    k_mix_mean<<<1, 32, 0, c->stream>>>(m.part0, m.partd, kRedBlocks, c->nn, m.mean);
+    k_mix_mean<<<1, 256, 0, c->stream>>>(m.part0, m.partd, kRedBlocks, c->nn, m.mean);
     MIX_LAUNCHED();
     mean = m.mean;
   }
@@ -544,7 +540,7 @@ int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev
     k_mix_rescale<<<gn, 256, 0, c->stream>>>(p0, m.d, m.pf0, m.pfd, m.nfac, c->nn, c->nx, c->ny, c->nz, (float)c->dx,
                                              (float)c->dy, (float)c->dz, m.npart0, m.dpart);
     MIX_LAUNCHED();
-    k_mix_dip_final<<<1, 32, 0, c->stream>>>(m.dpart, norb * kMixNormBlocks, gamma, c->dv, dd_dev + 9 * (size_t)it);
+    k_mix_dip_final<<<1, 256, 0, c->stream>>>(m.dpart, norb * kMixNormBlocks, gamma, c->dv, dd_dev + 9 * (size_t)it);
     MIX_LAUNCHED();
   }
   k_mix_p1<<<nb, 256, 0, c->stream>>>(p0, m.d, p1, m.tot);  // psi' = psi + delta

@@ -86,10 +86,10 @@ __global__ void k_dipole_part(const double2 *__restrict__ p0, const double2 *__r
 
 // out[0..2] dip, [3..5] dip_pert, [6..8] d_dip = (dip_pert - dip)/gamma
 __global__ void k_dipole_final(const double *__restrict__ part, int nb, double gamma, double *__restrict__ out) {
+  __shared__ double sh[8];
+  double s[6];
+  for (int k = 0; k < 6; k++) s[k] = block_sum_seq(part + k, nb, 6, sh);
   if (threadIdx.x != 0) return;
-  double s[6] = {0, 0, 0, 0, 0, 0};
-  for (int b = 0; b < nb; b++)
-    for (int k = 0; k < 6; k++) s[k] += part[6 * b + k];
   for (int k = 0; k < 6; k++) out[k] = s[k];
   for (int k = 0; k < 3; k++) out[6 + k] = (s[3 + k] - s[k]) / gamma;  // tddft_plot.f90:57
 }
@@ -263,7 +263,7 @@ static int dipole_dev(opaw_ctx *c, double gamma, double *out_dev) {
   OPAW_CHECK(scratch_red(c, &part, &n0, &n1, &dipw, c->norb[0]));
   k_dipole_part<<<kDipBlocks, 256, 0, c->stream>>>(c->d_psi[0], c->d_psi[1], c->norb[0], c->nn, c->nx, c->ny, c->nz,
                                                    c->dx, c->dy, c->dz, c->dv, dipw);
-  k_dipole_final<<<1, 32, 0, c->stream>>>(dipw, kDipBlocks, gamma, out_dev);
+  k_dipole_final<<<1, 256, 0, c->stream>>>(dipw, kDipBlocks, gamma, out_dev);
   c->launches += 2;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;

@@ -403,12 +403,10 @@ __global__ void k_sum2(const double *__restrict__ a, const double *__restrict__ 
 // factor = rnel / ((sum nhat + sum dens) * dv)  (nhat.f90:32-37); also the mean of a
 __global__ void k_renorm_factor(const double *__restrict__ part, int nb, double dv, double rnel, int64_t n,
                                 double *__restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double sa = 0, sb = 0;
-  for (int i = 0; i < nb; i++) {
-    sa += part[2 * i];
-    sb += part[2 * i + 1];
-  }
+  __shared__ double sh[8];
+  const double sa = block_sum_seq(part, nb, 2, sh);
+  const double sb = block_sum_seq(part + 1, nb, 2, sh);
+  if (threadIdx.x != 0) return;
   out[0] = rnel / (sa * dv + sb * dv);
   out[1] = sa / (double)n;
 }
@@ -503,7 +501,7 @@ int nhat_step(opaw_ctx *c, int set) {
     }
   }
   k_sum2<<<kRedBlocks, 256, 0, c->stream>>>(c->d_nhat[set], c->d_dens[set], c->nn, part);
-  k_renorm_factor<<<1, 32, 0, c->stream>>>(part, kRedBlocks, c->dv, c->rnel, c->nn, fac);
+  k_renorm_factor<<<1, 256, 0, c->stream>>>(part, kRedBlocks, c->dv, c->rnel, c->nn, fac);
   k_scale2<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_nhat[set], c->d_dens[set], c->nn, fac);
   c->launches += 3;
   OPAW_CUDA(cudaGetLastError());
@@ -531,7 +529,7 @@ int vks_step(opaw_ctx *c, int set, int fp32_hartree) {
     double *part = red_scratch(c);
     double *fac = part + 2 * kRedBlocks;
     k_sum2<<<kRedBlocks, 256, 0, c->stream>>>(c->d_vh[set], nullptr, c->nn, part);
-    k_renorm_factor<<<1, 32, 0, c->stream>>>(part, kRedBlocks, c->dv, 1.0, c->nn, fac);
+    k_renorm_factor<<<1, 256, 0, c->stream>>>(part, kRedBlocks, c->dv, 1.0, c->nn, fac);
     c->launches += 2;
     mean = fac + 1;
   }
