@@ -165,6 +165,26 @@ int opaw_vh(opaw_ctx *ctx, const double *dens, double *vh);
 /* rconv (library_vh_convolution_r8_r2c.f90:13-39) on an arbitrary real grid:
  * gout = 1/N ifft(bk * fft(gin)), host arrays of n0*n1*n2 */
 int opaw_rconv(int n0, int n1, int n2, const double *gin, const double *bk, double *gout);
+/* rconv for callers that cannot allocate device memory (no counterpart in
+ * the reference; it exists because some callers of this library cannot call
+ * cudaMalloc: a host program that fixed its device memory budget at start-up,
+ * code running while a stream is captured into a CUDA graph, or a process
+ * whose allocator a library must not touch).  gin, bk and gout are device
+ * arrays of n0*n1*n2 doubles owned by the caller; the work runs on `stream`
+ * (NULL: the legacy default stream) and the call returns after it finished.
+ * No cudaMalloc, cudaFree or allocating library routine is called: the
+ * scratch is a fixed file-scope device array, so
+ *   - each extent must be <= 256 with prime factors 2, 3, 5, 7 and
+ *     n0*n1*n2 <= 262144 (4 MiB of complex128 scratch, plus 12 KiB of
+ *     twiddles, held by every GPU that loads the library until exit);
+ *     larger sizes are rejected with OPAW_ERR_ARG;
+ *   - the first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) for that device; make that first call before
+ *     any stream capture;
+ *   - all calls share the one scratch array: calls that overlap on the GPU
+ *     (different host threads or streams) race and must not be issued
+ *     concurrently. */
+int opaw_rconv_noalloc(int n0, int n1, int n2, const double *gin, const double *bk, double *gout, void *stream);
 /* LDA v_xc (libxc LDA_X + LDA_C_PW, vxc_libxc.f90:15-23), host arrays */
 int opaw_vxc_lda(opaw_ctx *ctx, const double *dens, double *vxc, int64_t n);
 

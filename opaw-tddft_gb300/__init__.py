@@ -89,6 +89,7 @@ SIGNATURES = {
     "opaw_rebuild": (ct.c_int, [_P, ct.c_int, ct.c_int]),
     "opaw_vh": (ct.c_int, [_P, _P, _P]),
     "opaw_rconv": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, _P, _P, _P]),
+    "opaw_rconv_noalloc": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, _P, _P, _P, _P]),
     "opaw_vxc_lda": (ct.c_int, [_P, _P, _P, ct.c_int64]),
     "opaw_excite": (ct.c_int, [_P, ct.c_int, ct.c_double]),
     "opaw_dipole": (ct.c_int, [_P, ct.c_double, _P, _P, _P]),
