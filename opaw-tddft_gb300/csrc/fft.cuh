@@ -91,7 +91,92 @@ template <typename C> struct Butterfly<C, 8> {
   }
 };
 
-// generic odd radix (3, 5, 7) from the twiddle table: y_s = sum_q u_q W_r^{qs}
+// radix 3 with the constants of W3 = -1/2 + s i sqrt(3)/2
+template <typename C> struct Butterfly<C, 3> {
+  static __device__ __forceinline__ void run(C *u, const C *, int, int sign) {
+    typedef typename CplxOf<C>::R R;
+    const R h3 = (R)0.86602540378443864676372317075294;  // sqrt(3)/2
+    const C t1 = cadd(u[1], u[2]);
+    C t2;
+    t2.x = u[0].x - (R)0.5 * t1.x;
+    t2.y = u[0].y - (R)0.5 * t1.y;
+    const C t3 = cscale(mul_si(csub(u[1], u[2]), sign), h3);
+    u[0] = cadd(u[0], t1);
+    u[1] = cadd(t2, t3);
+    u[2] = csub(t2, t3);
+  }
+};
+
+// radix 6 = 3 x 2: two 3-point DFTs, twiddles W6^c, then 2-point DFTs
+template <typename C> struct Butterfly<C, 6> {
+  static __device__ __forceinline__ void run(C *u, const C *, int, int sign) {
+    typedef typename CplxOf<C>::R R;
+    const R h3 = (R)0.86602540378443864676372317075294;
+    C a[3] = {u[0], u[2], u[4]};
+    C b[3] = {u[1], u[3], u[5]};
+    Butterfly<C, 3>::run(a, nullptr, 0, sign);
+    Butterfly<C, 3>::run(b, nullptr, 0, sign);
+    // W6^1 = 1/2 + s i sqrt3/2, W6^2 = -1/2 + s i sqrt3/2
+    C w1, w2;
+    w1.x = (R)0.5 * b[1].x - sign * h3 * b[1].y;
+    w1.y = (R)0.5 * b[1].y + sign * h3 * b[1].x;
+    w2.x = (R)-0.5 * b[2].x - sign * h3 * b[2].y;
+    w2.y = (R)-0.5 * b[2].y + sign * h3 * b[2].x;
+    u[0] = cadd(a[0], b[0]);
+    u[3] = csub(a[0], b[0]);
+    u[1] = cadd(a[1], w1);
+    u[4] = csub(a[1], w1);
+    u[2] = cadd(a[2], w2);
+    u[5] = csub(a[2], w2);
+  }
+};
+
+// radix 16 = 4 x 4: four 4-point DFTs over q = 4a + b, twiddles W16^{bc},
+// four 4-point DFTs over b
+template <typename C> struct Butterfly<C, 16> {
+  static __device__ __forceinline__ C rot(C z, int e, int sign) {
+    // z * W16^e for e in 0..9 (W16 = exp(s 2 pi i / 16))
+    typedef typename CplxOf<C>::R R;
+    const R c1 = (R)0.92387953251128675612818318939679;  // cos(pi/8)
+    const R s1 = (R)0.38268343236508977172845998403040;  // sin(pi/8)
+    const R h = (R)0.70710678118654752440084436210485;
+    R cr, ci;
+    switch (e) {
+      case 0: return z;
+      case 1: cr = c1; ci = s1; break;
+      case 2: cr = h; ci = h; break;
+      case 3: cr = s1; ci = c1; break;
+      case 4: return mul_si(z, sign);
+      case 6: cr = -h; ci = h; break;
+      case 9: cr = -c1; ci = -s1; break;
+      default: cr = 1; ci = 0; break;
+    }
+    ci *= sign;
+    C r;
+    r.x = z.x * cr - z.y * ci;
+    r.y = z.x * ci + z.y * cr;
+    return r;
+  }
+  static __device__ __forceinline__ void run(C *u, const C *, int, int sign) {
+    C A[4][4];
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      C t[4] = {u[b], u[4 + b], u[8 + b], u[12 + b]};
+      Butterfly<C, 4>::run(t, nullptr, 0, sign);
+#pragma unroll
+      for (int c = 0; c < 4; c++) A[b][c] = rot(t[c], b * c, sign);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      C t[4] = {A[0][c], A[1][c], A[2][c], A[3][c]};
+      Butterfly<C, 4>::run(t, nullptr, 0, sign);
+#pragma unroll
+      for (int d = 0; d < 4; d++) u[c + 4 * d] = t[d];
+    }
+  }
+};
+
+// generic odd radix (5, 7) from the twiddle table: y_s = sum_q u_q W_r^{qs}
 template <typename C, int R> struct Butterfly {
   static __device__ __forceinline__ void run(C *u, const C *tw, int n, int sign) {
     C y[R];
@@ -284,16 +369,16 @@ inline AxisDev axis_dev(const FFTAxis &a) {
 // consecutive lines of the same butterfly, which keeps shared memory free of
 // bank conflicts for every stage and every axis.
 // ------------------------------------------------------------------------
-constexpr int kRadixPref[6] = {8, 4, 2, 3, 5, 7};
+constexpr int kRadixPref[8] = {16, 8, 6, 4, 2, 3, 5, 7};
 constexpr int ct_nstage(int n) {
   int c = 0;
-  for (int k = 0; k < 6; k++)
+  for (int k = 0; k < 8; k++)
     while (n % kRadixPref[k] == 0) { n /= kRadixPref[k]; c++; }
   return n == 1 ? c : -1;
 }
 constexpr int ct_radix(int n, int s) {
   int c = 0;
-  for (int k = 0; k < 6; k++)
+  for (int k = 0; k < 8; k++)
     while (n % kRadixPref[k] == 0) {
       if (c == s) return kRadixPref[k];
       n /= kRadixPref[k];
