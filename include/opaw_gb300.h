@@ -138,6 +138,22 @@ int opaw_proj_dev(opaw_ctx *ctx, int which, int dtype, const void *pin, int norb
  * unnormalised 3D DFT of norb device arrays, sign -1 forward, +1 backward */
 int opaw_fft3d_dev(opaw_ctx *ctx, int dtype, void *data, int norb, int sign);
 
+/* Gram matrix G = dv A^H B of two device orbital batches (the orbital Gram
+ * of orthog_phi.f90:76-111 and the subspace matrices of diag.f90:49-97),
+ * complex128 host output, column-major G[i + na*j] */
+int opaw_gram_dev(opaw_ctx *ctx, int dtype, const void *A, int na, const void *B, int nb, double *G);
+/* subspace rotation out_j = sum_i A_i M[i + na*j] (orthog_phi.f90:148-156,
+ * diag.f90:118); M complex128 host, column-major; out must differ from A */
+int opaw_rotate_dev(opaw_ctx *ctx, int dtype, const void *A, int na, const double *M, int nb, void *out);
+/* orthog_phi (orthog_phi.f90, h_type = 1): canonical orthogonalisation of the
+ * resident orbitals of `set`, Psi <- Psi V diag(l)^-1/2 with G = V diag(l) V^H;
+ * eig (may be NULL) receives the Gram eigenvalues l ascending */
+int opaw_orthog(opaw_ctx *ctx, int set, double *eig);
+/* host-only complex Hermitian eigensolver (cyclic Jacobi) used by
+ * opaw_orthog, replacing EISPACK ch (library_1_matrix_all.f90:351-401):
+ * H (n x n complex128, column-major, overwritten), w ascending, V columns */
+int opaw_herm_eig(int n, double *H, double *w, double *V);
+
 /* ---- host-buffer twins of the operators (Fortran arrays in and out) ---- */
 
 int opaw_h_phi(opaw_ctx *ctx, int set, int dtype, const double *pin, double *hp, int norb);

@@ -78,6 +78,10 @@ SIGNATURES = {
     "opaw_shs_apply_dev": (ct.c_int, [_P, ct.c_int, ct.c_int, _P, _P, ct.c_int]),
     "opaw_proj_dev": (ct.c_int, [_P, ct.c_int, ct.c_int, _P, ct.c_int, _P]),
     "opaw_fft3d_dev": (ct.c_int, [_P, ct.c_int, _P, ct.c_int, ct.c_int]),
+    "opaw_gram_dev": (ct.c_int, [_P, ct.c_int, _P, ct.c_int, _P, ct.c_int, _P]),
+    "opaw_rotate_dev": (ct.c_int, [_P, ct.c_int, _P, ct.c_int, _P, ct.c_int, _P]),
+    "opaw_orthog": (ct.c_int, [_P, ct.c_int, _P]),
+    "opaw_herm_eig": (ct.c_int, [ct.c_int, _P, _P, _P]),
     "opaw_h_phi": (ct.c_int, [_P, ct.c_int, ct.c_int, _P, _P, ct.c_int]),
     "opaw_sn_phi": (ct.c_int, [_P, ct.c_int, ct.c_double, _P, _P, ct.c_int]),
     "opaw_shs": (ct.c_int, [_P, ct.c_int, ct.c_int, _P, _P, ct.c_int]),
@@ -156,6 +160,7 @@ class Context:
             D("dij0", s.dij0), D("eijkl", s.eijkl), s.dij_max,
         )
         self._sys = st
+        self._norb = [0, 0]
         h = ct.c_void_p()
         _check(lib().opaw_dev_init(ct.byref(st), ct.byref(h)))
         self.h = h
@@ -191,6 +196,7 @@ class Context:
         a = _arr(psi, np.complex128)
         norb = a.size // self.nn
         _check(lib().opaw_psi_upload(self.h, set_, _ptr(a), norb))
+        self._norb[set_] = norb
 
     def download(self, set_, norb):
         out = np.empty((norb,) + self.system.shape_f, np.complex128)
@@ -261,6 +267,25 @@ class Context:
     def fft3d_dev(self, dtype, ptr, norb, sign):
         _check(lib().opaw_fft3d_dev(self.h, dtype, ct.c_void_p(ptr), norb, sign))
 
+    def gram_dev(self, dtype, a_ptr, na, b_ptr, nb):
+        out = np.empty((nb, na), np.complex128)  # C order [j][i] == column-major G[i + na j]
+        _check(lib().opaw_gram_dev(self.h, dtype, ct.c_void_p(a_ptr), na, ct.c_void_p(b_ptr), nb, _ptr(out)))
+        return out.T
+
+    def rotate_dev(self, dtype, a_ptr, na, M, out_ptr):
+        Mf = np.asfortranarray(M, dtype=np.complex128)
+        _check(lib().opaw_rotate_dev(self.h, dtype, ct.c_void_p(a_ptr), na, Mf.ctypes.data_as(ct.c_void_p),
+                                     Mf.shape[1], ct.c_void_p(out_ptr)))
+
+    def orthog(self, set_=0):
+        """orthog_phi: canonical orthogonalisation of the resident orbitals."""
+        w = np.empty(self.system_norb(set_))
+        _check(lib().opaw_orthog(self.h, set_, _ptr(w)))
+        return w
+
+    def system_norb(self, set_):
+        return self._norb[set_]
+
     def proj_dev(self, which, dtype, pin_ptr, norb):
         out = np.empty((norb, self.ns), np.complex128)
         _check(lib().opaw_proj_dev(self.h, which, dtype, ct.c_void_p(pin_ptr), norb, _ptr(out)))
@@ -302,6 +327,7 @@ class Context:
     # ---- kick, dipole, propagation
     def excite(self, ipol, gamma):
         _check(lib().opaw_excite(self.h, ipol, float(gamma)))
+        self._norb[1] = self._norb[0]
 
     def dipole(self, gamma):
         d0 = np.zeros(3)
@@ -337,3 +363,14 @@ def rconv(gin, bk):
     out = np.empty_like(g)
     _check(lib().opaw_rconv(n0, n1, n2, _ptr(g), _ptr(b), _ptr(out)))
     return out
+
+
+def herm_eig(H):
+    """Eigenvalues (ascending) and eigenvectors of a complex Hermitian matrix
+    with the library's host Jacobi solver."""
+    A = np.array(H, dtype=np.complex128, order="F", copy=True)
+    n = A.shape[0]
+    w = np.empty(n)
+    V = np.empty((n, n), np.complex128, order="F")
+    _check(lib().opaw_herm_eig(n, A.ctypes.data_as(ct.c_void_p), _ptr(w), V.ctypes.data_as(ct.c_void_p)))
+    return w, V

@@ -227,6 +227,7 @@ struct opaw_ctx {
   opaw::DeviceBuf work[12];
   opaw::DeviceBuf coef[4];       // [norb][ns] double2
   opaw::DeviceBuf coefr;         // single-precision copy of the scatter coefficients
+  opaw::DeviceBuf gram, gramout; // Gram partials, small matrices
   opaw::DeviceBuf mix[14];       // buffers of the mixed-precision difference step
   opaw::DeviceBuf red;           // reductions
   double *h_red = nullptr;       // pinned host mirror of small reductions

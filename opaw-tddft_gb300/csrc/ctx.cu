@@ -290,6 +290,8 @@ static void destroy(opaw_ctx *c) {
   for (auto &b : c->work) cudaFree(b.p);
   for (auto &b : c->coef) cudaFree(b.p);
   cudaFree(c->coefr.p);
+  cudaFree(c->gram.p);
+  cudaFree(c->gramout.p);
   cudaFree(c->d_boxg);
   cudaFree(c->d_boff);
   for (auto &b : c->mix) cudaFree(b.p);

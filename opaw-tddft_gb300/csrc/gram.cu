@@ -1,0 +1,306 @@
+// gram.cu — orbital Gram matrices and subspace rotations (the "sij" / Gram
+// row of the path): G = dv A^H B (orthog_phi.f90:76-111 Gram, diag.f90:78
+// subspace Hamiltonian), Psi <- Psi M (orthog_phi.f90:148-156, diag.f90:118),
+// and the canonical orthogonalisation of the resident orbitals
+// (orthog_phi.f90, h_type = 1: G = V diag(l) V^H, Psi <- Psi V l^-1/2).
+// The small Hermitian eigenproblem runs on the host (cyclic complex Jacobi,
+// deterministic); the reference uses EISPACK `ch` (library_1_matrix_all.f90).
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "fft.cuh"
+
+namespace opaw {
+
+constexpr int kGramTile = 16;   // 16 x 16 output tile per CTA
+constexpr int kGramK = 32;      // grid points per shared-memory sub-block
+constexpr int kGramSplit = 152; // K splits (one wave of CTAs per output tile row)
+
+// part[z][i][j] = sum over the z-th slice of the grid of conj(A_i) B_j,
+// FP32 (or FP64) products summed per 32-point sub-block, FP64 across them
+template <typename R>
+__global__ void __launch_bounds__(256) k_gram(const typename Tr<R>::C *__restrict__ A, int na,
+                                              const typename Tr<R>::C *__restrict__ B, int nb, int64_t nn,
+                                              double2 *__restrict__ part) {
+  typedef typename Tr<R>::C C;
+  __shared__ C sa[kGramTile][kGramK + 1];
+  __shared__ C sb[kGramTile][kGramK + 1];
+  const int ti = threadIdx.x / kGramTile, tj = threadIdx.x % kGramTile;
+  const int i0 = blockIdx.x * kGramTile, j0 = blockIdx.y * kGramTile;
+  const int z = blockIdx.z, nz = gridDim.z;
+  const int64_t k0 = nn * z / nz, k1 = nn * (z + 1) / nz;
+  double accx = 0, accy = 0;
+  for (int64_t kb = k0; kb < k1; kb += kGramK) {
+    for (int e = threadIdx.x; e < kGramTile * kGramK; e += 256) {
+      const int r = e / kGramK, k = e % kGramK;
+      const int64_t g = kb + k;
+      C va, vb;
+      va.x = va.y = vb.x = vb.y = 0;
+      if (g < k1) {
+        if (i0 + r < na) va = A[(int64_t)(i0 + r) * nn + g];
+        if (j0 + r < nb) vb = B[(int64_t)(j0 + r) * nn + g];
+      }
+      sa[r][k] = va;
+      sb[r][k] = vb;
+    }
+    __syncthreads();
+    R sx = 0, sy = 0;
+#pragma unroll 8
+    for (int k = 0; k < kGramK; k++) {
+      const C a = sa[ti][k], b = sb[tj][k];
+      sx += a.x * b.x + a.y * b.y;  // conj(a) b
+      sy += a.x * b.y - a.y * b.x;
+    }
+    accx += (double)sx;
+    accy += (double)sy;
+    __syncthreads();
+  }
+  const int i = i0 + ti, j = j0 + tj;
+  if (i < na && j < nb) part[((int64_t)z * na + i) * nb + j] = make_double2(accx, accy);
+}
+
+// G[i + na j] = dv sum_z part[z][i][j] (fixed order)
+__global__ void k_gram_reduce(const double2 *__restrict__ part, int nz, int na, int nb, double dv,
+                              double2 *__restrict__ G) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= na * nb) return;
+  const int i = t / nb, j = t % nb;
+  double sx = 0, sy = 0;
+  for (int z = 0; z < nz; z++) {
+    const double2 v = part[((int64_t)z * na + i) * nb + j];
+    sx += v.x;
+    sy += v.y;
+  }
+  G[i + (int64_t)na * j] = make_double2(sx * dv, sy * dv);
+}
+
+// out_j = sum_i A_i M[i + na j]: 256 grid points x 16 output orbitals per CTA
+template <typename R>
+__global__ void __launch_bounds__(256) k_rotate(const typename Tr<R>::C *__restrict__ A, int na,
+                                                const double2 *__restrict__ M, int nb, int64_t nn,
+                                                typename Tr<R>::C *__restrict__ out) {
+  typedef typename Tr<R>::C C;
+  __shared__ C sm[kGramTile][kGramTile];
+  const int64_t g = blockIdx.x * (int64_t)256 + threadIdx.x;
+  const int j0 = blockIdx.y * kGramTile;
+  R ax[kGramTile], ay[kGramTile];
+#pragma unroll
+  for (int jj = 0; jj < kGramTile; jj++) ax[jj] = ay[jj] = 0;
+  for (int i0 = 0; i0 < na; i0 += kGramTile) {
+    {
+      const int r = threadIdx.x / kGramTile, q = threadIdx.x % kGramTile;
+      C v;
+      v.x = v.y = 0;
+      if (i0 + r < na && j0 + q < nb) {
+        const double2 d = M[(i0 + r) + (int64_t)na * (j0 + q)];
+        v.x = (R)d.x;
+        v.y = (R)d.y;
+      }
+      sm[r][q] = v;
+    }
+    __syncthreads();
+    if (g < nn) {
+      for (int ii = 0; ii < kGramTile && i0 + ii < na; ii++) {
+        const C a = A[(int64_t)(i0 + ii) * nn + g];
+#pragma unroll
+        for (int jj = 0; jj < kGramTile; jj++) {
+          const C m = sm[ii][jj];
+          ax[jj] += a.x * m.x - a.y * m.y;
+          ay[jj] += a.x * m.y + a.y * m.x;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (g < nn) {
+#pragma unroll
+    for (int jj = 0; jj < kGramTile; jj++) {
+      if (j0 + jj < nb) {
+        C v;
+        v.x = ax[jj];
+        v.y = ay[jj];
+        out[(int64_t)(j0 + jj) * nn + g] = v;
+      }
+    }
+  }
+}
+
+template <typename R>
+int gram_t(opaw_ctx *c, const typename Tr<R>::C *A, int na, const typename Tr<R>::C *B, int nb, double2 *Gdev) {
+  OPAW_CHECK(ensure(c->gram, sizeof(double2) * (size_t)kGramSplit * na * nb + 16));
+  double2 *part = (double2 *)c->gram.p;
+  dim3 grid((na + kGramTile - 1) / kGramTile, (nb + kGramTile - 1) / kGramTile, kGramSplit);
+  k_gram<R><<<grid, 256, 0, c->stream>>>(A, na, B, nb, c->nn, part);
+  k_gram_reduce<<<grid1((int64_t)na * nb, 128), 128, 0, c->stream>>>(part, kGramSplit, na, nb, c->dv, Gdev);
+  c->launches += 2;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+template <typename R>
+int rotate_t(opaw_ctx *c, const typename Tr<R>::C *A, int na, const double2 *Mdev, int nb, typename Tr<R>::C *out) {
+  dim3 grid(grid1(c->nn, 256), (nb + kGramTile - 1) / kGramTile);
+  k_rotate<R><<<grid, 256, 0, c->stream>>>(A, na, Mdev, nb, c->nn, out);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// ---- host: cyclic Jacobi for a complex Hermitian matrix (column-major).
+// On return w holds the eigenvalues ascending and V the eigenvectors.
+void herm_eig(int n, std::vector<std::complex<double>> &H, std::vector<double> &w,
+              std::vector<std::complex<double>> &V) {
+  typedef std::complex<double> cd;
+  auto h = [&](int i, int j) -> cd & { return H[i + (size_t)n * j]; };
+  V.assign((size_t)n * n, cd(0, 0));
+  for (int i = 0; i < n; i++) V[i + (size_t)n * i] = 1.0;
+  double fro = 0;
+  for (auto &x : H) fro += std::norm(x);
+  fro = std::sqrt(fro);
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0;
+    for (int p = 0; p < n; p++)
+      for (int q = p + 1; q < n; q++) off += std::norm(h(p, q));
+    if (std::sqrt(off) <= 1e-15 * (fro > 0 ? fro : 1.0)) break;
+    for (int p = 0; p < n - 1; p++)
+      for (int q = p + 1; q < n; q++) {
+        const cd bpq = h(p, q);
+        const double r = std::abs(bpq);
+        if (r == 0.0) continue;
+        const cd ph = bpq / r;  // e^{i phi}
+        const double a = h(p, p).real(), d = h(q, q).real();
+        const double tau = (d - a) / (2.0 * r);
+        const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+        const double cc = 1.0 / std::sqrt(1.0 + t * t), ss = t * cc;
+        // R = [[c, s], [-s e^{-i phi}, c e^{-i phi}]] on columns p, q
+        const cd em = std::conj(ph);
+        for (int k = 0; k < n; k++) {
+          const cd hp = h(k, p), hq = h(k, q);
+          h(k, p) = cc * hp - ss * em * hq;
+          h(k, q) = ss * hp + cc * em * hq;
+        }
+        for (int k = 0; k < n; k++) {
+          const cd hp = h(p, k), hq = h(q, k);
+          h(p, k) = cc * hp - ss * ph * hq;
+          h(q, k) = ss * hp + cc * ph * hq;
+        }
+        h(p, q) = h(q, p) = 0.0;
+        h(p, p) = h(p, p).real();
+        h(q, q) = h(q, q).real();
+        for (int k = 0; k < n; k++) {
+          const cd vp = V[k + (size_t)n * p], vq = V[k + (size_t)n * q];
+          V[k + (size_t)n * p] = cc * vp - ss * em * vq;
+          V[k + (size_t)n * q] = ss * vp + cc * em * vq;
+        }
+      }
+  }
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; i++) idx[i] = i;
+  std::vector<double> ev(n);
+  for (int i = 0; i < n; i++) ev[i] = h(i, i).real();
+  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return ev[x] < ev[y] || (ev[x] == ev[y] && x < y); });
+  std::vector<cd> Vs((size_t)n * n);
+  w.resize(n);
+  for (int j = 0; j < n; j++) {
+    w[j] = ev[idx[j]];
+    for (int k = 0; k < n; k++) Vs[k + (size_t)n * j] = V[k + (size_t)n * idx[j]];
+  }
+  V.swap(Vs);
+}
+
+}  // namespace opaw
+
+using namespace opaw;
+
+extern "C" {
+
+int opaw_gram_dev(opaw_ctx *c, int dtype, const void *A, int na, const void *B, int nb, double *G) {
+  if (!c || !A || !B || !G || na <= 0 || nb <= 0) {
+    set_error("bad arguments");
+    return OPAW_ERR_ARG;
+  }
+  OPAW_CHECK(ensure(c->gramout, sizeof(double2) * (size_t)na * nb));
+  double2 *Gd = (double2 *)c->gramout.p;
+  if (dtype == OPAW_C128) OPAW_CHECK(gram_t<double>(c, (const double2 *)A, na, (const double2 *)B, nb, Gd));
+  else if (dtype == OPAW_C64) OPAW_CHECK(gram_t<float>(c, (const float2 *)A, na, (const float2 *)B, nb, Gd));
+  else {
+    set_error("dtype must be OPAW_C128 or OPAW_C64");
+    return OPAW_ERR_ARG;
+  }
+  OPAW_CUDA(cudaMemcpyAsync(G, Gd, sizeof(double2) * (size_t)na * nb, cudaMemcpyDeviceToHost, c->stream));
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  return OPAW_OK;
+}
+
+int opaw_rotate_dev(opaw_ctx *c, int dtype, const void *A, int na, const double *M, int nb, void *out) {
+  if (!c || !A || !M || !out || na <= 0 || nb <= 0 || A == out) {
+    set_error("bad arguments (out must differ from A)");
+    return OPAW_ERR_ARG;
+  }
+  OPAW_CHECK(ensure(c->gramout, sizeof(double2) * (size_t)na * nb));
+  double2 *Md = (double2 *)c->gramout.p;
+  OPAW_CUDA(cudaMemcpyAsync(Md, M, sizeof(double2) * (size_t)na * nb, cudaMemcpyHostToDevice, c->stream));
+  if (dtype == OPAW_C128) OPAW_CHECK(rotate_t<double>(c, (const double2 *)A, na, Md, nb, (double2 *)out));
+  else if (dtype == OPAW_C64) OPAW_CHECK(rotate_t<float>(c, (const float2 *)A, na, Md, nb, (float2 *)out));
+  else {
+    set_error("dtype must be OPAW_C128 or OPAW_C64");
+    return OPAW_ERR_ARG;
+  }
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  return OPAW_OK;
+}
+
+int opaw_orthog(opaw_ctx *c, int set, double *eig_out) {
+  if (!c || (set != 0 && set != 1)) {
+    set_error("bad arguments");
+    return OPAW_ERR_ARG;
+  }
+  const int n = c->norb[set];
+  if (n == 0) {
+    set_error("no orbitals uploaded for this set");
+    return OPAW_ERR_STATE;
+  }
+  std::vector<std::complex<double>> G((size_t)n * n), V;
+  OPAW_CHECK(opaw_gram_dev(c, OPAW_C128, c->d_psi[set], n, c->d_psi[set], n, (double *)G.data()));
+  for (int i = 0; i < n; i++)  // exact Hermitian symmetry before the eigensolve
+    for (int j = i + 1; j < n; j++) {
+      const std::complex<double> a = 0.5 * (G[i + (size_t)n * j] + std::conj(G[j + (size_t)n * i]));
+      G[i + (size_t)n * j] = a;
+      G[j + (size_t)n * i] = std::conj(a);
+    }
+  std::vector<double> w;
+  herm_eig(n, G, w, V);
+  for (int j = 0; j < n; j++) {
+    if (!(w[j] > 0)) {
+      set_error("orbitals are linearly dependent (Gram eigenvalue <= 0)");
+      return OPAW_ERR_NONFINITE;
+    }
+    const double f = 1.0 / std::sqrt(w[j]);  // orthog_phi.f90: p1(:,i) / sqrt(eig(i))
+    for (int k = 0; k < n; k++) V[k + (size_t)n * j] *= f;
+  }
+  if (eig_out)
+    for (int j = 0; j < n; j++) eig_out[j] = w[j];
+  OPAW_CHECK(ensure(c->work[7], sizeof(double2) * (size_t)c->nn * n));
+  OPAW_CHECK(opaw_rotate_dev(c, OPAW_C128, c->d_psi[set], n, (const double *)V.data(), n, c->work[7].p));
+  OPAW_CUDA(cudaMemcpyAsync(c->d_psi[set], c->work[7].p, sizeof(double2) * (size_t)c->nn * n,
+                            cudaMemcpyDeviceToDevice, c->stream));
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  return OPAW_OK;
+}
+
+int opaw_herm_eig(int n, double *H, double *w, double *V) {
+  if (n <= 0 || !H || !w || !V) {
+    set_error("bad arguments");
+    return OPAW_ERR_ARG;
+  }
+  std::vector<std::complex<double>> h((std::complex<double> *)H, (std::complex<double> *)H + (size_t)n * n), v;
+  std::vector<double> ww;
+  herm_eig(n, h, ww, v);
+  for (int i = 0; i < n; i++) w[i] = ww[i];
+  std::copy(v.begin(), v.end(), (std::complex<double> *)V);
+  return OPAW_OK;
+}
+
+}  // extern "C"

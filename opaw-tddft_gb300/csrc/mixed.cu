@@ -13,10 +13,9 @@
 //
 // so every complex64 quantity of the kicked set is a difference and keeps its
 // relative precision.  The rebuild forms the density, rho_ij, compensation
-// charge and potential differences directly: Hartree is linear (one complex64
-// transform carries n0 in its real and the difference in its imaginary part),
-// the LDA difference and the charge-renormalisation factors are taken in
-// FP64.  psi, delta, the RK4 accumulation, the norms and the dipole are FP64.
+// charge and potential differences directly: Hartree is linear (the
+// difference density gets its own complex64 transform), the LDA difference
+// and the charge-renormalisation factors are taken in FP64.  psi, delta, the RK4 accumulation, the norms and the dipole are FP64.
 //
 // In exact arithmetic this is the reference algorithm; OPAW_PREC_FP64 runs
 // the reference's own form for comparison.
@@ -476,8 +475,11 @@ static int mix_rebuild(opaw_ctx *c, Mix &m, const float2 *y0, const float2 *yd) 
   k_mix_renorm<<<nb, 256, 0, c->stream>>>(m.r0raw, m.h0raw, m.drraw, m.dhraw, m.fac, c->d_dens[0], c->d_nhat[0],
                                           c->d_dens[1], c->d_nhat[1], m.src0, m.srcd, m.ddens, c->nn);
   MIX_LAUNCHED();
-  // Hartree of n0 + n^0 and of the difference in one complex64 transform
-  OPAW_CHECK(hartree_t<float>(c, m.src0, m.srcd, m.vh0, m.dvh));
+  // Hartree of n0 + n^0 and of the difference: two complex64 transforms, so
+  // the difference keeps its own relative precision (packing it with the
+  // ~1e3 times larger n0 into one transform would round it relative to n0)
+  OPAW_CHECK(hartree_t<float>(c, m.src0, nullptr, m.vh0, nullptr));
+  OPAW_CHECK(hartree_t<float>(c, m.srcd, nullptr, m.dvh, nullptr));
   const double *mean = nullptr;
   if (c->periodic) {  // tddft_pot.f90:42-45
     OPAW_CHECK(sums2(c, m.vh0, nullptr, m.part0));

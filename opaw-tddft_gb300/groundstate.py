@@ -1,0 +1,164 @@
+"""Stationary initial states for the propagation.
+
+A real OPAW-TDDFT run starts from the self-consistent ground state of the
+SCF (main.f90:67-96): the occupied orbitals are eigenvectors of
+S^-1/2 H[rho] S^-1/2, where rho is their own density, so without a kick the
+density does not move and the kicked set carries a small linear response.
+The seeded random orbitals of `synthetic` are far from that regime.  This
+module produces such a state for a synthetic system, using the device
+operators of the library:
+
+* `lowest_states` — Chebyshev-filtered subspace iteration with Rayleigh-Ritz
+  (the reference's chebyr_m.f90 filter, orthog_phi.f90 orthogonalisation and
+  diag.f90 subspace diagonalisation), for the lowest eigenvectors of
+  S^-1/2 H0 S^-1/2 with H0 = T + v_ks0 + sum p~ D0 <p~|;
+* `stationary_system` — rebuilds rho, n^, v_ks and D_ij from those orbitals
+  and shifts v_loc and D0 so that the rebuilt Hamiltonian is exactly H0: the
+  orbitals are then an exact stationary state of the TDDFT Hamiltonian.
+
+Device memory is handled with torch tensors (plumbing); every operator runs
+in libopaw_gb300.so.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+import opaw_tddft_gb300 as pkg
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _shs(ctx, dtype, X, Y):
+    norb = X.shape[0]
+    ctx.shs_apply_dev(0, dtype, X.data_ptr(), Y.data_ptr(), norb)
+    ctx.sync()
+
+
+def _orthonormalise(ctx, dtype, X, scratch):
+    """X <- X G^-1/2 (canonical orthogonalisation, orthog_phi.f90)."""
+    norb = X.shape[0]
+    G = ctx.gram_dev(dtype, X.data_ptr(), norb, X.data_ptr(), norb)
+    G = 0.5 * (G + G.conj().T)
+    w, V = np.linalg.eigh(G)
+    if w.min() <= 0:
+        raise RuntimeError("subspace lost rank")
+    ctx.rotate_dev(dtype, X.data_ptr(), norb, V / np.sqrt(w)[None, :], scratch.data_ptr())
+    X.copy_(scratch)
+
+
+def _rayleigh_ritz(ctx, dtype, X, HX, scratch):
+    """Subspace diagonalisation (diag.f90): X <- X V, HX <- HX V."""
+    norb = X.shape[0]
+    Hs = ctx.gram_dev(dtype, X.data_ptr(), norb, HX.data_ptr(), norb)
+    Hs = 0.5 * (Hs + Hs.conj().T)
+    w, V = np.linalg.eigh(Hs)
+    ctx.rotate_dev(dtype, X.data_ptr(), norb, V, scratch.data_ptr())
+    X.copy_(scratch)
+    ctx.rotate_dev(dtype, HX.data_ptr(), norb, V, scratch.data_ptr())
+    HX.copy_(scratch)
+    return w
+
+
+def _residuals(X, HX, w, dv):
+    torch = _torch()
+    ww = torch.as_tensor(w, device=X.device, dtype=torch.float64).to(X.real.dtype)
+    R = HX - X * ww[:, None]
+    return torch.sqrt((R.abs() ** 2).sum(dim=1).double() * dv).cpu().numpy()
+
+
+def lowest_states(ctx, psi0, n_iter=30, degree=10, tol=1e-4, fp64_polish=4, verbose=False):
+    """Lowest eigenpairs of S^-1/2 H S^-1/2 (set 0's v_ks and D_ij) starting
+    from the orbitals psi0 [norb, nn].  FP32 Chebyshev-filtered subspace
+    iteration until the largest residual is below tol, then `fp64_polish`
+    FP64 Rayleigh-Ritz / residual-correction sweeps.  Returns (eigenvalues,
+    orbitals complex128 [norb, nn], residual norms)."""
+    torch = _torch()
+    dv = ctx.system.dv
+    norb = psi0.shape[0]
+    dt32 = pkg.OPAW_C64
+    X = torch.from_numpy(np.ascontiguousarray(psi0, dtype=np.complex64)).to("cuda")
+    HX = torch.empty_like(X)
+    Y0 = torch.empty_like(X)
+    Y1 = torch.empty_like(X)
+    S = torch.empty_like(X)
+    _orthonormalise(ctx, dt32, X, S)
+    # upper spectral bound: power iteration on one vector
+    v = X[:1].clone()
+    hv = torch.empty_like(v)
+    lam_max = 0.0
+    for _ in range(30):
+        _shs(ctx, dt32, v, hv)
+        lam_max = float(torch.sqrt((hv.abs() ** 2).sum() / (v.abs() ** 2).sum()))
+        v = hv / hv.abs().max()
+    lam_max *= 1.05
+    _shs(ctx, dt32, X, HX)
+    w = _rayleigh_ritz(ctx, dt32, X, HX, S)
+    for it in range(n_iter):
+        res = _residuals(X, HX, w, dv)
+        if verbose:
+            print(f"chebyshev iteration {it}: eig[0]={w[0]:.6f} eig[-1]={w[-1]:.6f} max residual {res.max():.3e}")
+        if res.max() < tol:
+            break
+        # scaled Chebyshev filter damping [a, lam_max] (chebyr_m.f90:20-45)
+        a = float(w[-1]) + 0.1 * (float(w[-1]) - float(w[0]) + 1e-3)
+        b = lam_max
+        e = 0.5 * (b + a)
+        h = 0.5 * (b - a)
+        sigma = h / (float(w[0]) - e)
+        sigma1 = sigma
+        _shs(ctx, dt32, X, Y1)
+        Y1.sub_(e * X).mul_(sigma1 / h)
+        Y0.copy_(X)
+        for _k in range(2, degree + 1):
+            sigma2 = 1.0 / (2.0 / sigma1 - sigma)
+            _shs(ctx, dt32, Y1, HX)
+            HX.sub_(e * Y1).mul_(2.0 * sigma2 / h).sub_((sigma * sigma2) * Y0)
+            Y0, Y1, HX = Y1, HX, Y0
+            sigma = sigma2
+        X.copy_(Y1)
+        _orthonormalise(ctx, dt32, X, S)
+        _shs(ctx, dt32, X, HX)
+        w = _rayleigh_ritz(ctx, dt32, X, HX, S)
+    # FP64 polish: Rayleigh-Ritz on [X, residual] pairs, orthonormalised
+    X64 = X.to(torch.complex128)
+    H64 = torch.empty_like(X64)
+    S64 = torch.empty_like(X64)
+    dt64 = pkg.OPAW_C128
+    _orthonormalise(ctx, dt64, X64, S64)
+    _shs(ctx, dt64, X64, H64)
+    w = _rayleigh_ritz(ctx, dt64, X64, H64, S64)
+    for _ in range(fp64_polish):
+        ww = torch.as_tensor(w, device="cuda", dtype=torch.float64)
+        R = H64 - X64 * ww[:, None]
+        # one block-Jacobi-like correction step x <- x - r / (lam_max - eps) keeps the order
+        X64.sub_(R / (lam_max - ww[:, None]))
+        _orthonormalise(ctx, dt64, X64, S64)
+        _shs(ctx, dt64, X64, H64)
+        w = _rayleigh_ritz(ctx, dt64, X64, H64, S64)
+    res = _residuals(X64, H64, w, dv)
+    return w, X64.cpu().numpy(), res
+
+
+def stationary_system(system, psi):
+    """Shift v_loc and D0 of `system` so that the Hamiltonian rebuilt from the
+    orbitals psi (rho_ij, density, n^, v_H, v_xc, D_ij of tddft_rhoij.f90,
+    tddft_dens.f90, nhat.f90, tddft_pot.f90, get_dij.f90) equals
+    v_ks = system.vks0 and D = system.dij_init.  Returns a new System."""
+    target_v = np.asarray(system.vks0, np.float64)
+    target_d = np.asarray(system.dij_init, np.float64)
+    s1 = system
+    for _ in range(2):  # v_loc first (it changes Dhat), then D0
+        ctx = pkg.Context(s1)
+        ctx.upload(0, psi)
+        ctx.rebuild(0, pkg.PREC_FP64)
+        vks = ctx.get_vks(0)
+        dij = ctx.get_dij(0)
+        ctx.close()
+        s1 = dataclasses.replace(s1, vloc=s1.vloc + (target_v - vks), dij0=s1.dij0 + (target_d - dij))
+    return s1

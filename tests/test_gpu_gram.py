@@ -1,0 +1,101 @@
+"""GPU tests of the Gram / subspace-rotation row (orthog_phi.f90, diag.f90)
+and of the stationary ground states built with it."""
+import numpy as np
+import pytest
+
+import opaw_tddft_gb300 as pkg
+from opaw_tddft_gb300 import groundstate, synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.fixture(scope="module")
+def spec():
+    s = synthetic.small_system("spec", norb=6)
+    c = pkg.Context(s)
+    c.set_vks(0, s.vks0)
+    c.set_dij(0, s.dij_init)
+    yield s, c
+    c.close()
+
+
+def test_gram_and_rotate(spec):
+    torch = pytest.importorskip("torch")
+    s, c = spec
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((6, s.nn)) + 1j * rng.standard_normal((6, s.nn))
+    B = rng.standard_normal((5, s.nn)) + 1j * rng.standard_normal((5, s.nn))
+    ref = A.conj() @ B.T * s.dv
+    for dtype, tdt, tol in [(pkg.OPAW_C128, torch.complex128, 1e-12), (pkg.OPAW_C64, torch.complex64, 1e-5)]:
+        a = torch.from_numpy(A).to(tdt).cuda()
+        b = torch.from_numpy(B).to(tdt).cuda()
+        G = c.gram_dev(dtype, a.data_ptr(), 6, b.data_ptr(), 5)
+        assert rel(G, ref) < tol
+        M = rng.standard_normal((6, 3)) + 1j * rng.standard_normal((6, 3))
+        out = torch.empty((3, s.nn), dtype=tdt, device="cuda")
+        c.rotate_dev(dtype, a.data_ptr(), 6, M, out.data_ptr())
+        assert rel(out.cpu().numpy(), M.T @ A) < tol
+
+
+def test_orthog_canonical(spec):
+    s, c = spec
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((6, s.nn)) + 1j * rng.standard_normal((6, s.nn))
+    c.upload(0, A)
+    w = c.orthog(0)
+    G0 = A.conj() @ A.T * s.dv
+    assert np.allclose(w, np.linalg.eigvalsh(G0), rtol=1e-11)
+    X = c.download(0, 6).reshape(6, -1)
+    assert np.abs(X.conj() @ X.T * s.dv - np.eye(6)).max() < 1e-12
+    # same span: the projector onto span(A) reproduces X
+    Q, _ = np.linalg.qr(A.T)
+    assert np.abs(Q @ (Q.conj().T @ X.T) - X.T).max() < 1e-10 * np.abs(X).max()
+
+
+def test_stationary_ground_state():
+    """Chebyshev subspace iteration + the v_loc / D0 shift give an exact
+    stationary state: without a kick the density does not move."""
+    s = synthetic.small_system("spec", norb=4)
+    c = pkg.Context(s)
+    c.set_vks(0, s.vks0)
+    c.set_dij(0, s.dij_init)
+    w, psi, res = groundstate.lowest_states(c, synthetic.orbitals(s, 4, seed=8).reshape(4, -1), n_iter=60, tol=1e-5)
+    c.close()
+    assert res.max() < 1e-6, res
+    s2 = groundstate.stationary_system(s, psi)
+    c = pkg.Context(s2)
+    c.upload(0, psi)
+    c.rebuild(0, pkg.PREC_FP64)
+    assert rel(c.get_vks(0), s.vks0) < 1e-12
+    assert rel(c.get_dij(0), s.dij_init) < 1e-11
+    rho0 = c.get_density(0)
+    c.excite(1, 0.0)
+    c.tddft_steps(5, 0.05, 1e-3, pkg.PREC_FP64)
+    c.rebuild(0, pkg.PREC_FP64)
+    assert rel(c.get_density(0), rho0) < 1e-5
+    c.close()
+
+
+def test_mixed_dipole_on_stationary_state():
+    """The mixed-precision signal against FP64 from a stationary ground state
+    (the regime of a real run): relative error <= 1e-6 over 20 steps."""
+    s = synthetic.small_system("spec", norb=4)
+    c = pkg.Context(s)
+    c.set_vks(0, s.vks0)
+    c.set_dij(0, s.dij_init)
+    w, psi, res = groundstate.lowest_states(c, synthetic.orbitals(s, 4, seed=8).reshape(4, -1), n_iter=60, tol=1e-5)
+    c.close()
+    s2 = groundstate.stationary_system(s, psi)
+    c = pkg.Context(s2)
+    out = {}
+    for prec in (pkg.PREC_FP64, pkg.PREC_MIXED):
+        c.upload(0, psi)
+        c.excite(1, 1e-3)
+        out[prec] = c.tddft_steps(20, 0.05, 1e-3, prec)[:, 0]
+    err = np.abs(out[pkg.PREC_MIXED] - out[pkg.PREC_FP64]).max() / np.abs(out[pkg.PREC_FP64]).max()
+    assert err < 1e-6, err
+    c.close()
