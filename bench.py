@@ -315,8 +315,10 @@ def main():
         c0 = pkg.Context(s)
         c0.set_vks(0, s.vks0)
         c0.set_dij(0, s.dij_init)
-        w, psi0, res = groundstate.lowest_states(c0, psi0, n_iter=60, tol=1e-4)
+        w, psi0, res = groundstate.lowest_states(c0, psi0, n_iter=80, tol=1e-4)
         c0.close()
+        if not res.max() < 1e-3:
+            raise RuntimeError(f"ground state did not converge: max eigen-residual {res.max():.3e}")
         s = groundstate.stationary_system(s, psi0)
         state = {"initial_state": "stationary ground state: lowest eigenvectors of S^-1/2 H S^-1/2 by Chebyshev "
                                   "subspace iteration, v_loc/D0 shifted so H[rho(psi)] is that Hamiltonian",

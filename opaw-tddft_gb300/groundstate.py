@@ -72,42 +72,56 @@ def _residuals(X, HX, w, dv):
     return torch.sqrt((R.abs() ** 2).sum(dim=1).double() * dv).cpu().numpy()
 
 
-def lowest_states(ctx, psi0, n_iter=30, degree=10, tol=1e-4, fp64_polish=4, verbose=False):
+def lowest_states(ctx, psi0, n_iter=60, degree=10, tol=1e-4, fp64_polish=4, nbuf=None, seed=0, verbose=False):
     """Lowest eigenpairs of S^-1/2 H S^-1/2 (set 0's v_ks and D_ij) starting
     from the orbitals psi0 [norb, nn].  FP32 Chebyshev-filtered subspace
-    iteration until the largest residual is below tol, then `fp64_polish`
-    FP64 Rayleigh-Ritz / residual-correction sweeps.  Returns (eigenvalues,
-    orbitals complex128 [norb, nn], residual norms)."""
+    iteration on norb + nbuf vectors (the buffer vectors converge last and are
+    dropped) until the largest residual of the wanted ones is below tol, then
+    `fp64_polish` FP64 correction / Rayleigh-Ritz sweeps.  Returns
+    (eigenvalues, orbitals complex128 [norb, nn], residual norms)."""
     torch = _torch()
     dv = ctx.system.dv
+    nn = ctx.nn
     norb = psi0.shape[0]
+    if nbuf is None:
+        nbuf = max(4, norb // 8)
+    nsub = norb + nbuf
     dt32 = pkg.OPAW_C64
-    X = torch.from_numpy(np.ascontiguousarray(psi0, dtype=np.complex64)).to("cuda")
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+
+    def noise(n):
+        return torch.complex(torch.randn(n, nn, device="cuda", generator=gen),
+                             torch.randn(n, nn, device="cuda", generator=gen))
+
+    X = torch.empty((nsub, nn), dtype=torch.complex64, device="cuda")
+    X[:norb] = torch.from_numpy(np.ascontiguousarray(psi0, dtype=np.complex64)).to("cuda")
+    X[norb:] = noise(nbuf)
     HX = torch.empty_like(X)
     Y0 = torch.empty_like(X)
     Y1 = torch.empty_like(X)
     S = torch.empty_like(X)
     _orthonormalise(ctx, dt32, X, S)
-    # upper spectral bound: power iteration on one vector
-    v = X[:1].clone()
+    # upper spectral bound: power iteration from white noise (all k present)
+    v = noise(1)
     hv = torch.empty_like(v)
     lam_max = 0.0
-    for _ in range(30):
+    for _ in range(40):
+        v = v / torch.sqrt((v.abs() ** 2).sum())
         _shs(ctx, dt32, v, hv)
-        lam_max = float(torch.sqrt((hv.abs() ** 2).sum() / (v.abs() ** 2).sum()))
-        v = hv / hv.abs().max()
-    lam_max *= 1.05
+        lam_max = float(torch.sqrt((hv.abs() ** 2).sum()))
+        v = hv
+    lam_max *= 1.2
     _shs(ctx, dt32, X, HX)
     w = _rayleigh_ritz(ctx, dt32, X, HX, S)
     for it in range(n_iter):
-        res = _residuals(X, HX, w, dv)
+        res = _residuals(X[:norb], HX[:norb], w[:norb], dv)
         if verbose:
-            print(f"chebyshev iteration {it}: eig[0]={w[0]:.6f} eig[-1]={w[-1]:.6f} max residual {res.max():.3e}")
+            print(f"chebyshev iteration {it}: eig[0]={w[0]:.6f} eig[norb-1]={w[norb - 1]:.6f} max residual {res.max():.3e}")
         if res.max() < tol:
             break
         # scaled Chebyshev filter damping [a, lam_max] (chebyr_m.f90:20-45)
-        a = float(w[-1]) + 0.1 * (float(w[-1]) - float(w[0]) + 1e-3)
-        b = lam_max
+        a = float(w[-1])
+        b = max(lam_max, a + 1.0)
         e = 0.5 * (b + a)
         h = 0.5 * (b - a)
         sigma = h / (float(w[0]) - e)
@@ -125,8 +139,8 @@ def lowest_states(ctx, psi0, n_iter=30, degree=10, tol=1e-4, fp64_polish=4, verb
         _orthonormalise(ctx, dt32, X, S)
         _shs(ctx, dt32, X, HX)
         w = _rayleigh_ritz(ctx, dt32, X, HX, S)
-    # FP64 polish: Rayleigh-Ritz on [X, residual] pairs, orthonormalised
-    X64 = X.to(torch.complex128)
+    # FP64 polish of the wanted vectors
+    X64 = X[:norb].to(torch.complex128)
     H64 = torch.empty_like(X64)
     S64 = torch.empty_like(X64)
     dt64 = pkg.OPAW_C128
@@ -136,12 +150,13 @@ def lowest_states(ctx, psi0, n_iter=30, degree=10, tol=1e-4, fp64_polish=4, verb
     for _ in range(fp64_polish):
         ww = torch.as_tensor(w, device="cuda", dtype=torch.float64)
         R = H64 - X64 * ww[:, None]
-        # one block-Jacobi-like correction step x <- x - r / (lam_max - eps) keeps the order
         X64.sub_(R / (lam_max - ww[:, None]))
         _orthonormalise(ctx, dt64, X64, S64)
         _shs(ctx, dt64, X64, H64)
         w = _rayleigh_ritz(ctx, dt64, X64, H64, S64)
     res = _residuals(X64, H64, w, dv)
+    if not np.all(np.isfinite(res)):
+        raise RuntimeError("ground-state iteration produced non-finite orbitals")
     return w, X64.cpu().numpy(), res
 
 
