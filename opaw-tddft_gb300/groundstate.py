@@ -93,9 +93,22 @@ def lowest_states(ctx, psi0, n_iter=60, degree=10, tol=1e-4, fp64_polish=4, nbuf
         return torch.complex(torch.randn(n, nn, device="cuda", generator=gen),
                              torch.randn(n, nn, device="cuda", generator=gen))
 
+    def smooth_noise(n):
+        # Gaussian-filtered noise (sigma = 1.5 Bohr), like the seed orbitals:
+        # low Ritz values, so the buffer does not push the filter cut up
+        s = ctx.system
+        z = noise(n).reshape(n, s.nz, s.ny, s.nx)
+        kx = 2 * np.pi * np.fft.fftfreq(s.nx, s.dx)
+        ky = 2 * np.pi * np.fft.fftfreq(s.ny, s.dy)
+        kz = 2 * np.pi * np.fft.fftfreq(s.nz, s.dz)
+        k2 = kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2
+        filt = torch.from_numpy(np.exp(-k2 * 1.5 * 1.5 / 2.0).astype(np.float32)).to("cuda")
+        z = torch.fft.ifftn(torch.fft.fftn(z, dim=(1, 2, 3)) * filt, dim=(1, 2, 3))
+        return z.reshape(n, nn).to(torch.complex64)
+
     X = torch.empty((nsub, nn), dtype=torch.complex64, device="cuda")
     X[:norb] = torch.from_numpy(np.ascontiguousarray(psi0, dtype=np.complex64)).to("cuda")
-    X[norb:] = noise(nbuf)
+    X[norb:] = smooth_noise(nbuf)
     HX = torch.empty_like(X)
     Y0 = torch.empty_like(X)
     Y1 = torch.empty_like(X)
@@ -126,10 +139,17 @@ def lowest_states(ctx, psi0, n_iter=60, degree=10, tol=1e-4, fp64_polish=4, nbuf
         h = 0.5 * (b - a)
         sigma = h / (float(w[0]) - e)
         sigma1 = sigma
+        # degree capped so the filter amplifies the lowest Ritz direction at
+        # most ~300x over the cut: the filtered block stays well conditioned
+        # for single-precision orthonormalisation
+        x0 = (e - float(w[0])) / h
+        m = degree
+        if x0 > 1.0:
+            m = int(max(2, min(degree, np.floor(np.arccosh(300.0) / np.arccosh(x0)))))
         _shs(ctx, dt32, X, Y1)
         Y1.sub_(e * X).mul_(sigma1 / h)
         Y0.copy_(X)
-        for _k in range(2, degree + 1):
+        for _k in range(2, m + 1):
             sigma2 = 1.0 / (2.0 / sigma1 - sigma)
             _shs(ctx, dt32, Y1, HX)
             HX.sub_(e * Y1).mul_(2.0 * sigma2 / h).sub_((sigma * sigma2) * Y0)

@@ -318,9 +318,11 @@ def orbitals(sysobj: System, norb: int, seed: int = 11, sigma: float = 1.5, chun
     flat = psi.reshape(norb, -1)
     dv = sysobj.dv
     for _ in range(2):
+        # rows are orbitals: G = conj(Psi) Psi^T dv = L L^H, so conj(L)^-1 Psi
+        # has the identity as its Gram matrix
         G = (flat.conj() @ flat.T) * dv
         Lc = np.linalg.cholesky(G)
-        flat[:] = np.linalg.solve(Lc, flat)
+        flat[:] = np.linalg.solve(Lc.conj(), flat)
     return psi
 
 
