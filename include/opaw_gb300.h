@@ -93,7 +93,9 @@ typedef struct opaw_ctx opaw_ctx;
 int opaw_dev_init(const opaw_system *sys, opaw_ctx **out);
 int opaw_dev_free(opaw_ctx *ctx);
 const char *opaw_last_error(void);
-/* the cudaStream_t all work of this context is issued on */
+/* the cudaStream_t all work of this context is issued on (non-blocking: a
+ * caller that writes a device input on another stream orders that work
+ * before the call itself, e.g. by issuing it on this stream) */
 void *opaw_stream(opaw_ctx *ctx);
 /* number of this library's kernels launched since the context was made */
 int64_t opaw_kernel_launches(opaw_ctx *ctx);

@@ -72,7 +72,20 @@ def _residuals(X, HX, w, dv):
     return torch.sqrt((R.abs() ** 2).sum(dim=1).double() * dv).cpu().numpy()
 
 
-def lowest_states(ctx, psi0, n_iter=60, degree=10, tol=1e-4, fp64_polish=4, nbuf=None, seed=0, verbose=False):
+def lowest_states(ctx, psi0, n_iter=200, degree=24, tol=1e-4, fp64_polish=4, nbuf=None, seed=0, verbose=False):
+    """Lowest eigenpairs of S^-1/2 H S^-1/2; see `_lowest_states`.  Every
+    torch operation runs on the library's stream (opaw_stream): the device
+    entry points read their inputs in that stream's order, so a torch kernel
+    queued on another stream could still be writing an input when the
+    library's kernels read it."""
+    torch = _torch()
+    with torch.cuda.stream(torch.cuda.ExternalStream(ctx.stream)):
+        out = _lowest_states(ctx, psi0, n_iter, degree, tol, fp64_polish, nbuf, seed, verbose)
+        torch.cuda.current_stream().synchronize()
+    return out
+
+
+def _lowest_states(ctx, psi0, n_iter, degree, tol, fp64_polish, nbuf, seed, verbose):
     """Lowest eigenpairs of S^-1/2 H S^-1/2 (set 0's v_ks and D_ij) starting
     from the orbitals psi0 [norb, nn].  FP32 Chebyshev-filtered subspace
     iteration on norb + nbuf vectors (the buffer vectors converge last and are
@@ -84,7 +97,7 @@ def lowest_states(ctx, psi0, n_iter=60, degree=10, tol=1e-4, fp64_polish=4, nbuf
     nn = ctx.nn
     norb = psi0.shape[0]
     if nbuf is None:
-        nbuf = max(4, norb // 8)
+        nbuf = max(8, norb // 4)
     nsub = norb + nbuf
     dt32 = pkg.OPAW_C64
     gen = torch.Generator(device="cuda").manual_seed(seed)
@@ -118,12 +131,20 @@ def lowest_states(ctx, psi0, n_iter=60, degree=10, tol=1e-4, fp64_polish=4, nbuf
     v = noise(1)
     hv = torch.empty_like(v)
     lam_max = 0.0
-    for _ in range(40):
+    for _ in range(60):
         v = v / torch.sqrt((v.abs() ** 2).sum())
         _shs(ctx, dt32, v, hv)
         lam_max = float(torch.sqrt((hv.abs() ** 2).sum()))
         v = hv
-    lam_max *= 1.2
+    # the power iteration approaches the sparse top of the kinetic spectrum
+    # from below; the filter must not amplify anything above b, so also take
+    # the kinetic maximum (ek.f90) plus the largest potential, with margins
+    s_ = ctx.system
+    tmax = 0.5 * ((np.pi / s_.dx) ** 2 + (np.pi / s_.dy) ** 2 + (np.pi / s_.dz) ** 2)
+    if s_.ekcut > 0:
+        tmax = min(tmax, s_.ekcut)
+    vmax = float(np.max(ctx.get_vks(0)))
+    lam_max = 1.1 * max(lam_max, tmax + max(vmax, 0.0)) + 0.5
     _shs(ctx, dt32, X, HX)
     w = _rayleigh_ritz(ctx, dt32, X, HX, S)
     for it in range(n_iter):
@@ -156,6 +177,8 @@ def lowest_states(ctx, psi0, n_iter=60, degree=10, tol=1e-4, fp64_polish=4, nbuf
             Y0, Y1, HX = Y1, HX, Y0
             sigma = sigma2
         X.copy_(Y1)
+        if verbose:
+            print(f"  filter a={a:.4f} b={b:.4f} m={m} lam_max={lam_max:.3f} |Y| max row {float(torch.sqrt((X.abs() ** 2).sum(dim=1)).max()):.3e}")
         _orthonormalise(ctx, dt32, X, S)
         _shs(ctx, dt32, X, HX)
         w = _rayleigh_ritz(ctx, dt32, X, HX, S)
