@@ -42,12 +42,14 @@ CPU_SAMPLE_NORB = 2
 def workload_config(norb):
     return {
         "workload": f"OPAW-TDDFT RK4 step, synthetic 96^3 grid h=0.4, {norb} orbitals x 2 sets, 40 atoms x 8 "
-                    "projectors (16^3 boxes), MT Hartree 192^3, LDA, dt=0.05, kick gamma=1e-3 along x",
+                    "projectors (16^3 boxes), kinetic capped at the box sphere (ekcut 30.84 Ha), MT Hartree 192^3, "
+                    "LDA, dt=0.05, kick gamma=1e-3 along x",
         "grid": [96, 96, 96],
         "orbitals_per_set": norb,
         "sets": 2,
         "atoms": 40,
         "projectors_per_atom": 8,
+        "ekcut_ha": 30.843,
         "l2": "inputs larger than L2 (orbitals 3.6 GB resident)",
     }
 

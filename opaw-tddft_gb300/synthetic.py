@@ -134,6 +134,18 @@ def _place_atoms(rng, natom, lo, hi, dmin, max_tries=200000):
     return np.array(pts)
 
 
+def reference_ekcut(n, h, ek_factor=1.0):
+    """The kinetic cap ekcut that the reference derives when none is read
+    (prepare_libpaw.f90:189-194): getcut.f90:39-41 takes ecut =
+    0.5 (2 pi)^2 boxsq (ek_factor - 1e-10), boxsq the smallest reduced |G|^2
+    on the faces of the FFT box (bound.f90: indices +-(n_k/2) in integer
+    division, metric 1/L_k^2 for an orthorhombic cell at the Gamma point,
+    so the minimum sits at a face centre).  ek.f90:42-44 then clips every
+    k^2/2 above it, which bounds the spectrum the RK4 step sees."""
+    boxsq = min(((nk // 2) / (nk * hk)) ** 2 for nk, hk in zip(n, h))
+    return 0.5 * (2.0 * np.pi) ** 2 * boxsq * (ek_factor - 1e-10)
+
+
 def build_system(
     n=(24, 20, 16),
     h=0.5,
@@ -142,7 +154,7 @@ def build_system(
     rc=0.8,
     rpad=1.0,
     alphas=(0.5, 0.8),
-    ekcut=0.0,
+    ekcut=None,
     periodic=0,
     scale_vh=None,
     norb=4,
@@ -153,10 +165,14 @@ def build_system(
     comp_rc=None,
     comp_sigma=0.45,
 ):
-    """Builds a synthetic system; `n` is (nx, ny, nz) and h the spacing (all axes)."""
+    """Builds a synthetic system; `n` is (nx, ny, nz) and h the spacing (all
+    axes).  ekcut None takes the reference's default cap (`reference_ekcut`);
+    0 leaves the kinetic energy uncapped."""
     rng = np.random.default_rng(seed)
     nx, ny, nz = n
     dx = dy = dz = float(h)
+    if ekcut is None:
+        ekcut = reference_ekcut((nx, ny, nz), (dx, dy, dz))
     xs, ys, zs = _coords(nx, dx), _coords(ny, dy), _coords(nz, dz)
     L = np.array([nx * dx, ny * dy, nz * dz])
     xmax = L / 2.0
@@ -339,11 +355,13 @@ def small_system(kind="tiny", seed=7, norb=4):
     """Test-sized systems.  'tiny' 24x20x16; 'odd' exercises radices 3,5,7;
     'edge' is periodic with boxes that wrap around the faces; 'spec' uses
     extents with compile-time specialised FFT kernels (32, 48, 64 and the
-    64, 96, 128 Hartree box)."""
+    64, 96, 128 Hartree box).  All but 'odd' take the reference's kinetic
+    cap; 'odd' leaves it off (ekcut 0) so both branches of the kinetic
+    factor are exercised."""
     if kind == "tiny":
         return build_system(n=(24, 20, 16), h=0.5, natom=3, seed=seed, rc=0.8, norb=norb)
     if kind == "odd":
-        return build_system(n=(30, 28, 20), h=0.5, natom=4, seed=seed, rc=0.8, norb=norb)
+        return build_system(n=(30, 28, 20), h=0.5, natom=4, seed=seed, rc=0.8, norb=norb, ekcut=0.0)
     if kind == "edge":
         coords = np.array([[5.9, 0.3, -0.2], [-1.0, -4.8, 3.7], [0.5, 1.5, 0.1]])
         return build_system(n=(24, 20, 16), h=0.5, natom=3, seed=seed, rc=0.8, norb=norb,

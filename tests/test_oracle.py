@@ -111,6 +111,25 @@ def test_hermiticity(tiny):
 def test_ek_table(tiny):
     s, _, o = tiny
     assert np.array_equal(o.ek(), numpy_ref.ek(s).reshape(-1))
+    assert s.ekcut > 0 and np.max(o.ek()) * s.nn == pytest.approx(s.ekcut, rel=1e-12)
+
+
+@pytest.mark.parametrize("n,h", [((24, 20, 16), (0.5, 0.5, 0.5)), ((30, 28, 21), (0.5, 0.45, 0.4)),
+                                 ((96, 96, 96), (0.4, 0.4, 0.4)), ((96, 64, 48), (0.45, 0.45, 0.45))])
+def test_reference_ekcut_is_box_sphere(n, h):
+    """The default cap against a direct scan of the FFT-box faces (bound.f90:
+    every point with one reduced index at +-(n_k/2), metric 1/L_k^2, Gamma
+    point), then getcut.f90:39-41 with ek_factor = 1."""
+    L = [nk * hk for nk, hk in zip(n, h)]
+    dsqmin = math.inf
+    for ax in range(3):
+        grids = [np.arange(-(nk // 2), nk // 2 + 1) for nk in n]
+        grids[ax] = np.array([-(n[ax] // 2), n[ax] // 2])
+        i1, i2, i3 = np.meshgrid(*grids, indexing="ij")
+        d = (i1 / L[0]) ** 2 + (i2 / L[1]) ** 2 + (i3 / L[2]) ** 2
+        dsqmin = min(dsqmin, float(d.min()))
+    ecut = 0.5 * (2 * math.pi) ** 2 * dsqmin * (1.0 - 1e-10)
+    assert synthetic.reference_ekcut(n, h) == pytest.approx(ecut, rel=1e-14)
 
 
 def test_charge_sum_rule_and_rebuild(tiny):
