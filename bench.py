@@ -347,9 +347,9 @@ def main():
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(stream)
-    dd_mixed = []
-    for _ in range(args.steps):
-        dd_mixed.append(ctx.tddft_steps(1, DT, GAMMA, pkg.PREC_MIXED)[0])
+    # one call propagates the K steps, as the driver loop would issue a block
+    # of steps (the dipole of every step is still computed and returned)
+    dd_mixed = ctx.tddft_steps(args.steps, DT, GAMMA, pkg.PREC_MIXED)
     e1.record(stream)
     torch.cuda.synchronize()
     el_ms = e0.elapsed_time(e1)

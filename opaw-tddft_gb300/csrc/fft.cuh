@@ -9,6 +9,9 @@
 // (lib/library_fftw_v3.f90:56-83): unnormalised, forward sign -1, backward +1.
 #pragma once
 
+#include <type_traits>
+#include <utility>
+
 #include "common.cuh"
 
 namespace opaw {
@@ -328,12 +331,35 @@ __global__ void __launch_bounds__(256) k_fft_axis(AxisDev ax, Dims3 d, int TL, i
 }
 
 // plain load/store between two batched arrays (may alias)
+// ---- staging helpers shared by the shared-memory FFT kernels
+// Ops whose load is a plain read of array raw(b) at g stage their tile with
+// cp.async (global -> shared, no registers, every copy of a thread in flight
+// at once); ops with a prefetch/finish split (pre + fin) have their epilogue
+// operands loaded in chunks before any store.
+template <class Op, class = void> struct HasRaw : std::false_type {};
+template <class Op>
+struct HasRaw<Op, std::void_t<decltype(std::declval<const Op &>().raw(0))>> : std::true_type {};
+template <class Op, class = void> struct HasPre : std::false_type {};
+template <class Op>
+struct HasPre<Op, std::void_t<decltype(std::declval<const Op &>().pre(0, int64_t(0)))>> : std::true_type {};
+
+template <typename C> __device__ __forceinline__ void cp_async_elem(C *smem, const C *gmem) {
+  static_assert(sizeof(C) == 8 || sizeof(C) == 16, "complex64 or complex128 elements");
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(C) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename C> struct OpCopy {
   const C *src;
   C *dst;
   int64_t bstride;
   static constexpr bool kMid = false;
   __device__ C load(int b, int64_t g) const { return src[b * bstride + g]; }
+  __device__ const C *raw(int b) const { return src + b * bstride; }
   __device__ void store(int b, int64_t g, C v) const { dst[b * bstride + g] = v; }
   __device__ double line(int64_t) const { return 0.0; }
   __device__ C mid(int, int64_t, double, int, C v) const { return v; }
@@ -470,14 +496,26 @@ __global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, int sign, const C *__re
     jstride = d.n0 * d.n1;
   }
   constexpr int TOT = TL * N;
+  if constexpr (HasRaw<Op>::value) {
+    const C *src = op.raw(b);
 #pragma unroll 4
-  for (int e = threadIdx.x; e < TOT; e += NT) {
-    int l, j;
-    if (AXIS == 0) { l = e / N; j = e - l * N; } else { j = e / TL; l = e - j * TL; }
-    C v;
-    if (l < nl) v = op.load(b, base + l * lstride + j * jstride);
-    else { v.x = 0; v.y = 0; }
-    bufa[j * LS + l] = v;
+    for (int e = threadIdx.x; e < TOT; e += NT) {
+      int l, j;
+      if (AXIS == 0) { l = e / N; j = e - l * N; } else { j = e / TL; l = e - j * TL; }
+      if (l < nl) cp_async_elem(&bufa[j * LS + l], src + base + l * lstride + j * jstride);
+      else { bufa[j * LS + l].x = 0; bufa[j * LS + l].y = 0; }
+    }
+    cp_async_wait_all();
+  } else {
+#pragma unroll 4
+    for (int e = threadIdx.x; e < TOT; e += NT) {
+      int l, j;
+      if (AXIS == 0) { l = e / N; j = e - l * N; } else { j = e / TL; l = e - j * TL; }
+      C v;
+      if (l < nl) v = op.load(b, base + l * lstride + j * jstride);
+      else { v.x = 0; v.y = 0; }
+      bufa[j * LS + l] = v;
+    }
   }
   __syncthreads();
   C *res;
@@ -604,10 +642,32 @@ __global__ void __launch_bounds__(384, 2) k_fft_xy(int sign, const C *__restrict
   const int b = blockIdx.y;
   const int64_t base = (int64_t)blockIdx.x * NX * NY;
   constexpr int TOT = NX * NY;
-#pragma unroll 4
-  for (int e = threadIdx.x; e < TOT; e += NT) {
-    const int y = e / NX, x = e - y * NX;
-    pl[y * LX + x] = op.load(b, base + e);
+  constexpr int CH = 8;  // elements per thread whose loads are issued together
+  if constexpr (HasRaw<Op>::value) {
+    const C *src = op.raw(b) + base;
+#pragma unroll 8
+    for (int e = threadIdx.x; e < TOT; e += NT) {
+      const int y = e / NX, x = e - y * NX;
+      cp_async_elem(&pl[y * LX + x], src + e);
+    }
+    cp_async_wait_all();
+  } else {
+    for (int e0 = threadIdx.x; e0 < TOT; e0 += NT * CH) {
+      C r[CH];
+#pragma unroll
+      for (int j = 0; j < CH; j++) {
+        const int e = e0 + j * NT;
+        if (e < TOT) r[j] = op.load(b, base + e);
+      }
+#pragma unroll
+      for (int j = 0; j < CH; j++) {
+        const int e = e0 + j * NT;
+        if (e < TOT) {
+          const int y = e / NX, x = e - y * NX;
+          pl[y * LX + x] = r[j];
+        }
+      }
+    }
   }
   __syncthreads();
   if (sign < 0) {
@@ -617,10 +677,29 @@ __global__ void __launch_bounds__(384, 2) k_fft_xy(int sign, const C *__restrict
     XyStages<C, NY, NX, 1, LX, NT, 0>::run(pl, ty, sign);
     XyStages<C, NX, NY, LX, 1, NT, 0>::run(pl, tx, sign);
   }
+  if constexpr (HasPre<Op>::value) {
+    for (int e0 = threadIdx.x; e0 < TOT; e0 += NT * CH) {
+      decltype(op.pre(0, int64_t(0))) q[CH];
+#pragma unroll
+      for (int j = 0; j < CH; j++) {
+        const int e = e0 + j * NT;
+        if (e < TOT) q[j] = op.pre(b, base + e);
+      }
+#pragma unroll
+      for (int j = 0; j < CH; j++) {
+        const int e = e0 + j * NT;
+        if (e < TOT) {
+          const int y = e / NX, x = e - y * NX;
+          op.fin(b, base + e, pl[y * LX + x], q[j]);
+        }
+      }
+    }
+  } else {
 #pragma unroll 4
-  for (int e = threadIdx.x; e < TOT; e += NT) {
-    const int y = e / NX, x = e - y * NX;
-    op.store(b, base + e, pl[y * LX + x]);
+    for (int e = threadIdx.x; e < TOT; e += NT) {
+      const int y = e / NX, x = e - y * NX;
+      op.store(b, base + e, pl[y * LX + x]);
+    }
   }
 }
 

@@ -4,9 +4,9 @@
 //   h_apply  F^-1[ek F psi] + v_ks psi + sum p D <p|psi>   (hphi.f90:1-66)
 //   sn_apply psi + sum p1 ((1+s)^n - 1) <p1|psi>           (snphi.f90:1-49)
 //   shs      S^-1/2 H S^-1/2                               (shs.f90:3-23)
-// Every reduction runs in a fixed order (one CTA per atom and orbital group
-// for the box sums; one thread per grid point, atoms in order, for the
-// scatter), so FP64 results are bit-reproducible run to run.
+// Every reduction runs in a fixed order (one warp per atom and orbital for
+// the box sums; one thread per grid point, atoms in order, for the scatter),
+// so FP64 results are bit-reproducible run to run.
 #include "fft.cuh"
 
 namespace opaw {
@@ -50,76 +50,87 @@ template <int NV, int LEVEL = 0> struct Halve {
 };
 
 // out[o*ns + soff[a] + i] = dv * sum_box P_a[i][b] * psi_o[g(b)]   (p real: Gamma point)
-template <typename R, int MSMAX, int OB>
-__global__ void __launch_bounds__(256) k_gather(const typename Tr<R>::C *__restrict__ psi, int64_t nn, int norb,
-                                                const R *__restrict__ P, const int64_t *__restrict__ poff,
-                                                const int *__restrict__ boxg, const int64_t *__restrict__ boff,
-                                                const int *__restrict__ nrough, const int *__restrict__ ms,
-                                                const int64_t *__restrict__ soff, double dv,
-                                                double2 *__restrict__ out, int ns) {
+// One warp per orbital and kGatherWarps orbitals per CTA over one atom's box:
+// lane l sums the points l, l+32, ... (two per iteration, their loads issued
+// together) into 2*MSMAX registers, then a shuffle tree adds the lanes.  The
+// warps of a CTA read the same projector rows, which L1 serves once, so the
+// projector tables cost one L2 read per atom and orbital group.  The order of
+// every sum is fixed (bit-reproducible).
+constexpr int kGatherWarps = 8;
+
+template <typename R, int MSMAX>
+__global__ void __launch_bounds__(32 * kGatherWarps)
+    k_gather(const typename Tr<R>::C *__restrict__ psi, int64_t nn, int norb, const R *__restrict__ P,
+             const int64_t *__restrict__ poff, const int *__restrict__ boxg, const int64_t *__restrict__ boff,
+             const int *__restrict__ nrough, const int *__restrict__ ms, const int64_t *__restrict__ soff, double dv,
+             double *__restrict__ out, int ns) {
   typedef typename Tr<R>::C C;
-  constexpr int NV = OB * MSMAX * 2;  // value index (o * MSMAX + i) * 2 + re/im
-  static_assert(NV >= 32 && (NV & (NV - 1)) == 0, "NV must be a power of two >= 32");
+  constexpr int NV = 2 * MSMAX;  // value index 2 i + re/im
+  static_assert(NV == 16 || NV == 32, "8 or 16 projectors per atom");
   const int a = blockIdx.x;
-  const int o0 = blockIdx.y * OB;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int o = blockIdx.y * kGatherWarps + warp;
+  if (o >= norb) return;  // whole warps leave: no block-wide barrier follows
   const int m = ms[a];
   const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
   const int *bg = boxg + boff[a];  // wrapped grid index of each box point (proj.f90:27-37)
   const R *Pa = P + poff[a];
+  const C *po = psi + (int64_t)o * nn;
   R v[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) v[k] = 0;
-  for (int b = threadIdx.x; b < nbox; b += blockDim.x) {
-    const int64_t g = bg[b];
-    R p[MSMAX];
+  int b = lane;
+  for (; b + 32 < nbox; b += 64) {
+    const int g0 = bg[b], g1 = bg[b + 32];
+    R p0[MSMAX], p1[MSMAX];
 #pragma unroll
-    for (int i = 0; i < MSMAX; i++) p[i] = (i < m) ? Pa[(int64_t)i * nbox + b] : (R)0;
+    for (int i = 0; i < MSMAX; i++) {
+      p0[i] = (i < m) ? Pa[(int64_t)i * nbox + b] : (R)0;
+      p1[i] = (i < m) ? Pa[(int64_t)i * nbox + b + 32] : (R)0;
+    }
+    const C z0 = po[g0], z1 = po[g1];
 #pragma unroll
-    for (int o = 0; o < OB; o++) {
-      if (o0 + o < norb) {
-        const C z = psi[(int64_t)(o0 + o) * nn + g];
-#pragma unroll
-        for (int i = 0; i < MSMAX; i++) {
-          v[(o * MSMAX + i) * 2] += p[i] * z.x;
-          v[(o * MSMAX + i) * 2 + 1] += p[i] * z.y;
-        }
-      }
+    for (int i = 0; i < MSMAX; i++) {
+      v[2 * i] += p0[i] * z0.x;
+      v[2 * i + 1] += p0[i] * z0.y;
+      v[2 * i] += p1[i] * z1.x;
+      v[2 * i + 1] += p1[i] * z1.y;
     }
   }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Halve<NV>::run(v, lane);
-  constexpr int PER = NV / 32;
-  __shared__ R red[8][NV];
+  if (b < nbox) {
+    const int g0 = bg[b];
+    const C z0 = po[g0];
 #pragma unroll
-  for (int k = 0; k < PER; k++) red[warp][lane * PER + k] = v[k];
-  __syncthreads();
-  const int nw = blockDim.x >> 5;
-  for (int t = threadIdx.x; t < OB * m; t += blockDim.x) {
-    const int o = t / m, i = t % m;
-    if (o0 + o >= norb) continue;
-    R sx = 0, sy = 0;
-    for (int w = 0; w < nw; w++) {
-      sx += red[w][(o * MSMAX + i) * 2];
-      sy += red[w][(o * MSMAX + i) * 2 + 1];
+    for (int i = 0; i < MSMAX; i++) {
+      const R p = (i < m) ? Pa[(int64_t)i * nbox + b] : (R)0;
+      v[2 * i] += p * z0.x;
+      v[2 * i + 1] += p * z0.y;
     }
-    out[(int64_t)(o0 + o) * ns + soff[a] + i] = make_double2((double)sx * dv, (double)sy * dv);
   }
+  Halve<NV>::run(v, lane);  // lane L: value L * NV / 32 (NV = 16: lanes L, L^1 hold halves of it)
+  R sum = v[0];
+  int idx = lane;
+  if constexpr (NV == 16) {
+    sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+    idx = lane >> 1;
+  }
+  const int i = idx >> 1;
+  if (i < m && (NV == 32 || (lane & 1) == 0)) out[2 * ((int64_t)o * ns + soff[a] + i) + (idx & 1)] = (double)sum * dv;
 }
 
 template <typename R>
 int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, double2 *coef) {
   if (c->natom == 0) return OPAW_OK;
   const R *P = ProjTab<R>::get(c, which);
+  const dim3 grid(c->natom, (norb + kGatherWarps - 1) / kGatherWarps);
   if (c->msmax <= 8) {
-    constexpr int OB = 2;
-    dim3 grid(c->natom, (norb + OB - 1) / OB);
-    k_gather<R, 8, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_boxg, c->d_boff, c->d_nrough,
-                                                    c->d_ms, c->d_soff, c->dv, coef, c->ns);
+    k_gather<R, 8><<<grid, 32 * kGatherWarps, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_boxg, c->d_boff,
+                                                              c->d_nrough, c->d_ms, c->d_soff, c->dv,
+                                                              (double *)coef, c->ns);
   } else if (c->msmax <= 16) {
-    constexpr int OB = sizeof(R) == 4 ? 2 : 1;
-    dim3 grid(c->natom, (norb + OB - 1) / OB);
-    k_gather<R, 16, OB><<<grid, 256, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_boxg, c->d_boff,
-                                                     c->d_nrough, c->d_ms, c->d_soff, c->dv, coef, c->ns);
+    k_gather<R, 16><<<grid, 32 * kGatherWarps, 0, c->stream>>>(pin, c->nn, norb, P, c->d_poff, c->d_boxg, c->d_boff,
+                                                               c->d_nrough, c->d_ms, c->d_soff, c->dv,
+                                                               (double *)coef, c->ns);
   } else {
     set_error("more than 16 projectors per atom");
     return OPAW_ERR_ARG;
@@ -169,13 +180,14 @@ __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__rest
       }
     }
     const int oa = blockIdx.y * kScatterOrb, ob = min(norb, oa + kScatterOrb);
-    for (int o0 = oa; o0 < ob; o0 += 4) {
-      C cur[4];
+    constexpr int Q = 8;  // orbitals whose values are loaded together
+    for (int o0 = oa; o0 < ob; o0 += Q) {
+      C cur[Q];
 #pragma unroll
-      for (int q = 0; q < 4; q++)
+      for (int q = 0; q < Q; q++)
         if (o0 + q < ob) cur[q] = dst[(int64_t)(o0 + q) * nn];
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
+      for (int q = 0; q < Q; q++) {
         if (o0 + q < ob) {
           const C *co = coef + (int64_t)(o0 + q) * ns;
           R sx = 0, sy = 0;
@@ -197,7 +209,7 @@ __global__ void __launch_bounds__(256) k_union_scatter(typename Tr<R>::C *__rest
         }
       }
 #pragma unroll
-      for (int q = 0; q < 4; q++)
+      for (int q = 0; q < Q; q++)
         if (o0 + q < ob) dst[(int64_t)(o0 + q) * nn] = cur[q];
     }
     return;
@@ -334,6 +346,7 @@ template <> struct OpKin<double> {
   double ekcut, ntot;
   static constexpr bool kMid = true;
   __device__ double2 load(int b, int64_t g) const { return buf[b * bstride + g]; }
+  __device__ const double2 *raw(int b) const { return buf + b * bstride; }
   __device__ void store(int b, int64_t g, double2 v) const { buf[b * bstride + g] = v; }
   // z-lines: the line index is the (x, y) position
   __device__ double line(int64_t gl) const {
@@ -355,6 +368,7 @@ template <> struct OpKin<float> {
   float ekcut, invn;
   static constexpr bool kMid = true;
   __device__ float2 load(int b, int64_t g) const { return buf[b * bstride + g]; }
+  __device__ const float2 *raw(int b) const { return buf + b * bstride; }
   __device__ void store(int b, int64_t g, float2 v) const { buf[b * bstride + g] = v; }
   __device__ float line(int64_t gl) const {
     const int t = (int)gl;
@@ -382,20 +396,32 @@ template <typename R> struct OpHFinal {
   const R *dv;
   static constexpr bool kMid = false;
   __device__ C load(int b, int64_t g) const { return src[b * bstride + g]; }
-  __device__ void store(int b, int64_t g, C v) const {
-    const C p = pin[b * bstride + g];
-    const R w = vks[g];
-    C r;
-    r.x = v.x + p.x * w;
-    r.y = v.y + p.y * w;
+  // the epilogue operands of one element, loaded ahead of the stores
+  struct Pre {
+    C p, t;
+    R w, d;
+  };
+  __device__ Pre pre(int b, int64_t g) const {
+    Pre q;
+    q.p = pin[b * bstride + g];
+    q.w = vks[g];
     if (t0) {
-      const C t = t0[b * bstride + g];
-      const R d = dv[g];
-      r.x += t.x * d;
-      r.y += t.y * d;
+      q.t = t0[b * bstride + g];
+      q.d = dv[g];
+    }
+    return q;
+  }
+  __device__ void fin(int b, int64_t g, C v, const Pre &q) const {
+    C r;
+    r.x = v.x + q.p.x * q.w;
+    r.y = v.y + q.p.y * q.w;
+    if (t0) {
+      r.x += q.t.x * q.d;
+      r.y += q.t.y * q.d;
     }
     hp[b * bstride + g] = r;
   }
+  __device__ void store(int b, int64_t g, C v) const { fin(b, g, v, pre(b, g)); }
   __device__ double line(int64_t) const { return 0.0; }
   __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
