@@ -182,6 +182,15 @@ struct opaw_ctx {
   int *d_upt = nullptr, *d_ustart = nullptr, *d_uatom = nullptr, *d_ubox = nullptr;
   int *d_boxg = nullptr;         // per atom and box point: the wrapped linear grid index
   int64_t *d_boff = nullptr;     // per atom offset into d_boxg
+  int *d_uidx = nullptr;         // per grid point: its union index, -1 outside every box
+  // projector overlaps <p_x|p_y> (x, y = p~ or p~1; FP64, dv included) as
+  // dense ms_a x ms_b blocks for every pair of atoms whose boxes share a
+  // grid point: block k of row atom a is (a, ovl_atom[k]) for k in
+  // [ovl_start[a], ovl_start[a+1]), stored row-major at ovl_off[k]
+  int novl = 0;
+  int *d_ovl_start = nullptr, *d_ovl_atom = nullptr;
+  int64_t *d_ovl_off = nullptr;
+  double *d_ovl[4] = {nullptr, nullptr, nullptr, nullptr};  // <p~|p~>, <p~|p~1>, <p~1|p~>, <p~1|p~1>
 
   // compensation charge tables
   int ncomp = 0;             // total sphere points
@@ -228,7 +237,7 @@ struct opaw_ctx {
   opaw::DeviceBuf coef[4];       // [norb][ns] double2
   opaw::DeviceBuf coefr;         // single-precision copy of the scatter coefficients
   opaw::DeviceBuf gram, gramout; // Gram partials, small matrices
-  opaw::DeviceBuf mix[14];       // buffers of the mixed-precision difference step
+  opaw::DeviceBuf mix[16];       // buffers of the mixed-precision difference step
   opaw::DeviceBuf red;           // reductions
   double *h_red = nullptr;       // pinned host mirror of small reductions
 };
@@ -256,6 +265,24 @@ template <typename R>
 int h_apply_ex(opaw_ctx *c, const R *vks, const double *dij, const typename Tr<R>::C *pin, typename Tr<R>::C *hp,
                int norb, const double2 *cpre, const typename Tr<R>::C *t0, const R *dv, const double2 *c0,
                const double *ddij);
+// projector coefficient algebra (hamiltonian.cu): cout = D cin, and
+// cout = D cin + dD c0 (hphi.f90:43-47)
+__global__ void k_coef_dij(const double2 *__restrict__ cin, double2 *__restrict__ cout, int norb, int ns,
+                           const int *__restrict__ slot_atom, const int64_t *__restrict__ soff,
+                           const int64_t *__restrict__ doff, const int *__restrict__ ms,
+                           const double *__restrict__ dij);
+__global__ void k_coef_dij2(const double2 *__restrict__ cin, const double2 *__restrict__ c0,
+                            double2 *__restrict__ cout, int norb, int ns, const int *__restrict__ slot_atom,
+                            const int64_t *__restrict__ soff, const int64_t *__restrict__ doff,
+                            const int *__restrict__ ms, const double *__restrict__ dij,
+                            const double *__restrict__ ddij);
+// the grid part of h_phi (kinetic + local, + dv t0 when t0 is given)
+template <typename R>
+int h_fft(opaw_ctx *c, const R *vks, const typename Tr<R>::C *pin, typename Tr<R>::C *hp, int norb,
+          const typename Tr<R>::C *t0, const R *dv);
+// <p~|pin> and <p~1|pin> in one pass over the boxes
+template <typename R>
+int gather2(opaw_ctx *c, const typename Tr<R>::C *pin, int norb, double2 *c0, double2 *c1);
 
 // (fft.cu) batched 3D FFT of `batch` arrays; sign -1 forward, +1 backward
 template <typename R>

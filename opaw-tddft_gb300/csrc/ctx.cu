@@ -172,6 +172,59 @@ static int build(opaw_ctx *c, const opaw_system *s) {
     OPAW_CHECK(upload(&c->d_ustart, ustart.data(), ustart.size()));
     OPAW_CHECK(upload(&c->d_uatom, uatom.data(), uatom.size()));
     OPAW_CHECK(upload(&c->d_ubox, ubox.data(), ubox.size()));
+    std::vector<int> uidx((size_t)c->nn, -1);
+    for (int u = 0; u < c->nunion; u++) uidx[upt[u]] = u;
+    OPAW_CHECK(upload(&c->d_uidx, uidx.data(), uidx.size()));
+    // projector overlaps: every pair of entries at a union point adds
+    // P_x[a][i](b) P_y[a'][j](b') dv to block (a, a'), element (i, j)
+    std::vector<std::vector<int>> nbr(na);
+    for (int u = 0; u < c->nunion; u++)
+      for (int e1 = ustart[u]; e1 < ustart[u + 1]; e1++)
+        for (int e2 = ustart[u]; e2 < ustart[u + 1]; e2++) nbr[uatom[e1]].push_back(uatom[e2]);
+    std::vector<int> ostart(na + 1, 0), oatom;
+    std::vector<int64_t> ooff;
+    int64_t tot = 0;
+    for (int a = 0; a < na; a++) {
+      std::sort(nbr[a].begin(), nbr[a].end());
+      nbr[a].erase(std::unique(nbr[a].begin(), nbr[a].end()), nbr[a].end());
+      for (int b : nbr[a]) {
+        oatom.push_back(b);
+        ooff.push_back(tot);
+        tot += (int64_t)s->ms[a] * s->ms[b];
+      }
+      ostart[a + 1] = (int)oatom.size();
+    }
+    c->novl = (int)oatom.size();
+    auto block_of = [&](int a, int b) {
+      const int k0 = ostart[a], k1 = ostart[a + 1];
+      const int k = (int)(std::lower_bound(oatom.begin() + k0, oatom.begin() + k1, b) - oatom.begin());
+      return k;
+    };
+    std::vector<double> ov[4];
+    for (auto &v : ov) v.assign((size_t)(tot ? tot : 1), 0.0);
+    const double *tab[2] = {s->p3d, s->p3d1};
+    for (int u = 0; u < c->nunion; u++)
+      for (int e1 = ustart[u]; e1 < ustart[u + 1]; e1++) {
+        const int a = uatom[e1], ba = ubox[e1], ma = s->ms[a];
+        const int64_t na_box = boff[a + 1] - boff[a];
+        for (int e2 = ustart[u]; e2 < ustart[u + 1]; e2++) {
+          const int b = uatom[e2], bb = ubox[e2], mb = s->ms[b];
+          const int64_t nb_box = boff[b + 1] - boff[b];
+          const int64_t off = ooff[block_of(a, b)];
+          for (int x = 0; x < 2; x++)
+            for (int y = 0; y < 2; y++) {
+              double *O = ov[2 * x + y].data() + off;
+              for (int i = 0; i < ma; i++) {
+                const double pa = tab[x][c->h_poff[a] + (int64_t)i * na_box + ba] * c->dv;
+                for (int j = 0; j < mb; j++) O[(int64_t)i * mb + j] += pa * tab[y][c->h_poff[b] + (int64_t)j * nb_box + bb];
+              }
+            }
+        }
+      }
+    OPAW_CHECK(upload(&c->d_ovl_start, ostart.data(), ostart.size()));
+    OPAW_CHECK(upload(&c->d_ovl_atom, oatom.data(), oatom.size()));
+    OPAW_CHECK(upload(&c->d_ovl_off, ooff.data(), ooff.size()));
+    for (int k = 0; k < 4; k++) OPAW_CHECK(upload(&c->d_ovl[k], ov[k].data(), ov[k].size()));
   }
   // compensation spheres
   c->h_ngrid.assign(s->ngrid, s->ngrid + na);
@@ -294,6 +347,11 @@ static void destroy(opaw_ctx *c) {
   cudaFree(c->gramout.p);
   cudaFree(c->d_boxg);
   cudaFree(c->d_boff);
+  cudaFree(c->d_uidx);
+  cudaFree(c->d_ovl_start);
+  cudaFree(c->d_ovl_atom);
+  cudaFree(c->d_ovl_off);
+  for (int k = 0; k < 4; k++) cudaFree(c->d_ovl[k]);
   for (auto &b : c->mix) cudaFree(b.p);
   cudaFree(c->red.p);
   if (c->h_red) cudaFreeHost(c->h_red);

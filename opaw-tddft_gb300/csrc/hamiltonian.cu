@@ -51,7 +51,7 @@ template <int NV, int LEVEL = 0> struct Halve {
 
 // out[o*ns + soff[a] + i] = dv * sum_box P_a[i][b] * psi_o[g(b)]   (p real: Gamma point)
 // One warp per orbital and kGatherWarps orbitals per CTA over one atom's box:
-// lane l sums the points l, l+32, ... (two per iteration, their loads issued
+// lane l sums the points l, l+32, ... (U per iteration, their loads issued
 // together) into 2*MSMAX registers, then a shuffle tree adds the lanes.  The
 // warps of a CTA read the same projector rows, which L1 serves once, so the
 // projector tables cost one L2 read per atom and orbital group.  The order of
@@ -79,32 +79,30 @@ __global__ void __launch_bounds__(32 * kGatherWarps)
   R v[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) v[k] = 0;
-  int b = lane;
-  for (; b + 32 < nbox; b += 64) {
-    const int g0 = bg[b], g1 = bg[b + 32];
-    R p0[MSMAX], p1[MSMAX];
+  // U points per lane and iteration: their index loads, then their orbital
+  // loads, are all in flight before the first product
+  constexpr int U = (sizeof(R) == 4 && MSMAX <= 8) ? 8 : 4;
+  for (int b0 = lane; b0 < nbox; b0 += 32 * U) {
+    int gg[U];
+    C z[U];
 #pragma unroll
-    for (int i = 0; i < MSMAX; i++) {
-      p0[i] = (i < m) ? Pa[(int64_t)i * nbox + b] : (R)0;
-      p1[i] = (i < m) ? Pa[(int64_t)i * nbox + b + 32] : (R)0;
+    for (int k = 0; k < U; k++) gg[k] = (b0 + 32 * k < nbox) ? bg[b0 + 32 * k] : -1;
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      if (gg[k] >= 0) z[k] = po[gg[k]];
+      else z[k].x = z[k].y = (R)0;
     }
-    const C z0 = po[g0], z1 = po[g1];
 #pragma unroll
-    for (int i = 0; i < MSMAX; i++) {
-      v[2 * i] += p0[i] * z0.x;
-      v[2 * i + 1] += p0[i] * z0.y;
-      v[2 * i] += p1[i] * z1.x;
-      v[2 * i + 1] += p1[i] * z1.y;
-    }
-  }
-  if (b < nbox) {
-    const int g0 = bg[b];
-    const C z0 = po[g0];
+    for (int k = 0; k < U; k++) {
+      const int b = b0 + 32 * k;
+      if (b < nbox) {
 #pragma unroll
-    for (int i = 0; i < MSMAX; i++) {
-      const R p = (i < m) ? Pa[(int64_t)i * nbox + b] : (R)0;
-      v[2 * i] += p * z0.x;
-      v[2 * i + 1] += p * z0.y;
+        for (int i = 0; i < MSMAX; i++) {
+          const R p = (i < m) ? Pa[(int64_t)i * nbox + b] : (R)0;
+          v[2 * i] += p * z[k].x;
+          v[2 * i + 1] += p * z[k].y;
+        }
+      }
     }
   }
   Halve<NV>::run(v, lane);  // lane L: value L * NV / 32 (NV = 16: lanes L, L^1 hold halves of it)
@@ -135,6 +133,100 @@ int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, doubl
     set_error("more than 16 projectors per atom");
     return OPAW_ERR_ARG;
   }
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+// both projector families in one pass over the boxes: out0 = <p~|psi>,
+// out1 = <p~1|psi>.  CTA = one atom and kG2Warps orbitals (a warp each); the
+// box is walked in chunks of 256 (FP64: 128) points whose projector rows of both
+// tables are staged once in shared memory for all the CTA's warps, while
+// each lane's orbital loads for the chunk are already in flight.  Lane L ends
+// with values L*PER .. L*PER+PER-1 of the shuffle tree (fixed order).
+constexpr int kG2Warps = 16;
+
+template <typename R, int MSMAX>
+__global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) ? 2 : 1)
+    k_gather2(const typename Tr<R>::C *__restrict__ psi, int64_t nn, int norb, const R *__restrict__ P0,
+              const R *__restrict__ P1, const int64_t *__restrict__ poff, const int *__restrict__ boxg,
+              const int64_t *__restrict__ boff, const int *__restrict__ nrough, const int *__restrict__ ms,
+              const int64_t *__restrict__ soff, double dv, double *__restrict__ out0, double *__restrict__ out1,
+              int ns) {
+  typedef typename Tr<R>::C C;
+  constexpr int H = 2 * MSMAX;  // values per table: 2 i + re/im
+  constexpr int NV = 2 * H;
+  constexpr int PER = NV / 32;
+  constexpr int kG2Chunk = sizeof(R) == 4 ? 256 : 128;  // at most 32 KB of staged rows
+  constexpr int U = kG2Chunk / 32;  // points per lane and chunk
+  static_assert(NV == 32 || NV == 64, "8 or 16 projectors per atom");
+  __shared__ R sp[2][MSMAX][kG2Chunk];
+  const int a = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int o = blockIdx.y * kG2Warps + warp;
+  const bool live = o < norb;  // idle warps still take part in the staging
+  const int m = ms[a];
+  const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+  const int *bg = boxg + boff[a];
+  const R *Pa = P0 + poff[a];
+  const R *Qa = P1 + poff[a];
+  const C *po = psi + (int64_t)(live ? o : 0) * nn;
+  R v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) v[k] = 0;
+  for (int c0 = 0; c0 < nbox; c0 += kG2Chunk) {
+    C z[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      const int b = c0 + lane + 32 * k;
+      z[k].x = z[k].y = (R)0;
+      if (live && b < nbox) z[k] = po[bg[b]];
+    }
+    __syncthreads();  // the previous chunk's rows are no longer read
+    for (int e = threadIdx.x; e < 2 * MSMAX * kG2Chunk; e += blockDim.x) {
+      const int tab = e / (MSMAX * kG2Chunk), r = e - tab * (MSMAX * kG2Chunk);
+      const int i = r / kG2Chunk, j = r - i * kG2Chunk;
+      const int b = c0 + j;
+      sp[tab][i][j] = (i < m && b < nbox) ? (tab ? Qa : Pa)[(int64_t)i * nbox + b] : (R)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      const int j = lane + 32 * k;
+#pragma unroll
+      for (int i = 0; i < MSMAX; i++) {
+        const R p = sp[0][i][j], q = sp[1][i][j];
+        v[2 * i] += p * z[k].x;
+        v[2 * i + 1] += p * z[k].y;
+        v[H + 2 * i] += q * z[k].x;
+        v[H + 2 * i + 1] += q * z[k].y;
+      }
+    }
+  }
+  if (!live) return;  // no block-wide barrier follows
+  Halve<NV>::run(v, lane);
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const int idx = lane * PER + k;
+    const int tab = idx / H, r = idx - tab * H;
+    const int i = r >> 1;
+    if (i < m) (tab ? out1 : out0)[2 * ((int64_t)o * ns + soff[a] + i) + (r & 1)] = (double)v[k] * dv;
+  }
+}
+
+template <typename R>
+int gather2(opaw_ctx *c, const typename Tr<R>::C *pin, int norb, double2 *c0, double2 *c1) {
+  if (c->natom == 0) return OPAW_OK;
+  const R *P0 = ProjTab<R>::get(c, 0), *P1 = ProjTab<R>::get(c, 1);
+  const dim3 grid(c->natom, (norb + kG2Warps - 1) / kG2Warps);
+  if (c->msmax <= 8)
+    k_gather2<R, 8><<<grid, 32 * kG2Warps, 0, c->stream>>>(pin, c->nn, norb, P0, P1, c->d_poff, c->d_boxg,
+                                                           c->d_boff, c->d_nrough, c->d_ms, c->d_soff, c->dv,
+                                                           (double *)c0, (double *)c1, c->ns);
+  else
+    k_gather2<R, 16><<<grid, 32 * kG2Warps, 0, c->stream>>>(pin, c->nn, norb, P0, P1, c->d_poff, c->d_boxg,
+                                                            c->d_boff, c->d_nrough, c->d_ms, c->d_soff, c->dv,
+                                                            (double *)c0, (double *)c1, c->ns);
   c->launches++;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
@@ -503,12 +595,9 @@ template <typename R>
 int h_apply_ex(opaw_ctx *c, const R *vks, const double *dij, const typename Tr<R>::C *pin, typename Tr<R>::C *hp,
                int norb, const double2 *cpre, const typename Tr<R>::C *t0, const R *dv, const double2 *c0,
                const double *ddij) {
-  typedef typename Tr<R>::C C;
   if (norb <= 0) return OPAW_OK;
-  OPAW_CHECK(ensure(c->work[0], sizeof(C) * (size_t)c->nn * norb));
   OPAW_CHECK(ensure(c->coef[0], sizeof(double2) * (size_t)c->ns * norb + 16));
   OPAW_CHECK(ensure(c->coef[1], sizeof(double2) * (size_t)c->ns * norb + 16));
-  C *w = (C *)c->work[0].p;
   const double2 *cp = cpre;
   if (!cp) {
     OPAW_CHECK(gather<R>(c, 0, pin, norb, (double2 *)c->coef[0].p));
@@ -525,6 +614,20 @@ int h_apply_ex(opaw_ctx *c, const R *vks, const double *dij, const typename Tr<R
     c->launches++;
     OPAW_CUDA(cudaGetLastError());
   }
+  OPAW_CHECK(h_fft<R>(c, vks, pin, hp, norb, t0, dv));
+  OPAW_CHECK(union_scatter<R>(c, 0, hp, norb, c1));
+  return OPAW_OK;
+}
+
+// the grid part of h_phi: hp = F^-1[ek F pin] + v_ks pin (+ dv t0)
+// (hphi.f90:16-21), without the projector term
+template <typename R>
+int h_fft(opaw_ctx *c, const R *vks, const typename Tr<R>::C *pin, typename Tr<R>::C *hp, int norb,
+          const typename Tr<R>::C *t0, const R *dv) {
+  typedef typename Tr<R>::C C;
+  if (norb <= 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->work[0], sizeof(C) * (size_t)c->nn * norb));
+  C *w = (C *)c->work[0].p;
   Dims3 d{c->nx, c->ny, c->nz};
   OpCopy<C> x_in{pin, w, c->nn};
   OpCopy<C> inplace{w, w, c->nn};
@@ -543,7 +646,6 @@ int h_apply_ex(opaw_ctx *c, const R *vks, const double *dij, const typename Tr<R
     OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, +1, inplace)));
     OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, +1, fin)));
   }
-  OPAW_CHECK(union_scatter<R>(c, 0, hp, norb, c1));
   return OPAW_OK;
 }
 
@@ -602,7 +704,9 @@ int shs_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>
   template int sn_apply<R>(opaw_ctx *, double, const Tr<R>::C *, Tr<R>::C *, int);                  \
   template int shs_apply<R>(opaw_ctx *, int, const Tr<R>::C *, Tr<R>::C *, int);                    \
   template int h_apply_ex<R>(opaw_ctx *, const R *, const double *, const Tr<R>::C *, Tr<R>::C *, int,  \
-                             const double2 *, const Tr<R>::C *, const R *, const double2 *, const double *);
+                             const double2 *, const Tr<R>::C *, const R *, const double2 *, const double *); \
+  template int h_fft<R>(opaw_ctx *, const R *, const Tr<R>::C *, Tr<R>::C *, int, const Tr<R>::C *, const R *); \
+  template int gather2<R>(opaw_ctx *, const Tr<R>::C *, int, double2 *, double2 *);
 OPAW_INST(float)
 OPAW_INST(double)
 

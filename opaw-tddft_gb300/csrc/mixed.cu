@@ -15,7 +15,14 @@
 // relative precision.  The rebuild forms the density, rho_ij, compensation
 // charge and potential differences directly: Hartree is linear (the
 // difference density gets its own complex64 transform), the LDA difference
-// and the charge-renormalisation factors are taken in FP64.  psi, delta, the RK4 accumulation, the norms and the dipole are FP64.
+// and the charge-renormalisation factors are taken in FP64.  psi, delta, the
+// final RK4 combination, the norms and the dipole are FP64.
+//
+// Per stage the orbitals are touched by the three FFT passes of H (the last
+// one fused with v_ks), one two-table gather of H's grid part, and one fused
+// pass (RK4 accumulation, S^-1/2 of the next stage vector, its density); the
+// projector algebra in between (S^-1/2, D_ij, overlaps) runs on [orbital][slot]
+// coefficient vectors in FP64.
 //
 // In exact arithmetic this is the reference algorithm; OPAW_PREC_FP64 runs
 // the reference's own form for comparison.
@@ -64,23 +71,6 @@ __global__ void k_mix_drhoij(const double2 *__restrict__ c0, const double2 *__re
 
 // density difference 2 sum_occ (2 Re(conj(t0) td) + |td|^2), complex64 inputs,
 // 16-orbital partial sums in FP32 added in FP64
-__global__ void k_mix_drho(const float2 *__restrict__ t0, const float2 *__restrict__ td, int norb, int64_t nn,
-                           double *__restrict__ out) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nn) return;
-  double acc = 0;
-  for (int o0 = 0; o0 < norb; o0 += 16) {
-    float part = 0.f;
-    const int o1 = min(norb, o0 + 16);
-    for (int o = o0; o < o1; o++) {
-      const float2 a = t0[(int64_t)o * nn + i], b = td[(int64_t)o * nn + i];
-      part += 2.f * (a.x * b.x + a.y * b.y) + b.x * b.x + b.y * b.y;
-    }
-    acc += (double)part;
-  }
-  out[i] = 2.0 * acc;
-}
-
 // renormalisation factors (nhat.f90:32-37) of both sets from the raw sums:
 // f0 = rnel / S0, f1 = rnel / (S0 + dS), df = f1 - f0 = -rnel dS / (S0 (S0 + dS))
 __global__ void k_mix_factors(const double *__restrict__ p0, const double *__restrict__ pd, int nb, double dv,
@@ -119,22 +109,72 @@ __global__ void k_mix_renorm(const double *__restrict__ r0raw, const double *__r
   ddens[i] = dr;
 }
 
-__device__ __forceinline__ double vxc_lda(double n) {
-  if (!(n > 1e-15)) return 0.0;
-  const double pi = 3.14159265358979323846;
-  const double vx = -cbrt(3.0 * n / pi);
-  const double A = 0.031091, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382, b4 = 0.49294;
-  const double rs = cbrt(3.0 / (4.0 * pi * n));
-  const double srs = sqrt(rs);
-  const double Q = 2.0 * A * (b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs);
-  const double dQ = 2.0 * A * (0.5 * b1 / srs + b2 + 1.5 * b3 * srs + 2.0 * b4 * rs);
-  const double lg = log(1.0 + 1.0 / Q);
-  const double ec = -2.0 * A * (1.0 + a1 * rs) * lg;
-  const double dec = -2.0 * A * a1 * lg + 2.0 * A * (1.0 + a1 * rs) * dQ / (Q * Q + Q);
-  return vx + (ec - rs / 3.0 * dec);
+// Slater + PW92 LDA (the formula of vxc_point in rebuild.cu) in FP32, and the difference
+// vxc(n0 + dn) - vxc(n0) from divided differences of every factor, so it
+// keeps the relative precision of dn instead of losing it to the cancellation
+// of two nearly equal potentials:
+//   u = n^1/3:  du = dn / (u1^2 + u1 u0 + u0^2),  d rs = -(3/4pi)^1/3 du / (u1 u0)
+//   d sqrt(rs) = d rs / (s1 + s0),  d(rs s) = d rs s1 + rs0 ds,  d(rs^2) = d rs (rs1 + rs0)
+//   d log(1 + 1/Q) = log1p(-dQ / (Q1 (Q0 + 1)))
+//   d(dQ/(Q(Q+1))) = (d(dQ) G0 - dQ0 dQ (Q1 + Q0 + 1)) / (G1 G0),  G = Q (Q + 1)
+// and products by d(ab) = da b1 + a0 db.
+struct LdaF {
+  float u, rs, s, Q, dQ, lg;
+};
+constexpr float kPwA = 0.031091f, kPwA1 = 0.21370f, kPwB1 = 7.5957f, kPwB2 = 3.5876f, kPwB3 = 1.6382f,
+                kPwB4 = 0.49294f;
+constexpr float kCx = 0.98474502184269641f;   // (3/pi)^(1/3)
+constexpr float kCrs = 0.62035049089940001f;  // (3/(4 pi))^(1/3)
+
+__device__ __forceinline__ LdaF lda_parts(float n) {
+  LdaF p;
+  p.u = cbrtf(n);
+  p.rs = kCrs / p.u;
+  p.s = sqrtf(p.rs);
+  p.Q = 2.f * kPwA * (kPwB1 * p.s + kPwB2 * p.rs + kPwB3 * p.rs * p.s + kPwB4 * p.rs * p.rs);
+  p.dQ = 2.f * kPwA * (0.5f * kPwB1 / p.s + kPwB2 + 1.5f * kPwB3 * p.s + 2.f * kPwB4 * p.rs);
+  p.lg = log1pf(1.f / p.Q);
+  return p;
 }
 
-// potentials of both sets: v0 = vH0 + vxc(n0 + nc) + vloc, dv = dvH + vxc(n1 + nc) - vxc(n0 + nc)
+__device__ __forceinline__ float lda_dec(const LdaF &p) {
+  return -2.f * kPwA * kPwA1 * p.lg + 2.f * kPwA * (1.f + kPwA1 * p.rs) * p.dQ / (p.Q * (p.Q + 1.f));
+}
+
+__device__ __forceinline__ float vxc_of_parts(const LdaF &p) {
+  const float ec = -2.f * kPwA * (1.f + kPwA1 * p.rs) * p.lg;
+  return -kCx * p.u + (ec - p.rs / 3.f * lda_dec(p));
+}
+
+__device__ __forceinline__ void vxc_pair_f(float n0, float dn, float &x0, float &dx) {
+  const float n1 = n0 + dn;
+  const bool ok0 = n0 > 1e-15f, ok1 = n1 > 1e-15f;
+  if (!ok0 || !ok1) {  // below the cut-off of vxc_point one of the two is zero
+    x0 = ok0 ? vxc_of_parts(lda_parts(n0)) : 0.f;
+    dx = (ok1 ? vxc_of_parts(lda_parts(n1)) : 0.f) - x0;
+    return;
+  }
+  const LdaF p0 = lda_parts(n0), p1 = lda_parts(n1);
+  x0 = vxc_of_parts(p0);
+  const float du = dn / (p1.u * p1.u + p1.u * p0.u + p0.u * p0.u);
+  const float dvx = -kCx * du;
+  const float drs = -kCrs * du / (p1.u * p0.u);
+  const float ds = drs / (p1.s + p0.s);
+  const float drss = drs * p1.s + p0.rs * ds;
+  const float drs2 = drs * (p1.rs + p0.rs);
+  const float dQ = 2.f * kPwA * (kPwB1 * ds + kPwB2 * drs + kPwB3 * drss + kPwB4 * drs2);
+  const float ddQ = 2.f * kPwA * (-0.5f * kPwB1 * ds / (p1.s * p0.s) + 1.5f * kPwB3 * ds + 2.f * kPwB4 * drs);
+  const float dlg = log1pf(-dQ / (p1.Q * (p0.Q + 1.f)));
+  const float dec_ = -2.f * kPwA * (kPwA1 * drs * p1.lg + (1.f + kPwA1 * p0.rs) * dlg);
+  const float G0 = p0.Q * (p0.Q + 1.f), G1 = p1.Q * (p1.Q + 1.f);
+  const float F1 = p1.dQ / G1;
+  const float dF = (ddQ * G0 - p0.dQ * dQ * (p1.Q + p0.Q + 1.f)) / (G1 * G0);
+  const float ddec = -2.f * kPwA * kPwA1 * dlg + 2.f * kPwA * (kPwA1 * drs * F1 + (1.f + kPwA1 * p0.rs) * dF);
+  dx = dvx + dec_ - (drs * lda_dec(p1) + p0.rs * ddec) / 3.f;
+}
+
+// potentials of both sets: v0 = vH0 + vxc(n0 + nc) + vloc, dv = dvH + vxc(n1 + nc) - vxc(n0 + nc),
+// the LDA terms in FP32 (vxc_pair_f), the sums in FP64
 __global__ void k_mix_pot(const double *__restrict__ dens0, const double *__restrict__ ddens,
                           const double *__restrict__ core, const double *__restrict__ vloc,
                           const double *__restrict__ vh0, const double *__restrict__ dvh, const double *__restrict__ mean,
@@ -143,16 +183,16 @@ __global__ void k_mix_pot(const double *__restrict__ dens0, const double *__rest
                           double *__restrict__ vxc1o, double *__restrict__ vh1o, int64_t n) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double n0 = dens0[i] + core[i];
-  const double x0 = vxc_lda(n0);
-  const double x1 = vxc_lda(n0 + ddens[i]);
+  float x0f, dxf;
+  vxc_pair_f(d2f(dens0[i] + core[i]), d2f(ddens[i]), x0f, dxf);
+  const double x0 = f2d(x0f), dxc = f2d(dxf);
   double h0 = vh0[i], dh = dvh[i];
   if (mean) {
     h0 -= mean[0];
     dh -= mean[1];
   }
   const double v0 = h0 + x0 + vloc[i];
-  const double dv = dh + (x1 - x0);
+  const double dv = dh + dxc;
   const double v1 = v0 + dv;
   vks0[i] = v0;
   vks1[i] = v1;
@@ -160,7 +200,7 @@ __global__ void k_mix_pot(const double *__restrict__ dens0, const double *__rest
   vks1f[i] = (float)v1;
   dvf[i] = (float)dv;
   vxc0o[i] = x0;
-  vxc1o[i] = x1;
+  vxc1o[i] = x0 + dxc;
   vh1o[i] = h0 + dh;
 }
 
@@ -180,34 +220,346 @@ __global__ void k_mix_ddij(const double *__restrict__ d0, const double *__restri
   if (t < nd) dd[t] = d1[t] - d0[t];
 }
 
-// RK4 stage of both sets (rk4.f90:44-48): k = -i shs(y); ksum (+)= w k; y = p + dts k
-__global__ void k_mix_stage(const float2 *__restrict__ k0r, const float2 *__restrict__ kdr,
-                            const float2 *__restrict__ p0, const float2 *__restrict__ d,
-                            float2 *__restrict__ ks0, float2 *__restrict__ ksd, float2 *__restrict__ y0,
-                            float2 *__restrict__ yd, int64_t n, float w, int first, float dts, int write_y) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float2 a = k0r[i], b = kdr[i];
-  const float ax = a.y, ay = -a.x, bx = b.y, by = -b.x;
-  float2 s0, sd;
-  if (first) {
-    s0 = make_float2(w * ax, w * ay);
-    sd = make_float2(w * bx, w * by);
+// ------------------------------------------------------------ stage algebra --
+// Every projection a stage needs follows from two gathers per set: S^-1/2 is
+// x + P1 diag(sigma) <p~1|x> (snphi.f90:23-46) and the nonlocal part of H is
+// P D <p~|t> (hphi.f90:31-64), so with the overlap blocks O_xy = <p_x|p_y>
+//   u  = H t = u' + P cD,            u' = F^-1 ek F t + v t (+ dv t0),  cD = D <p~|t>
+//   k  = S^-1/2 u = u' + P cD + P1 c2,   c2 = sigma (<p~1|u'> + O10 cD)
+//   <p~1|k> = q1 + O11 c2,  <p~|k> = <p~|u'> + O00 cD + O01 c2,  q1 = <p~1|u'> + O10 cD
+// and the next stage vector y = pf + dts (-i k) (rk4.f90:44-48) has
+//   t' = S^-1/2 y = pf + dts (-i k) + P1 c3,   c3 = sigma (<p~1|pf> + dts (-i <p~1|k>))
+//   <p~|t'> = <p~|pf> + dts (-i <p~|k>) + O01 c3.
+// The coefficient algebra is FP64; arrays are [set][orbital][slot].
+struct Ovl {
+  const int *start, *atom;
+  const int64_t *off;
+  const double *O[4];  // <p~|p~>, <p~|p~1>, <p~1|p~>, <p~1|p~1>
+  const int *ms, *slot_atom;
+  const int64_t *soff;
+};
+
+static Ovl ovl_of(const opaw_ctx *c) {
+  Ovl v;
+  v.start = c->d_ovl_start;
+  v.atom = c->d_ovl_atom;
+  v.off = c->d_ovl_off;
+  for (int k = 0; k < 4; k++) v.O[k] = c->d_ovl[k];
+  v.ms = c->d_ms;
+  v.slot_atom = c->d_slot_atom;
+  v.soff = c->d_soff;
+  return v;
+}
+
+// (O_k x)[a, i] for one orbital's slot vector x
+__device__ __forceinline__ double2 ovl_mv(const Ovl &v, int k, int a, int i, const double2 *__restrict__ x) {
+  double sx = 0, sy = 0;
+  for (int q = v.start[a]; q < v.start[a + 1]; q++) {
+    const int b = v.atom[q], mb = v.ms[b];
+    const double *Ob = v.O[k] + v.off[q] + (int64_t)i * mb;
+    const double2 *xb = x + v.soff[b];
+    for (int j = 0; j < mb; j++) {
+      sx += Ob[j] * xb[j].x;
+      sy += Ob[j] * xb[j].y;
+    }
+  }
+  return make_double2(sx, sy);
+}
+
+__device__ __forceinline__ double2 mi(double2 z) { return make_double2(z.y, -z.x); }  // -i z
+
+// thread (slot t, orbital o, set X); grid (ceil(ns/128), norb, 2)
+#define MC_SLOT()                                                  \
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;             \
+  if (t >= ns) return;                                             \
+  const int o = blockIdx.y, X = blockIdx.z;                        \
+  const int a = v.slot_atom[t];                                    \
+  const int i = t - (int)v.soff[a];                                \
+  const int64_t base = ((int64_t)X * norb + o) * ns;               \
+  const int64_t g0 = ((int64_t)(2 * X) * norb + o) * ns;           \
+  const int64_t g1 = ((int64_t)(2 * X + 1) * norb + o) * ns;       \
+  (void)i; (void)g0; (void)g1
+
+// q1 = <p~1|u'> + O10 cD, c2 = sigma q1
+__global__ void k_mc_c2(Ovl v, const double2 *__restrict__ G, const double2 *__restrict__ cD,
+                        const double *__restrict__ sigma, double2 *__restrict__ q1, double2 *__restrict__ c2, int norb,
+                        int ns) {
+  MC_SLOT();
+  const double2 m = ovl_mv(v, 2, a, i, cD + base);
+  const double2 q = make_double2(G[g1 + t].x + m.x, G[g1 + t].y + m.y);
+  q1[base + t] = q;
+  c2[base + t] = make_double2(sigma[t] * q.x, sigma[t] * q.y);
+}
+
+// <p~1|k>, <p~|k>; the packed box coefficients (-i cD, -i c2) of the fused
+// pass; with write_t also c3 and <p~|pf> + dts (-i <p~|k>)
+__global__ void k_mc_k(Ovl v, const double2 *__restrict__ G, const double2 *__restrict__ A,
+                       const double2 *__restrict__ cD, const double2 *__restrict__ q1, const double2 *__restrict__ c2,
+                       const double *__restrict__ sigma, double dts, int write_t, double2 *__restrict__ c3,
+                       double2 *__restrict__ pre, float4 *__restrict__ cab, int norb, int ns) {
+  MC_SLOT();
+  const double2 d = cD[base + t], e = c2[base + t];
+  const double2 al = mi(d), be = mi(e);
+  cab[base + t] = make_float4(d2f(al.x), d2f(al.y), d2f(be.x), d2f(be.y));
+  if (!write_t) return;
+  const double2 m11 = ovl_mv(v, 3, a, i, c2 + base);
+  const double2 m00 = ovl_mv(v, 0, a, i, cD + base);
+  const double2 m01 = ovl_mv(v, 1, a, i, c2 + base);
+  const double2 k1 = mi(make_double2(q1[base + t].x + m11.x, q1[base + t].y + m11.y));
+  const double2 k0 = mi(make_double2(G[g0 + t].x + m00.x + m01.x, G[g0 + t].y + m00.y + m01.y));
+  const double2 y1 = make_double2(A[g1 + t].x + dts * k1.x, A[g1 + t].y + dts * k1.y);
+  c3[base + t] = make_double2(sigma[t] * y1.x, sigma[t] * y1.y);
+  pre[base + t] = make_double2(A[g0 + t].x + dts * k0.x, A[g0 + t].y + dts * k0.y);
+}
+
+// start of a step: c3 = sigma <p~1|pf>, pre = <p~|pf>
+__global__ void k_mc_start(Ovl v, const double2 *__restrict__ A, const double *__restrict__ sigma,
+                           double2 *__restrict__ c3, double2 *__restrict__ pre, int norb, int ns) {
+  MC_SLOT();
+  const double2 p1 = A[g1 + t];
+  c3[base + t] = make_double2(sigma[t] * p1.x, sigma[t] * p1.y);
+  pre[base + t] = A[g0 + t];
+}
+
+// <p~|t'> = pre + O01 c3, and the box coefficient c3 of t'
+__global__ void k_mc_t(Ovl v, const double2 *__restrict__ pre, const double2 *__restrict__ c3,
+                       double2 *__restrict__ c0n, float2 *__restrict__ cg, int norb, int ns) {
+  MC_SLOT();
+  const double2 m = ovl_mv(v, 1, a, i, c3 + base);
+  c0n[base + t] = make_double2(pre[base + t].x + m.x, pre[base + t].y + m.y);
+  cg[base + t] = make_float2(d2f(c3[base + t].x), d2f(c3[base + t].y));
+}
+#undef MC_SLOT
+
+// The fused grid pass of a stage, one thread per grid point over every
+// orbital of both sets:
+//   kf  = -i u' + P (-i cD) + P1 (-i c2)          (= -i S^-1/2 H t)
+//   ks  = w kf  (first stage)  or  ks + w kf      (rk4.f90:44-48)
+//   t'  = pf + dts kf + P1 c3                      (S^-1/2 of the next y)
+// and the raw densities of t' (tddft_dens.f90:56-77): 2 sum |t0|^2 and the
+// difference 2 sum (2 Re conj(t0) td + |td|^2), orbital partial sums of 16 in
+// FP32 added in FP64.  At the start of a step (stage = 0) it only forms
+// t = pf + P1 c3 and the densities.  Two kernels split the grid: the points
+// outside every projector box (no box terms, two orbitals' loads in flight)
+// and the union points (projector values in registers, coefficients
+// through L1); together they write every point once.
+struct FusedArgs {
+  const float2 *u0, *ud, *pf0, *pfd;
+  float2 *ks0, *ksd, *t0, *td;
+  double *r0raw, *drraw;
+  int norb;
+  int64_t nn;
+  float w, dts;
+  int stage, first, write_t;
+};
+
+struct DensAcc {
+  double a0 = 0, ad = 0;
+  float p0 = 0.f, pd = 0.f;
+  int cnt = 0;
+  __device__ __forceinline__ void add(float2 x, float2 y) {
+    p0 += x.x * x.x + x.y * x.y;
+    pd += 2.f * (x.x * y.x + x.y * y.y) + y.x * y.x + y.y * y.y;
+    if (++cnt == 16) {
+      a0 += (double)p0;
+      ad += (double)pd;
+      p0 = pd = 0.f;
+      cnt = 0;
+    }
+  }
+  __device__ __forceinline__ void store(const FusedArgs &f, int64_t g) {
+    a0 += (double)p0;
+    ad += (double)pd;
+    f.r0raw[g] = 2.0 * a0;
+    f.drraw[g] = 2.0 * ad;
+  }
+};
+
+// one orbital of both sets at one point, given the loaded values and the box terms
+__device__ __forceinline__ void fused_one(const FusedArgs &f, int64_t idx, float2 a0, float2 ad, float2 q0, float2 qd,
+                                          float2 s0, float2 sd, const float2 *B, const float2 *Gt, DensAcc &acc) {
+  float2 tv0, tvd;
+  if (f.stage) {
+    const float2 k0 = make_float2(a0.y + B[0].x, -a0.x + B[0].y);
+    const float2 kd = make_float2(ad.y + B[1].x, -ad.x + B[1].y);
+    float2 n0 = make_float2(f.w * k0.x, f.w * k0.y), nd = make_float2(f.w * kd.x, f.w * kd.y);
+    if (!f.first) {
+      n0.x += s0.x;
+      n0.y += s0.y;
+      nd.x += sd.x;
+      nd.y += sd.y;
+    }
+    f.ks0[idx] = n0;
+    f.ksd[idx] = nd;
+    if (!f.write_t) return;
+    tv0 = make_float2(q0.x + f.dts * k0.x + Gt[0].x, q0.y + f.dts * k0.y + Gt[0].y);
+    tvd = make_float2(qd.x + f.dts * kd.x + Gt[1].x, qd.y + f.dts * kd.y + Gt[1].y);
   } else {
-    s0 = ks0[i];
-    sd = ksd[i];
-    s0.x += w * ax;
-    s0.y += w * ay;
-    sd.x += w * bx;
-    sd.y += w * by;
+    tv0 = make_float2(q0.x + Gt[0].x, q0.y + Gt[0].y);
+    tvd = make_float2(qd.x + Gt[1].x, qd.y + Gt[1].y);
   }
-  ks0[i] = s0;
-  ksd[i] = sd;
-  if (write_y) {
-    const float2 pv = p0[i], dvv = d[i];
-    y0[i] = make_float2(pv.x + dts * ax, pv.y + dts * ay);
-    yd[i] = make_float2(dvv.x + dts * bx, dvv.y + dts * by);
+  f.t0[idx] = tv0;
+  f.td[idx] = tvd;
+  acc.add(tv0, tvd);
+}
+
+__global__ void __launch_bounds__(256) k_mix_dense(FusedArgs f, const int *__restrict__ uidx) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= f.nn || uidx[g] >= 0) return;
+  const float2 zero = make_float2(0.f, 0.f);
+  const float2 B[2] = {zero, zero};
+  DensAcc acc;
+  for (int o = 0; o < f.norb; o += 2) {
+    const int nj = (o + 1 < f.norb) ? 2 : 1;
+    float2 a0[2], ad[2], q0[2], qd[2], s0[2], sd[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      a0[j] = ad[j] = q0[j] = qd[j] = s0[j] = sd[j] = zero;
+      if (j < nj) {
+        const int64_t idx = (int64_t)(o + j) * f.nn + g;
+        if (f.stage) {
+          a0[j] = f.u0[idx];
+          ad[j] = f.ud[idx];
+          if (!f.first) {
+            s0[j] = f.ks0[idx];
+            sd[j] = f.ksd[idx];
+          }
+        }
+        if (f.write_t) {
+          q0[j] = f.pf0[idx];
+          qd[j] = f.pfd[idx];
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 2; j++)
+      if (j < nj) fused_one(f, (int64_t)(o + j) * f.nn + g, a0[j], ad[j], q0[j], qd[j], s0[j], sd[j], B, B, acc);
   }
+  if (f.write_t) acc.store(f, g);
+}
+
+// union points: thread = (point, group of kBoxOrb orbitals); the group's
+// density partials (the same 16-orbital FP32 sums as above, kBoxOrb = 16) go
+// to bpart[group][u] and k_mix_box_dens adds them in group order in FP64
+constexpr int kBoxOrb = 16;
+
+template <int EMAX, int MSMAX>
+__global__ void __launch_bounds__(128)
+    k_mix_box(FusedArgs f, int nunion, const int *__restrict__ upt, const int *__restrict__ ustart,
+              const int *__restrict__ uatom, const int *__restrict__ ubox, const float *__restrict__ P0,
+              const float *__restrict__ P1, const int64_t *__restrict__ poff, const int *__restrict__ nrough,
+              const int *__restrict__ ms, const int64_t *__restrict__ soff, const float4 *__restrict__ cab,
+              const float2 *__restrict__ cg, int ns, double *__restrict__ bpart) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nunion) return;
+  const int gy = blockIdx.y;
+  const int oa = gy * kBoxOrb, ob = min(f.norb, oa + kBoxOrb);
+  const int64_t g = upt[u];
+  const int e0 = ustart[u], ne = ustart[u + 1] - e0;
+  const bool fast = ne <= EMAX;
+  float pa[EMAX][MSMAX], pb[EMAX][MSMAX];
+  int so[EMAX], mm[EMAX];
+#pragma unroll
+  for (int e = 0; e < EMAX; e++) {
+    mm[e] = 0;
+    so[e] = 0;
+    if (fast && e < ne) {
+      const int a = uatom[e0 + e], b = ubox[e0 + e];
+      const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+      mm[e] = ms[a];
+      so[e] = (int)soff[a];
+#pragma unroll
+      for (int i = 0; i < MSMAX; i++) {
+        pa[e][i] = (i < mm[e]) ? P0[poff[a] + (int64_t)i * nbox + b] : 0.f;
+        pb[e][i] = (i < mm[e]) ? P1[poff[a] + (int64_t)i * nbox + b] : 0.f;
+      }
+    }
+  }
+  const int64_t kstride = (int64_t)f.norb * ns;  // between the two sets
+  const float2 zero = make_float2(0.f, 0.f);
+  DensAcc acc;
+  for (int o = oa; o < ob; o++) {
+    const int64_t idx = (int64_t)o * f.nn + g;
+    // the grid values first: their loads overlap the coefficient sums below
+    float2 a0 = zero, ad = zero, q0 = zero, qd = zero, s0 = zero, sd = zero;
+    if (f.stage) {
+      a0 = f.u0[idx];
+      ad = f.ud[idx];
+      if (!f.first) {
+        s0 = f.ks0[idx];
+        sd = f.ksd[idx];
+      }
+    }
+    if (f.write_t) {
+      q0 = f.pf0[idx];
+      qd = f.pfd[idx];
+    }
+    float2 B[2] = {zero, zero}, Gt[2] = {zero, zero};
+#pragma unroll
+    for (int X = 0; X < 2; X++) {
+      const float4 *ab = cab + X * kstride + (int64_t)o * ns;
+      const float2 *gg = cg + X * kstride + (int64_t)o * ns;
+      if (fast) {
+#pragma unroll
+        for (int e = 0; e < EMAX; e++) {
+#pragma unroll
+          for (int i = 0; i < MSMAX; i++) {
+            if (i < mm[e]) {
+              const int sl = so[e] + i;
+              if (f.stage) {
+                const float4 q = ab[sl];
+                B[X].x += pa[e][i] * q.x + pb[e][i] * q.z;
+                B[X].y += pa[e][i] * q.y + pb[e][i] * q.w;
+              }
+              if (f.write_t) {
+                const float2 q = gg[sl];
+                Gt[X].x += pb[e][i] * q.x;
+                Gt[X].y += pb[e][i] * q.y;
+              }
+            }
+          }
+        }
+      } else {
+        for (int e = e0; e < e0 + ne; e++) {
+          const int a = uatom[e], b = ubox[e];
+          const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+          const int m = ms[a], s0i = (int)soff[a];
+          for (int i = 0; i < m; i++) {
+            const float p = P0[poff[a] + (int64_t)i * nbox + b], q1 = P1[poff[a] + (int64_t)i * nbox + b];
+            if (f.stage) {
+              const float4 q = ab[s0i + i];
+              B[X].x += p * q.x + q1 * q.z;
+              B[X].y += p * q.y + q1 * q.w;
+            }
+            if (f.write_t) {
+              const float2 q = gg[s0i + i];
+              Gt[X].x += q1 * q.x;
+              Gt[X].y += q1 * q.y;
+            }
+          }
+        }
+      }
+    }
+    fused_one(f, idx, a0, ad, q0, qd, s0, sd, B, Gt, acc);
+  }
+  if (f.write_t) {
+    // the group's FP32 partial: moved into a0/ad if the group was full
+    bpart[(int64_t)(2 * gy) * nunion + u] = acc.a0 + (double)acc.p0;
+    bpart[(int64_t)(2 * gy + 1) * nunion + u] = acc.ad + (double)acc.pd;
+  }
+}
+
+__global__ void k_mix_box_dens(const double *__restrict__ bpart, int ngroups, int nunion, const int *__restrict__ upt,
+                               double *__restrict__ r0raw, double *__restrict__ drraw) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nunion) return;
+  double a0 = 0, ad = 0;
+  for (int q = 0; q < ngroups; q++) {
+    a0 += bpart[(int64_t)(2 * q) * nunion + u];
+    ad += bpart[(int64_t)(2 * q + 1) * nunion + u];
+  }
+  r0raw[upt[u]] = 2.0 * a0;
+  drraw[upt[u]] = 2.0 * ad;
 }
 
 // Tail of the step.  FP64 arithmetic only where psi and delta are updated;
@@ -394,9 +746,15 @@ __global__ void k_mix_p1(const double2 *__restrict__ p0, const double2 *__restri
 struct Mix {
   int norb;
   int64_t tot;
-  float2 *y0, *yd, *k0, *kd, *ks0, *ksd, *t0, *td, *pf0, *pfd;
+  float2 *u0, *ud, *ks0, *ksd, *t0, *td, *pf0, *pfd;
   double2 *d;
-  double2 *c0, *cd;
+  double2 *c0, *cd;    // <p~|t> of both sets (current buffer of the pair)
+  double2 *cnext;      // the other buffer of the pair
+  double2 *G, *A;      // [set][table][orbital][slot]: gathers of u' and of pf
+  double2 *cD, *q1, *c2, *c3, *pre;  // [set][orbital][slot]
+  double *bpart;       // [orbital group][2][union point]: density partials of the box pass
+  float4 *cab;         // [set][orbital][slot]: (-i cD, -i c2) in FP32
+  float2 *cg;          // [set][orbital][slot]: c3 in FP32
   double *r0raw, *h0raw, *drraw, *dhraw, *src0, *srcd, *ddens, *vh0, *dvh;
   float *dvf;
   double *drhoij, *ddij, *fac, *part0, *partd, *mean, *npart0, *npart1, *nfac, *dpart;
@@ -406,16 +764,33 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
   m.norb = norb;
   m.tot = c->nn * (int64_t)norb;
   const size_t cb = sizeof(float2) * (size_t)m.tot;
-  float2 **cs[10] = {&m.y0, &m.yd, &m.k0, &m.kd, &m.ks0, &m.ksd, &m.t0, &m.td, &m.pf0, &m.pfd};
-  for (int i = 0; i < 10; i++) {
+  float2 **cs[8] = {&m.u0, &m.ud, &m.ks0, &m.ksd, &m.t0, &m.td, &m.pf0, &m.pfd};
+  for (int i = 0; i < 8; i++) {
     OPAW_CHECK(ensure(c->mix[i], cb));
     *cs[i] = (float2 *)c->mix[i].p;
   }
   OPAW_CHECK(ensure(c->mix[10], sizeof(double2) * (size_t)m.tot));
   m.d = (double2 *)c->mix[10].p;
-  OPAW_CHECK(ensure(c->mix[11], sizeof(double2) * (size_t)c->ns * norb * 2 + 32));
-  m.c0 = (double2 *)c->mix[11].p;
-  m.cd = m.c0 + (size_t)c->ns * norb;
+  const size_t sv = (size_t)c->ns * norb;  // one slot vector per orbital
+  // c0/cd pair x2, G (4 sv), A (4 sv), cD, q1, c2, c3, pre (2 sv each)
+  OPAW_CHECK(ensure(c->mix[11], sizeof(double2) * (sv * (4 + 4 + 4 + 10)) + 64));
+  double2 *q = (double2 *)c->mix[11].p;
+  m.c0 = q;
+  m.cd = q + sv;
+  m.cnext = q + 2 * sv;
+  m.G = q + 4 * sv;
+  m.A = q + 8 * sv;
+  m.cD = q + 12 * sv;
+  m.q1 = q + 14 * sv;
+  m.c2 = q + 16 * sv;
+  m.c3 = q + 18 * sv;
+  m.pre = q + 20 * sv;
+  OPAW_CHECK(ensure(c->mix[8], sizeof(double) * 2 * (size_t)((norb + kBoxOrb - 1) / kBoxOrb) * c->nunion + 64));
+  m.bpart = (double *)c->mix[8].p;
+  OPAW_CHECK(ensure(c->mix[14], sizeof(float4) * 2 * sv + 64));
+  m.cab = (float4 *)c->mix[14].p;
+  OPAW_CHECK(ensure(c->mix[15], sizeof(float2) * 2 * sv + 64));
+  m.cg = (float2 *)c->mix[15].p;
   OPAW_CHECK(ensure(c->mix[12], sizeof(double) * (size_t)c->nn * 9 + sizeof(float) * (size_t)c->nn + 64));
   double *r = (double *)c->mix[12].p;
   double **rs[9] = {&m.r0raw, &m.h0raw, &m.drraw, &m.dhraw, &m.src0, &m.srcd, &m.ddens, &m.vh0, &m.dvh};
@@ -424,8 +799,8 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
   const size_t nparts = (size_t)norb * kMixNormBlocks;
   const size_t small = 2 * (size_t)c->nd + 16 + 4 * kRedBlocks + 16 + 4 * nparts + 3 * (size_t)norb + 6 * nparts + 64;
   OPAW_CHECK(ensure(c->mix[13], sizeof(double) * small));
-  double *q = (double *)c->mix[13].p;
-  m.drhoij = q;
+  double *qq = (double *)c->mix[13].p;
+  m.drhoij = qq;
   m.ddij = m.drhoij + c->nd;
   m.fac = m.ddij + c->nd;
   m.part0 = m.fac + 16;
@@ -444,28 +819,125 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
     OPAW_CUDA(cudaGetLastError()); \
   } while (0)
 
-// rebuild of both sets from y0 and the difference yd: leaves t0 = S^-1/2 y0,
-// td = S^-1/2 yd and their projections c0, cd for the following shs
-static int mix_rebuild(opaw_ctx *c, Mix &m, const float2 *y0, const float2 *yd) {
+// the <p~|t'> just formed become the current pair
+static void mix_swap(Mix &m, size_t sv) {
+  double2 *cur = m.c0;
+  m.c0 = m.cnext;
+  m.cd = m.cnext + sv;
+  m.cnext = cur;
+}
+
+// the fused grid pass (start of a step: stage = 0)
+static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, float w, float dts) {
+  FusedArgs f;
+  f.u0 = m.u0;
+  f.ud = m.ud;
+  f.pf0 = m.pf0;
+  f.pfd = m.pfd;
+  f.ks0 = m.ks0;
+  f.ksd = m.ksd;
+  f.t0 = m.t0;
+  f.td = m.td;
+  f.r0raw = m.r0raw;
+  f.drraw = m.drraw;
+  f.norb = m.norb;
+  f.nn = c->nn;
+  f.w = w;
+  f.dts = dts;
+  f.stage = stage;
+  f.first = first;
+  f.write_t = write_t;
+  k_mix_dense<<<grid1(c->nn, 256), 256, 0, c->stream>>>(f, c->d_uidx);
+  MIX_LAUNCHED();
+  if (c->nunion > 0) {
+    const float *P0 = c->d_p3d_f, *P1 = c->d_p3d1_f;
+    const int ngroups = (m.norb + kBoxOrb - 1) / kBoxOrb;
+    const dim3 nb(grid1(c->nunion, 128), ngroups);
+    if (c->msmax <= 8)
+      k_mix_box<2, 8><<<nb, 128, 0, c->stream>>>(f, c->nunion, c->d_upt, c->d_ustart, c->d_uatom, c->d_ubox, P0, P1,
+                                                 c->d_poff, c->d_nrough, c->d_ms, c->d_soff, m.cab, m.cg, c->ns,
+                                                 m.bpart);
+    else
+      k_mix_box<1, 16><<<nb, 128, 0, c->stream>>>(f, c->nunion, c->d_upt, c->d_ustart, c->d_uatom, c->d_ubox, P0, P1,
+                                                  c->d_poff, c->d_nrough, c->d_ms, c->d_soff, m.cab, m.cg, c->ns,
+                                                  m.bpart);
+    MIX_LAUNCHED();
+    if (write_t) {
+      k_mix_box_dens<<<grid1(c->nunion, 256), 256, 0, c->stream>>>(m.bpart, ngroups, c->nunion, c->d_upt, m.r0raw,
+                                                                   m.drraw);
+      MIX_LAUNCHED();
+    }
+  }
+  return OPAW_OK;
+}
+
+// t = S^-1/2 pf of both sets at the start of a step, their <p~|t> and raw densities
+static int mix_start_t(opaw_ctx *c, Mix &m) {
+  const int norb = m.norb;
+  const size_t sv = (size_t)c->ns * norb;
+  if (c->ns > 0) {
+    OPAW_CHECK(gather2<float>(c, m.pf0, norb, m.A, m.A + sv));
+    OPAW_CHECK(gather2<float>(c, m.pfd, norb, m.A + 2 * sv, m.A + 3 * sv));
+    const Ovl v = ovl_of(c);
+    const dim3 g(grid1(c->ns, 128), norb, 2);
+    k_mc_start<<<g, 128, 0, c->stream>>>(v, m.A, c->d_sigma[1], m.c3, m.pre, norb, c->ns);
+    MIX_LAUNCHED();
+    k_mc_t<<<g, 128, 0, c->stream>>>(v, m.pre, m.c3, m.cnext, m.cg, norb, c->ns);
+    MIX_LAUNCHED();
+    mix_swap(m, sv);
+  }
+  return mix_fused(c, m, 0, 0, 1, 0.f, 0.f);
+}
+
+// one RK4 stage of both sets from t, <p~|t> and the rebuilt potentials: the
+// grid part of H, the two gathers, the FP64 algebra and the fused pass
+static int mix_stage(opaw_ctx *c, Mix &m, int st, float w, double dts) {
+  const int norb = m.norb;
+  const size_t sv = (size_t)c->ns * norb;
+  const int write_t = st < 3;
+  OPAW_CHECK(h_fft<float>(c, c->d_vks_f[0], m.t0, m.u0, norb, nullptr, nullptr));
+  OPAW_CHECK(h_fft<float>(c, c->d_vks_f[1], m.td, m.ud, norb, m.t0, m.dvf));
+  if (c->ns > 0) {
+    OPAW_CHECK(gather2<float>(c, m.u0, norb, m.G, m.G + sv));
+    OPAW_CHECK(gather2<float>(c, m.ud, norb, m.G + 2 * sv, m.G + 3 * sv));
+    // cD = D <p~|t> (unperturbed), D' <p~|td> + (D' - D) <p~|t0> (difference)
+    const dim3 gc(grid1(c->ns, 128), norb);
+    k_coef_dij<<<gc, 128, 0, c->stream>>>(m.c0, m.cD, norb, c->ns, c->d_slot_atom, c->d_soff, c->d_doff, c->d_ms,
+                                          c->d_dij[0]);
+    MIX_LAUNCHED();
+    k_coef_dij2<<<gc, 128, 0, c->stream>>>(m.cd, m.c0, m.cD + sv, norb, c->ns, c->d_slot_atom, c->d_soff, c->d_doff,
+                                           c->d_ms, c->d_dij[1], m.ddij);
+    MIX_LAUNCHED();
+    const Ovl v = ovl_of(c);
+    const dim3 g(grid1(c->ns, 128), norb, 2);
+    k_mc_c2<<<g, 128, 0, c->stream>>>(v, m.G, m.cD, c->d_sigma[1], m.q1, m.c2, norb, c->ns);
+    MIX_LAUNCHED();
+    k_mc_k<<<g, 128, 0, c->stream>>>(v, m.G, m.A, m.cD, m.q1, m.c2, c->d_sigma[1], dts, write_t, m.c3, m.pre, m.cab,
+                                     norb, c->ns);
+    MIX_LAUNCHED();
+    if (write_t) {
+      k_mc_t<<<g, 128, 0, c->stream>>>(v, m.pre, m.c3, m.cnext, m.cg, norb, c->ns);
+      MIX_LAUNCHED();
+      mix_swap(m, sv);
+    }
+  }
+  return mix_fused(c, m, 1, st == 0, write_t, w, (float)dts);
+}
+
+// the rest of the rebuild (ncpaw_make_hamiltonian.f90:119-129) from <p~|t>
+// and the raw densities of both sets: rho_ij, n^, renormalisation, Hartree,
+// v_ks, D_ij of both sets and their differences
+static int mix_potentials(opaw_ctx *c, Mix &m) {
   const int norb = m.norb;
   const int nb = grid1(c->nn, 256);
-  // unperturbed set (ncpaw_make_hamiltonian.f90:119-129)
-  OPAW_CHECK(sn_apply<float>(c, -0.5, y0, m.t0, norb));
-  OPAW_CHECK(gather<float>(c, 0, m.t0, norb, m.c0));
   OPAW_CHECK(rhoij_of(c, m.c0, norb, c->d_rhoij[0]));
-  OPAW_CHECK(density_raw<float>(c, m.t0, norb, m.r0raw));
   OPAW_CHECK(nhat_raw_of(c, c->d_rhoij[0], m.h0raw));
-  // differences
-  OPAW_CHECK(sn_apply<float>(c, -0.5, yd, m.td, norb));
-  OPAW_CHECK(gather<float>(c, 0, m.td, norb, m.cd));
   if (c->nd > 0) {
     k_mix_drhoij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(m.c0, m.cd, norb, c->ns, c->nd, c->d_dslot_atom,
                                                            c->d_soff, c->d_doff, c->d_ms, c->d_rhoij[0], m.drhoij,
                                                            c->d_rhoij[1]);
     MIX_LAUNCHED();
   }
-  k_mix_drho<<<nb, 256, 0, c->stream>>>(m.t0, m.td, norb, c->nn, m.drraw);
-  MIX_LAUNCHED();
   OPAW_CHECK(nhat_raw_of(c, m.drhoij, m.dhraw));  // n^ is linear in rho_ij
   // charge renormalisation of both sets
   OPAW_CHECK(sums2(c, m.h0raw, m.r0raw, m.part0));
@@ -503,17 +975,6 @@ static int mix_rebuild(opaw_ctx *c, Mix &m, const float2 *y0, const float2 *yd) 
   return OPAW_OK;
 }
 
-// S^-1/2 H S^-1/2 of both sets from t0, td and their projections
-static int mix_shs(opaw_ctx *c, Mix &m) {
-  const int norb = m.norb;
-  OPAW_CHECK(h_apply_ex<float>(c, c->d_vks_f[0], c->d_dij[0], m.t0, m.k0, norb, m.c0, nullptr, nullptr, nullptr,
-                               nullptr));
-  OPAW_CHECK(sn_apply<float>(c, -0.5, m.k0, m.k0, norb));
-  OPAW_CHECK(h_apply_ex<float>(c, c->d_vks_f[1], c->d_dij[1], m.td, m.kd, norb, m.cd, m.t0, m.dvf, m.c0, m.ddij));
-  OPAW_CHECK(sn_apply<float>(c, -0.5, m.kd, m.kd, norb));
-  return OPAW_OK;
-}
-
 int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev) {
   const int norb = c->norb[0];
   Mix m;
@@ -527,13 +988,12 @@ int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev
   const float wts[4] = {1.f, 2.f, 2.f, 1.f};
   const double dts[4] = {dt / 2.0, dt / 2.0, dt, dt};
   for (int it = 0; it < nsteps; it++) {
-    OPAW_CHECK(mix_rebuild(c, m, m.pf0, m.pfd));  // ncpaw_make_hamiltonian_tddft (tddft.f90:75)
+    // ncpaw_make_hamiltonian_tddft (tddft.f90:75)
+    OPAW_CHECK(mix_start_t(c, m));
+    OPAW_CHECK(mix_potentials(c, m));
     for (int st = 0; st < 4; st++) {
-      OPAW_CHECK(mix_shs(c, m));
-      k_mix_stage<<<nb, 256, 0, c->stream>>>(m.k0, m.kd, m.pf0, m.pfd, m.ks0, m.ksd, m.y0, m.yd, m.tot, wts[st],
-                                             st == 0, (float)dts[st], st < 3);
-      MIX_LAUNCHED();
-      if (st < 3) OPAW_CHECK(mix_rebuild(c, m, m.y0, m.yd));  // rk4.f90:53-55
+      OPAW_CHECK(mix_stage(c, m, st, wts[st], dts[st]));
+      if (st < 3) OPAW_CHECK(mix_potentials(c, m));  // rk4.f90:53-55
     }
     k_mix_final<<<gn, 256, 0, c->stream>>>(p0, m.d, m.ks0, m.ksd, c->nn, dt / 6.0, m.npart1);
     MIX_LAUNCHED();
