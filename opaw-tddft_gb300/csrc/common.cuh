@@ -183,6 +183,7 @@ struct opaw_ctx {
   int *d_boxg = nullptr;         // per atom and box point: the wrapped linear grid index
   int64_t *d_boff = nullptr;     // per atom offset into d_boxg
   int *d_uidx = nullptr;         // per grid point: its union index, -1 outside every box
+  int maxbox = 0;                // largest projector box (points)
   // projector overlaps <p_x|p_y> (x, y = p~ or p~1; FP64, dv included) as
   // dense ms_a x ms_b blocks for every pair of atoms whose boxes share a
   // grid point: block k of row atom a is (a, ovl_atom[k]) for k in
@@ -239,6 +240,7 @@ struct opaw_ctx {
   opaw::DeviceBuf gram, gramout; // Gram partials, small matrices
   opaw::DeviceBuf mix[16];       // buffers of the mixed-precision difference step
   opaw::DeviceBuf red;           // reductions
+  opaw::DeviceBuf g2part;        // segment partials of the two-table gather
   double *h_red = nullptr;       // pinned host mirror of small reductions
 };
 

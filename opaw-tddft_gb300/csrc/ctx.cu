@@ -91,6 +91,7 @@ static int build(opaw_ctx *c, const opaw_system *s) {
       c->h_ir0[3 * a + k] = i0;
       nbox *= nr;
     }
+    c->maxbox = std::max(c->maxbox, (int)nbox);
     c->msmax = std::max(c->msmax, m);
     c->h_poff[a + 1] = c->h_poff[a] + m * nbox;
     c->h_soff[a + 1] = c->h_soff[a] + m;
@@ -354,6 +355,7 @@ static void destroy(opaw_ctx *c) {
   for (int k = 0; k < 4; k++) cudaFree(c->d_ovl[k]);
   for (auto &b : c->mix) cudaFree(b.p);
   cudaFree(c->red.p);
+  cudaFree(c->g2part.p);
   if (c->h_red) cudaFreeHost(c->h_red);
   fft3_free(c->fft);
   fft3_free(c->fftb);

@@ -7,6 +7,8 @@
 // Every reduction runs in a fixed order (one warp per atom and orbital for
 // the box sums; one thread per grid point, atoms in order, for the scatter),
 // so FP64 results are bit-reproducible run to run.
+#include <algorithm>
+
 #include "fft.cuh"
 
 namespace opaw {
@@ -152,7 +154,7 @@ __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) 
               const R *__restrict__ P1, const int64_t *__restrict__ poff, const int *__restrict__ boxg,
               const int64_t *__restrict__ boff, const int *__restrict__ nrough, const int *__restrict__ ms,
               const int64_t *__restrict__ soff, double dv, double *__restrict__ out0, double *__restrict__ out1,
-              int ns) {
+              int ns, int nseg) {
   typedef typename Tr<R>::C C;
   constexpr int H = 2 * MSMAX;  // values per table: 2 i + re/im
   constexpr int NV = 2 * H;
@@ -161,12 +163,15 @@ __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) 
   constexpr int U = kG2Chunk / 32;  // points per lane and chunk
   static_assert(NV == 32 || NV == 64, "8 or 16 projectors per atom");
   __shared__ R sp[2][MSMAX][kG2Chunk];
-  const int a = blockIdx.x;
+  const int a = blockIdx.x / nseg, seg = blockIdx.x - a * nseg;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int o = blockIdx.y * kG2Warps + warp;
   const bool live = o < norb;  // idle warps still take part in the staging
   const int m = ms[a];
   const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+  // this CTA's segment of the box, whole chunks
+  const int seglen = (nbox + nseg * kG2Chunk - 1) / (nseg * kG2Chunk) * kG2Chunk;
+  const int b0 = seg * seglen, b1 = min(nbox, b0 + seglen);
   const int *bg = boxg + boff[a];
   const R *Pa = P0 + poff[a];
   const R *Qa = P1 + poff[a];
@@ -174,20 +179,20 @@ __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) 
   R v[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) v[k] = 0;
-  for (int c0 = 0; c0 < nbox; c0 += kG2Chunk) {
+  for (int c0 = b0; c0 < b1; c0 += kG2Chunk) {
     C z[U];
 #pragma unroll
     for (int k = 0; k < U; k++) {
       const int b = c0 + lane + 32 * k;
       z[k].x = z[k].y = (R)0;
-      if (live && b < nbox) z[k] = po[bg[b]];
+      if (live && b < b1) z[k] = po[bg[b]];
     }
     __syncthreads();  // the previous chunk's rows are no longer read
     for (int e = threadIdx.x; e < 2 * MSMAX * kG2Chunk; e += blockDim.x) {
       const int tab = e / (MSMAX * kG2Chunk), r = e - tab * (MSMAX * kG2Chunk);
       const int i = r / kG2Chunk, j = r - i * kG2Chunk;
       const int b = c0 + j;
-      sp[tab][i][j] = (i < m && b < nbox) ? (tab ? Qa : Pa)[(int64_t)i * nbox + b] : (R)0;
+      sp[tab][i][j] = (i < m && b < b1) ? (tab ? Qa : Pa)[(int64_t)i * nbox + b] : (R)0;
     }
     __syncthreads();
 #pragma unroll
@@ -210,25 +215,59 @@ __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) 
     const int idx = lane * PER + k;
     const int tab = idx / H, r = idx - tab * H;
     const int i = r >> 1;
-    if (i < m) (tab ? out1 : out0)[2 * ((int64_t)o * ns + soff[a] + i) + (r & 1)] = (double)v[k] * dv;
+    if (i < m) {
+      // segment partial: [seg][table][orbital][slot] (nseg = 1: the result itself)
+      double *dst = nseg == 1 ? (tab ? out1 : out0) : out0 + (int64_t)(2 * seg + tab) * 2 * norb * ns;
+      dst[2 * ((int64_t)o * ns + soff[a] + i) + (r & 1)] = (double)v[k] * dv;
+    }
   }
+}
+
+// sum of the segment partials in segment order
+__global__ void k_gather2_sum(const double2 *__restrict__ part, int nseg, int64_t n, double2 *__restrict__ out0,
+                              double2 *__restrict__ out1) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= 2 * n) return;
+  const int tab = (int)(t / n);
+  const int64_t j = t - tab * n;
+  double sx = 0, sy = 0;
+  for (int q = 0; q < nseg; q++) {
+    const double2 v = part[(int64_t)(2 * q + tab) * n + j];
+    sx += v.x;
+    sy += v.y;
+  }
+  (tab ? out1 : out0)[j] = make_double2(sx, sy);
 }
 
 template <typename R>
 int gather2(opaw_ctx *c, const typename Tr<R>::C *pin, int norb, double2 *c0, double2 *c1) {
   if (c->natom == 0) return OPAW_OK;
   const R *P0 = ProjTab<R>::get(c, 0), *P1 = ProjTab<R>::get(c, 1);
-  const dim3 grid(c->natom, (norb + kG2Warps - 1) / kG2Warps);
+  // segments of about 1024 points per box: enough CTAs to fill the GPU
+  const int nseg = std::max(1, std::min(8, c->maxbox / 1024));
+  const int64_t n = (int64_t)c->ns * norb;
+  double *o0 = (double *)c0, *o1 = (double *)c1;
+  if (nseg > 1) {
+    OPAW_CHECK(ensure(c->g2part, sizeof(double2) * 2 * (size_t)nseg * n + 64));
+    o0 = (double *)c->g2part.p;
+    o1 = nullptr;
+  }
+  const dim3 grid(c->natom * nseg, (norb + kG2Warps - 1) / kG2Warps);
   if (c->msmax <= 8)
     k_gather2<R, 8><<<grid, 32 * kG2Warps, 0, c->stream>>>(pin, c->nn, norb, P0, P1, c->d_poff, c->d_boxg,
-                                                           c->d_boff, c->d_nrough, c->d_ms, c->d_soff, c->dv,
-                                                           (double *)c0, (double *)c1, c->ns);
+                                                           c->d_boff, c->d_nrough, c->d_ms, c->d_soff, c->dv, o0, o1,
+                                                           c->ns, nseg);
   else
     k_gather2<R, 16><<<grid, 32 * kG2Warps, 0, c->stream>>>(pin, c->nn, norb, P0, P1, c->d_poff, c->d_boxg,
-                                                            c->d_boff, c->d_nrough, c->d_ms, c->d_soff, c->dv,
-                                                            (double *)c0, (double *)c1, c->ns);
+                                                            c->d_boff, c->d_nrough, c->d_ms, c->d_soff, c->dv, o0,
+                                                            o1, c->ns, nseg);
   c->launches++;
   OPAW_CUDA(cudaGetLastError());
+  if (nseg > 1) {
+    k_gather2_sum<<<grid1(2 * n, 256), 256, 0, c->stream>>>((const double2 *)c->g2part.p, nseg, n, c0, c1);
+    c->launches++;
+    OPAW_CUDA(cudaGetLastError());
+  }
   return OPAW_OK;
 }
 

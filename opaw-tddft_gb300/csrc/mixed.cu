@@ -338,8 +338,9 @@ __global__ void k_mc_t(Ovl v, const double2 *__restrict__ pre, const double2 *__
 //   t'  = pf + dts kf + P1 c3                      (S^-1/2 of the next y)
 // and the raw densities of t' (tddft_dens.f90:56-77): 2 sum |t0|^2 and the
 // difference 2 sum (2 Re conj(t0) td + |td|^2), orbital partial sums of 16 in
-// FP32 added in FP64.  At the start of a step (stage = 0) it only forms
-// t = pf + P1 c3 and the densities.  Two kernels split the grid: the points
+// FP32 added with a compensated FP32 sum (DensAcc).  At the start of a step
+// (stage = 0) it only forms t = pf + P1 c3 and the densities.  Two kernels
+// split the grid: the points
 // outside every projector box (no box terms, two orbitals' loads in flight)
 // and the union points (projector values in registers, coefficients
 // through L1); together they write every point once.
@@ -353,25 +354,38 @@ struct FusedArgs {
   int stage, first, write_t;
 };
 
+// Density accumulation without the FP64 pipe (1/64 of the FP32 rate here):
+// FP32 sums of 16 orbitals, the group sums added with a compensated FP32
+// two-sum (about 48 significant bits), converted to FP64 once per point.
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x) {
+  const float t = s + x;
+  const float bp = t - s;
+  c += (s - (t - bp)) + (x - bp);
+  s = t;
+}
+
 struct DensAcc {
-  double a0 = 0, ad = 0;
-  float p0 = 0.f, pd = 0.f;
+  float h0 = 0.f, l0 = 0.f, hd = 0.f, ld = 0.f;  // compensated sums of the group sums
+  float p0 = 0.f, pd = 0.f;                       // the current group of 16 orbitals
   int cnt = 0;
   __device__ __forceinline__ void add(float2 x, float2 y) {
     p0 += x.x * x.x + x.y * x.y;
     pd += 2.f * (x.x * y.x + x.y * y.y) + y.x * y.x + y.y * y.y;
-    if (++cnt == 16) {
-      a0 += (double)p0;
-      ad += (double)pd;
-      p0 = pd = 0.f;
-      cnt = 0;
-    }
+    if (++cnt == 16) flush();
   }
+  __device__ __forceinline__ void flush() {
+    two_sum_acc(h0, l0, p0);
+    two_sum_acc(hd, ld, pd);
+    p0 = pd = 0.f;
+    cnt = 0;
+  }
+  // 2 sum (occupation 2, tddft_dens.f90:73); scaling by 2 is exact in FP32
+  __device__ __forceinline__ double total0() { return f2d(2.f * h0) + f2d(2.f * l0); }
+  __device__ __forceinline__ double totald() { return f2d(2.f * hd) + f2d(2.f * ld); }
   __device__ __forceinline__ void store(const FusedArgs &f, int64_t g) {
-    a0 += (double)p0;
-    ad += (double)pd;
-    f.r0raw[g] = 2.0 * a0;
-    f.drraw[g] = 2.0 * ad;
+    flush();
+    f.r0raw[g] = total0();
+    f.drraw[g] = totald();
   }
 };
 
@@ -439,8 +453,8 @@ __global__ void __launch_bounds__(256) k_mix_dense(FusedArgs f, const int *__res
 }
 
 // union points: thread = (point, group of kBoxOrb orbitals); the group's
-// density partials (the same 16-orbital FP32 sums as above, kBoxOrb = 16) go
-// to bpart[group][u] and k_mix_box_dens adds them in group order in FP64
+// density sums (the same 16-orbital FP32 sums as above, kBoxOrb = 16) go to
+// bpart[group][u] and k_mix_box_dens adds them in group order in FP64
 constexpr int kBoxOrb = 16;
 
 template <int EMAX, int MSMAX>
@@ -543,9 +557,9 @@ __global__ void __launch_bounds__(128)
     fused_one(f, idx, a0, ad, q0, qd, s0, sd, B, Gt, acc);
   }
   if (f.write_t) {
-    // the group's FP32 partial: moved into a0/ad if the group was full
-    bpart[(int64_t)(2 * gy) * nunion + u] = acc.a0 + (double)acc.p0;
-    bpart[(int64_t)(2 * gy + 1) * nunion + u] = acc.ad + (double)acc.pd;
+    acc.flush();  // the group's sums (already doubled)
+    bpart[(int64_t)(2 * gy) * nunion + u] = acc.total0();
+    bpart[(int64_t)(2 * gy + 1) * nunion + u] = acc.totald();
   }
 }
 
@@ -558,8 +572,8 @@ __global__ void k_mix_box_dens(const double *__restrict__ bpart, int ngroups, in
     a0 += bpart[(int64_t)(2 * q) * nunion + u];
     ad += bpart[(int64_t)(2 * q + 1) * nunion + u];
   }
-  r0raw[upt[u]] = 2.0 * a0;
-  drraw[upt[u]] = 2.0 * ad;
+  r0raw[upt[u]] = a0;
+  drraw[upt[u]] = ad;
 }
 
 // Tail of the step.  FP64 arithmetic only where psi and delta are updated;
