@@ -321,6 +321,21 @@ __global__ void k_mc_start(Ovl v, const double2 *__restrict__ A, const double *_
   pre[base + t] = A[g0 + t];
 }
 
+// the gathers of the hi arrays restored like the arrays themselves:
+// <p|psi> = f0 <p|x>, <p|delta> = df <p|x> + f1 <p|y> (both tables)
+__global__ void k_mc_scale_a(double2 *__restrict__ A, const double *__restrict__ fac, int norb, int ns) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns) return;
+  const int o = blockIdx.y, tab = blockIdx.z;
+  const int64_t sv = (int64_t)norb * ns;
+  const double f0 = fac[3 * o], f1 = fac[3 * o + 1], df = fac[3 * o + 2];
+  double2 *a0 = A + (int64_t)tab * sv + (int64_t)o * ns + t;  // set 0, table tab
+  double2 *ad = A + (int64_t)(2 + tab) * sv + (int64_t)o * ns + t;
+  const double2 x = *a0, y = *ad;
+  *ad = make_double2(df * x.x + f1 * y.x, df * x.y + f1 * y.y);
+  *a0 = make_double2(f0 * x.x, f0 * x.y);
+}
+
 // <p~|t'> = pre + O01 c3, and the box coefficient c3 of t'
 __global__ void k_mc_t(Ovl v, const double2 *__restrict__ pre, const double2 *__restrict__ c3,
                        double2 *__restrict__ c0n, float2 *__restrict__ cg, int norb, int ns) {
@@ -345,7 +360,8 @@ __global__ void k_mc_t(Ovl v, const double2 *__restrict__ pre, const double2 *__
 // and the union points (projector values in registers, coefficients
 // through L1); together they write every point once.
 struct FusedArgs {
-  const float2 *u0, *ud, *pf0, *pfd;
+  const float2 *u0, *ud, *pf0, *pfd;  // pf: the hi arrays x, y of the state, restored on read
+  const float *facf;                  // per orbital f0, f1, df: psi = f0 x, delta = df x + f1 y
   float2 *ks0, *ksd, *t0, *td;
   double *r0raw, *drraw;
   int norb;
@@ -388,6 +404,13 @@ struct DensAcc {
     f.drraw[g] = totald();
   }
 };
+
+// the restored complex64 psi and delta of orbital o from the hi arrays
+__device__ __forceinline__ void restore_pf(const FusedArgs &f, int o, float2 x, float2 y, float2 &q0, float2 &qd) {
+  const float f0 = f.facf[3 * o], f1 = f.facf[3 * o + 1], df = f.facf[3 * o + 2];
+  q0 = make_float2(f0 * x.x, f0 * x.y);
+  qd = make_float2(df * x.x + f1 * y.x, df * x.y + f1 * y.y);
+}
 
 // one orbital of both sets at one point, given the loaded values and the box terms
 __device__ __forceinline__ void fused_one(const FusedArgs &f, int64_t idx, float2 a0, float2 ad, float2 q0, float2 qd,
@@ -447,6 +470,9 @@ __global__ void __launch_bounds__(256) k_mix_dense(FusedArgs f, const int *__res
     }
 #pragma unroll
     for (int j = 0; j < 2; j++)
+      if (j < nj && f.write_t) restore_pf(f, o + j, q0[j], qd[j], q0[j], qd[j]);
+#pragma unroll
+    for (int j = 0; j < 2; j++)
       if (j < nj) fused_one(f, (int64_t)(o + j) * f.nn + g, a0[j], ad[j], q0[j], qd[j], s0[j], sd[j], B, B, acc);
   }
   if (f.write_t) acc.store(f, g);
@@ -504,10 +530,7 @@ __global__ void __launch_bounds__(128)
         sd = f.ksd[idx];
       }
     }
-    if (f.write_t) {
-      q0 = f.pf0[idx];
-      qd = f.pfd[idx];
-    }
+    if (f.write_t) restore_pf(f, o, f.pf0[idx], f.pfd[idx], q0, qd);
     float2 B[2] = {zero, zero}, Gt[2] = {zero, zero};
 #pragma unroll
     for (int X = 0; X < 2; X++) {
@@ -600,22 +623,66 @@ struct NormAcc {
   }
 };
 
-// start of a call: delta = psi' - psi, their complex64 copies, norm partials
-__global__ void k_mix_start(const double2 *__restrict__ p0, const double2 *__restrict__ p1, double2 *__restrict__ d,
-                            float2 *__restrict__ pf0, float2 *__restrict__ pfd, int64_t nn,
-                            double *__restrict__ part) {
+// ---- the state of a call in float-float ------------------------------------
+// psi and delta live as unevaluated sums hi + lo of two FP32 arrays (about 48
+// significant bits) while a call runs: FP64 arithmetic runs at 1/64 of the
+// FP32 rate on this part, and the hi arrays are the complex64 copies every
+// stage reads.  The error-free products and sums use rounding intrinsics so
+// that no multiply-add contraction changes them.  The norm restore of
+// rk4.f90:92-102 is kept as per-orbital factors (f0, f1, df) that the next
+// update and every reader of the hi arrays apply: psi = f0 x,
+// psi' - psi = df x + f1 y.
+struct FF {
+  float h, l;
+};
+__device__ __forceinline__ FF ff_of(double v) {
+  const float h = d2f(v);
+  return {h, d2f(v - f2d(h))};
+}
+__device__ __forceinline__ double ff_val(FF a) { return f2d(a.h) + f2d(a.l); }
+__device__ __forceinline__ FF ff_norm(float p, float e) {
+  const float h = __fadd_rn(p, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, p))};
+}
+// a x (the a.l x.l term, below 2^-46 relative, dropped)
+__device__ __forceinline__ FF ff_mul(FF a, FF x) {
+  const float p = __fmul_rn(a.h, x.h);
+  float e = __fmaf_rn(a.h, x.h, -p);
+  e = __fmaf_rn(a.h, x.l, e);
+  e = __fmaf_rn(a.l, x.h, e);
+  return ff_norm(p, e);
+}
+// a s for an FP32 s
+__device__ __forceinline__ FF ff_mulf(FF a, float s) {
+  const float p = __fmul_rn(a.h, s);
+  float e = __fmaf_rn(a.h, s, -p);
+  e = __fmaf_rn(a.l, s, e);
+  return ff_norm(p, e);
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float t = __fadd_rn(a.h, b.h);
+  const float bp = __fsub_rn(t, a.h);
+  const float e = __fadd_rn(__fadd_rn(__fsub_rn(a.h, __fsub_rn(t, bp)), __fsub_rn(b.h, bp)), __fadd_rn(a.l, b.l));
+  return ff_norm(t, e);
+}
+
+// start of a call: x = psi, y = psi' - psi in float-float, norm partials (the
+// targets of every norm restore of the call, rk4.f90:16)
+__global__ void k_mix_start(const double2 *__restrict__ p0, const double2 *__restrict__ p1,
+                            float2 *__restrict__ xh, float2 *__restrict__ xl, float2 *__restrict__ yh,
+                            float2 *__restrict__ yl, int64_t nn, double *__restrict__ part) {
   __shared__ double sh[8];
   const int o = blockIdx.y;
   NormAcc acc;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = (int64_t)o * nn + g;
     const double2 x = p0[i], y1 = p1[i];
-    const double2 y = make_double2(y1.x - x.x, y1.y - x.y);
-    d[i] = y;
-    const float2 xf = make_float2(d2f(x.x), d2f(x.y)), yf = make_float2(d2f(y.x), d2f(y.y));
-    pf0[i] = xf;
-    pfd[i] = yf;
-    acc.add(xf, yf);
+    const FF ax = ff_of(x.x), ay = ff_of(x.y), bx = ff_of(y1.x - x.x), by = ff_of(y1.y - x.y);
+    xh[i] = make_float2(ax.h, ay.h);
+    xl[i] = make_float2(ax.l, ay.l);
+    yh[i] = make_float2(bx.h, by.h);
+    yl[i] = make_float2(bx.l, by.l);
+    acc.add(make_float2(ax.h, ay.h), make_float2(bx.h, by.h));
   }
   acc.flush();
   const double A = bsum(acc.A, sh), B = bsum(acc.B, sh);
@@ -625,83 +692,46 @@ __global__ void k_mix_start(const double2 *__restrict__ p0, const double2 *__res
   }
 }
 
-// final RK4 combination (rk4.f90:22) of both sets, in place, with the norm
-// partials of the results
-__global__ void k_mix_final(double2 *__restrict__ p0, double2 *__restrict__ d, const float2 *__restrict__ ks0,
-                            const float2 *__restrict__ ksd, int64_t nn, double h6, double *__restrict__ part) {
-  __shared__ double sh[8];
-  const int o = blockIdx.y;
-  NormAcc acc;
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = (int64_t)o * nn + g;
-    const float2 s0 = ks0[i], sd = ksd[i];
-    double2 x = p0[i], y = d[i];
-    x.x += h6 * f2d(s0.x);
-    x.y += h6 * f2d(s0.y);
-    y.x += h6 * f2d(sd.x);
-    y.y += h6 * f2d(sd.y);
-    p0[i] = x;
-    d[i] = y;
-    acc.add(make_float2(d2f(x.x), d2f(x.y)), make_float2(d2f(y.x), d2f(y.y)));
-  }
-  acc.flush();
-  const double A = bsum(acc.A, sh), B = bsum(acc.B, sh);
-  if (threadIdx.x == 0) {
-    part[((int64_t)o * gridDim.x + blockIdx.x) * 2] = A;
-    part[((int64_t)o * gridDim.x + blockIdx.x) * 2 + 1] = B;
-  }
-}
-
-// per-orbital norm-restore factors (rk4.f90:92-102) of both sets:
-// f0 = sqrt(A0/A1), f1 = sqrt((A0+B0)/(A1+B1)), df = f1 - f0 without cancellation
-__global__ void k_mix_nfac(const double *__restrict__ part0, const double *__restrict__ part1, int nb, int norb,
-                           double *__restrict__ fac) {
+// pending factors of a fresh call: no restore yet
+__global__ void k_mix_fac_init(double *__restrict__ fac, float *__restrict__ facf, int norb) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= norb) return;
-  double A0 = 0, B0 = 0, A1 = 0, B1 = 0;
-  for (int b = 0; b < nb; b++) {
-    A0 += part0[((int64_t)o * nb + b) * 2];
-    B0 += part0[((int64_t)o * nb + b) * 2 + 1];
-    A1 += part1[((int64_t)o * nb + b) * 2];
-    B1 += part1[((int64_t)o * nb + b) * 2 + 1];
-  }
-  const double f0 = sqrt(A0 / A1);
-  const double a = B0 / A0, bb = B1 / A1;
-  const double rm1 = (a - bb) / (1.0 + bb);  // r - 1, r = (1 + a) / (1 + b)
-  const double sr = sqrt(1.0 + rm1);
-  const double df = f0 * rm1 / (sr + 1.0);
-  fac[3 * o] = f0;
-  fac[3 * o + 1] = f0 + df;
-  fac[3 * o + 2] = df;
+  fac[3 * o] = facf[3 * o] = 1.f;
+  fac[3 * o + 1] = facf[3 * o + 1] = 1.f;
+  fac[3 * o + 2] = facf[3 * o + 2] = 0.f;
 }
 
-// norm restore p0 = f0 p0u, delta = df p0u + f1 du, fused with what the next
-// step reads first: complex64 copies, norm partials, and the dipole partials
-// of this step (tddft_plot.f90:40-57: dip = sum r rho0 dv, dip' - dip = sum r drho dv)
-__global__ void k_mix_rescale(double2 *__restrict__ p0, double2 *__restrict__ d, float2 *__restrict__ pf0,
-                              float2 *__restrict__ pfd, const double *__restrict__ fac, int64_t nn, int nx, int ny,
-                              int nz, float dx, float dy, float dz, double *__restrict__ npart,
-                              double *__restrict__ dpart) {
+// final RK4 combination (rk4.f90:22) of both sets from the restored start
+// values: x' = f0 x + h6 ks0, y' = df x + f1 y + h6 ksd (float-float), with
+// the norm partials and the dipole partials (tddft_plot.f90:40-57) of x', y':
+// per orbital sum r |x'|^2 and sum r (2 Re conj(x') y' + |y'|^2)
+__global__ void k_mix_final(float2 *__restrict__ xh, float2 *__restrict__ xl, float2 *__restrict__ yh,
+                            float2 *__restrict__ yl, const float2 *__restrict__ ks0, const float2 *__restrict__ ksd,
+                            const double *__restrict__ fac, double h6, int64_t nn, int nx, int ny, int nz, float dx,
+                            float dy, float dz, double *__restrict__ npart, double *__restrict__ dpart) {
   __shared__ double sh[8];
   const int o = blockIdx.y;
-  const double f0 = fac[3 * o], f1 = fac[3 * o + 1], df = fac[3 * o + 2];
+  const FF f0 = ff_of(fac[3 * o]), f1 = ff_of(fac[3 * o + 1]), df = ff_of(fac[3 * o + 2]), hh = ff_of(h6);
   NormAcc acc;
   double D[6] = {0, 0, 0, 0, 0, 0};
   float Df[6] = {0, 0, 0, 0, 0, 0};
   int nd = 0;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = (int64_t)o * nn + g;
-    const double2 x = p0[i], y = d[i];
-    const double2 a = make_double2(f0 * x.x, f0 * x.y);
-    const double2 b = make_double2(df * x.x + f1 * y.x, df * x.y + f1 * y.y);
-    p0[i] = a;
-    d[i] = b;
-    const float2 af = make_float2(d2f(a.x), d2f(a.y)), bf = make_float2(d2f(b.x), d2f(b.y));
-    pf0[i] = af;
-    pfd[i] = bf;
+    const float2 a = xh[i], al = xl[i], b = yh[i], bl = yl[i], s0 = ks0[i], sd = ksd[i];
+    const FF Xx{a.x, al.x}, Xy{a.y, al.y}, Yx{b.x, bl.x}, Yy{b.y, bl.y};
+    const FF nxx = ff_add(ff_mul(f0, Xx), ff_mulf(hh, s0.x));
+    const FF nxy = ff_add(ff_mul(f0, Xy), ff_mulf(hh, s0.y));
+    const FF nyx = ff_add(ff_add(ff_mul(df, Xx), ff_mul(f1, Yx)), ff_mulf(hh, sd.x));
+    const FF nyy = ff_add(ff_add(ff_mul(df, Xy), ff_mul(f1, Yy)), ff_mulf(hh, sd.y));
+    const float2 af = make_float2(nxx.h, nxy.h), bf = make_float2(nyx.h, nyy.h);
+    xh[i] = af;
+    xl[i] = make_float2(nxx.l, nxy.l);
+    yh[i] = bf;
+    yl[i] = make_float2(nyx.l, nyy.l);
+    acc.add(af, bf);
     const float rho = af.x * af.x + af.y * af.y;
     const float drho = 2.f * (af.x * bf.x + af.y * bf.y) + bf.x * bf.x + bf.y * bf.y;
-    acc.add(af, bf);
     const int gi = (int)g, gxy = gi / nx;
     const int gx = gi - gxy * nx, gz = gxy / ny, gy = gxy - gz * ny;
     const float r[3] = {(float)(gx - nx / 2) * dx, (float)(gy - ny / 2) * dy, (float)(gz - nz / 2) * dz};
@@ -734,7 +764,50 @@ __global__ void k_mix_rescale(double2 *__restrict__ p0, double2 *__restrict__ d,
   }
 }
 
-// dipoles from the (orbital, block) partials: out[0..2] dip, [3..5] dip', [6..8] d_dip
+// per-orbital norm-restore factors (rk4.f90:92-102) of both sets against the
+// norms at the start of the call: f0 = sqrt(A0/A1),
+// f1 = sqrt((A0+B0)/(A1+B1)), df = f1 - f0 without cancellation
+__global__ void k_mix_nfac(const double *__restrict__ part0, const double *__restrict__ part1, int nb, int norb,
+                           double *__restrict__ fac, float *__restrict__ facf) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= norb) return;
+  double A0 = 0, B0 = 0, A1 = 0, B1 = 0;
+  for (int b = 0; b < nb; b++) {
+    A0 += part0[((int64_t)o * nb + b) * 2];
+    B0 += part0[((int64_t)o * nb + b) * 2 + 1];
+    A1 += part1[((int64_t)o * nb + b) * 2];
+    B1 += part1[((int64_t)o * nb + b) * 2 + 1];
+  }
+  const double f0 = sqrt(A0 / A1);
+  const double a = B0 / A0, bb = B1 / A1;
+  const double rm1 = (a - bb) / (1.0 + bb);  // r - 1, r = (1 + a) / (1 + b)
+  const double sr = sqrt(1.0 + rm1);
+  const double df = f0 * rm1 / (sr + 1.0);
+  fac[3 * o] = f0;
+  fac[3 * o + 1] = f0 + df;
+  fac[3 * o + 2] = df;
+  facf[3 * o] = d2f(f0);
+  facf[3 * o + 1] = d2f(f0 + df);
+  facf[3 * o + 2] = d2f(df);
+}
+
+// per-orbital dipole terms of the restored state: dip = f0^2 Sxx,
+// dip' - dip = (f1^2 - f0^2) Sxx + f1^2 Sxy, f1^2 - f0^2 = df (2 f0 + df)
+__global__ void k_mix_dip_orb(const double *__restrict__ dpart, const double *__restrict__ fac, int nb, int norb,
+                              double *__restrict__ dorb) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= norb) return;
+  double S[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < nb; b++)
+    for (int k = 0; k < 6; k++) S[k] += dpart[((int64_t)o * nb + b) * 6 + k];
+  const double f0 = fac[3 * o], f1 = fac[3 * o + 1], df = fac[3 * o + 2];
+  for (int k = 0; k < 3; k++) {
+    dorb[6 * (int64_t)o + k] = f0 * f0 * S[k];
+    dorb[6 * (int64_t)o + 3 + k] = df * (2.0 * f0 + df) * S[k] + f1 * f1 * S[3 + k];
+  }
+}
+
+// dipoles from the per-orbital terms: out[0..2] dip, [3..5] dip', [6..8] d_dip
 __global__ void k_mix_dip_final(const double *__restrict__ part, int nparts, double gamma, double dv,
                                 double *__restrict__ out) {
   __shared__ double sh[8];
@@ -749,19 +822,28 @@ __global__ void k_mix_dip_final(const double *__restrict__ part, int nparts, dou
   }
 }
 
-// psi' = psi + delta (once at the end of a call)
-__global__ void k_mix_p1(const double2 *__restrict__ p0, const double2 *__restrict__ d, double2 *__restrict__ p1,
-                         int64_t n) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) p1[i] = make_double2(p0[i].x + d[i].x, p0[i].y + d[i].y);
+// end of a call: the restored psi = f0 x and psi' = f1 (x + y) back to FP64
+__global__ void k_mix_end(double2 *__restrict__ p0, double2 *__restrict__ p1, const float2 *__restrict__ xh,
+                          const float2 *__restrict__ xl, const float2 *__restrict__ yh, const float2 *__restrict__ yl,
+                          const double *__restrict__ fac, int64_t nn) {
+  const int o = blockIdx.y;
+  const FF f0 = ff_of(fac[3 * o]), f1 = ff_of(fac[3 * o + 1]);
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = (int64_t)o * nn + g;
+    const float2 a = xh[i], al = xl[i], b = yh[i], bl = yl[i];
+    const FF Xx{a.x, al.x}, Xy{a.y, al.y}, Yx{b.x, bl.x}, Yy{b.y, bl.y};
+    p0[i] = make_double2(ff_val(ff_mul(f0, Xx)), ff_val(ff_mul(f0, Xy)));
+    p1[i] = make_double2(ff_val(ff_mul(f1, ff_add(Xx, Yx))), ff_val(ff_mul(f1, ff_add(Xy, Yy))));
+  }
 }
 
 // ----------------------------------------------------------------- driver --
 struct Mix {
   int norb;
   int64_t tot;
-  float2 *u0, *ud, *ks0, *ksd, *t0, *td, *pf0, *pfd;
-  double2 *d;
+  float2 *u0, *ud, *ks0, *ksd, *t0, *td;
+  float2 *pf0, *pfd;   // the hi arrays of the state x (psi), y (delta)
+  float2 *xl, *yl;     // their lo arrays
   double2 *c0, *cd;    // <p~|t> of both sets (current buffer of the pair)
   double2 *cnext;      // the other buffer of the pair
   double2 *G, *A;      // [set][table][orbital][slot]: gathers of u' and of pf
@@ -771,7 +853,8 @@ struct Mix {
   float2 *cg;          // [set][orbital][slot]: c3 in FP32
   double *r0raw, *h0raw, *drraw, *dhraw, *src0, *srcd, *ddens, *vh0, *dvh;
   float *dvf;
-  double *drhoij, *ddij, *fac, *part0, *partd, *mean, *npart0, *npart1, *nfac, *dpart;
+  double *drhoij, *ddij, *fac, *part0, *partd, *mean, *npart0, *npart1, *nfac, *dpart, *dorb;
+  float *facf;         // FP32 copy of nfac
 };
 
 static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
@@ -783,8 +866,9 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
     OPAW_CHECK(ensure(c->mix[i], cb));
     *cs[i] = (float2 *)c->mix[i].p;
   }
-  OPAW_CHECK(ensure(c->mix[10], sizeof(double2) * (size_t)m.tot));
-  m.d = (double2 *)c->mix[10].p;
+  OPAW_CHECK(ensure(c->mix[10], 2 * sizeof(float2) * (size_t)m.tot));
+  m.xl = (float2 *)c->mix[10].p;
+  m.yl = m.xl + m.tot;
   const size_t sv = (size_t)c->ns * norb;  // one slot vector per orbital
   // c0/cd pair x2, G (4 sv), A (4 sv), cD, q1, c2, c3, pre (2 sv each)
   OPAW_CHECK(ensure(c->mix[11], sizeof(double2) * (sv * (4 + 4 + 4 + 10)) + 64));
@@ -811,7 +895,8 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
   for (int i = 0; i < 9; i++) *rs[i] = r + (size_t)i * c->nn;
   m.dvf = (float *)(r + (size_t)9 * c->nn);
   const size_t nparts = (size_t)norb * kMixNormBlocks;
-  const size_t small = 2 * (size_t)c->nd + 16 + 4 * kRedBlocks + 16 + 4 * nparts + 3 * (size_t)norb + 6 * nparts + 64;
+  const size_t small = 2 * (size_t)c->nd + 16 + 4 * kRedBlocks + 16 + 4 * nparts + 3 * (size_t)norb + 6 * nparts +
+                       6 * (size_t)norb + 2 * (size_t)norb + 64;
   OPAW_CHECK(ensure(c->mix[13], sizeof(double) * small));
   double *qq = (double *)c->mix[13].p;
   m.drhoij = qq;
@@ -824,6 +909,8 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
   m.npart1 = m.npart0 + 2 * nparts;
   m.nfac = m.npart1 + 2 * nparts;
   m.dpart = m.nfac + 3 * (size_t)norb;
+  m.dorb = m.dpart + 6 * nparts;
+  m.facf = (float *)(m.dorb + 6 * (size_t)norb);
   return OPAW_OK;
 }
 
@@ -848,6 +935,7 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
   f.ud = m.ud;
   f.pf0 = m.pf0;
   f.pfd = m.pfd;
+  f.facf = m.facf;
   f.ks0 = m.ks0;
   f.ksd = m.ksd;
   f.t0 = m.t0;
@@ -894,6 +982,8 @@ static int mix_start_t(opaw_ctx *c, Mix &m) {
     OPAW_CHECK(gather2<float>(c, m.pfd, norb, m.A + 2 * sv, m.A + 3 * sv));
     const Ovl v = ovl_of(c);
     const dim3 g(grid1(c->ns, 128), norb, 2);
+    k_mc_scale_a<<<g, 128, 0, c->stream>>>(m.A, m.nfac, norb, c->ns);
+    MIX_LAUNCHED();
     k_mc_start<<<g, 128, 0, c->stream>>>(v, m.A, c->d_sigma[1], m.c3, m.pre, norb, c->ns);
     MIX_LAUNCHED();
     k_mc_t<<<g, 128, 0, c->stream>>>(v, m.pre, m.c3, m.cnext, m.cg, norb, c->ns);
@@ -993,11 +1083,12 @@ int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev
   const int norb = c->norb[0];
   Mix m;
   OPAW_CHECK(mix_bufs(c, norb, m));
-  const int nb = grid1(m.tot, 256);
   double2 *p0 = c->d_psi[0], *p1 = c->d_psi[1];
   const dim3 gn(kMixNormBlocks, norb);
-  // delta = psi' - psi, complex64 copies, norms of the step start (rk4.f90:16)
-  k_mix_start<<<gn, 256, 0, c->stream>>>(p0, p1, m.d, m.pf0, m.pfd, c->nn, m.npart0);
+  // x = psi, y = psi' - psi in float-float, the norms to restore (rk4.f90:16)
+  k_mix_start<<<gn, 256, 0, c->stream>>>(p0, p1, m.pf0, m.xl, m.pfd, m.yl, c->nn, m.npart0);
+  MIX_LAUNCHED();
+  k_mix_fac_init<<<grid1(norb, 128), 128, 0, c->stream>>>(m.nfac, m.facf, norb);
   MIX_LAUNCHED();
   const float wts[4] = {1.f, 2.f, 2.f, 1.f};
   const double dts[4] = {dt / 2.0, dt / 2.0, dt, dt};
@@ -1009,17 +1100,17 @@ int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev
       OPAW_CHECK(mix_stage(c, m, st, wts[st], dts[st]));
       if (st < 3) OPAW_CHECK(mix_potentials(c, m));  // rk4.f90:53-55
     }
-    k_mix_final<<<gn, 256, 0, c->stream>>>(p0, m.d, m.ks0, m.ksd, c->nn, dt / 6.0, m.npart1);
+    k_mix_final<<<gn, 256, 0, c->stream>>>(m.pf0, m.xl, m.pfd, m.yl, m.ks0, m.ksd, m.nfac, dt / 6.0, c->nn, c->nx,
+                                           c->ny, c->nz, (float)c->dx, (float)c->dy, (float)c->dz, m.npart1, m.dpart);
     MIX_LAUNCHED();
-    k_mix_nfac<<<grid1(norb, 128), 128, 0, c->stream>>>(m.npart0, m.npart1, kMixNormBlocks, norb, m.nfac);
+    k_mix_nfac<<<grid1(norb, 128), 128, 0, c->stream>>>(m.npart0, m.npart1, kMixNormBlocks, norb, m.nfac, m.facf);
     MIX_LAUNCHED();
-    k_mix_rescale<<<gn, 256, 0, c->stream>>>(p0, m.d, m.pf0, m.pfd, m.nfac, c->nn, c->nx, c->ny, c->nz, (float)c->dx,
-                                             (float)c->dy, (float)c->dz, m.npart0, m.dpart);
+    k_mix_dip_orb<<<grid1(norb, 128), 128, 0, c->stream>>>(m.dpart, m.nfac, kMixNormBlocks, norb, m.dorb);
     MIX_LAUNCHED();
-    k_mix_dip_final<<<1, 256, 0, c->stream>>>(m.dpart, norb * kMixNormBlocks, gamma, c->dv, dd_dev + 9 * (size_t)it);
+    k_mix_dip_final<<<1, 256, 0, c->stream>>>(m.dorb, norb, gamma, c->dv, dd_dev + 9 * (size_t)it);
     MIX_LAUNCHED();
   }
-  k_mix_p1<<<nb, 256, 0, c->stream>>>(p0, m.d, p1, m.tot);  // psi' = psi + delta
+  k_mix_end<<<gn, 256, 0, c->stream>>>(p0, p1, m.pf0, m.xl, m.pfd, m.yl, m.nfac, c->nn);
   MIX_LAUNCHED();
   return OPAW_OK;
 }
