@@ -154,6 +154,7 @@ struct opaw_ctx {
   int64_t nn;
   double dx, dy, dz, dv, ekcut, rnel, dij_max;
   int scale_vh, periodic;
+  int nsm = 0;  // multiprocessors of the context's device
   int nxb, nyb, nzb;
   int64_t nnb;
   int natom;

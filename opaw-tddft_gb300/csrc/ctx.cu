@@ -65,6 +65,11 @@ static int build(opaw_ctx *c, const opaw_system *s) {
   c->nnb = (int64_t)c->nxb * c->nyb * c->nzb;
   c->natom = s->natom;
   OPAW_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  {
+    int dev = 0;
+    OPAW_CUDA(cudaGetDevice(&dev));
+    OPAW_CUDA(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
 
   const int na = s->natom;
   c->h_ms.assign(s->ms, s->ms + na);

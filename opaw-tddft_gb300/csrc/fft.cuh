@@ -9,6 +9,7 @@
 // (lib/library_fftw_v3.f90:56-83): unnormalised, forward sign -1, backward +1.
 #pragma once
 
+#include <algorithm>
 #include <type_traits>
 #include <utility>
 
@@ -352,6 +353,12 @@ template <typename C> __device__ __forceinline__ void cp_async_elem(C *smem, con
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// asynchronous prefetch of a contiguous range into L2 (16-byte aligned start,
+// size a multiple of 16 bytes); no data reaches the SM
+__device__ __forceinline__ void l2_prefetch_bulk(const void *gmem, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(gmem), "r"(bytes) : "memory");
+}
+
 
 template <typename C> struct OpCopy {
   const C *src;
@@ -458,20 +465,10 @@ template <typename C, int N, int TL, int NT, int S> struct CtStages {
   }
 };
 
-template <typename C, int N, int TL, int AXIS, class Op>
-__global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, int sign, const C *__restrict__ twg, Op op) {
-  constexpr int NT = 256;
-  constexpr int LS = TL + 1;
-  static_assert(ct_nstage(N) > 0, "unsupported length");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *tw = reinterpret_cast<C *>(smem_raw);
-  C *bufa = tw + N;
-  C *bufb = bufa + N * LS;
-  for (int t = threadIdx.x; t < N; t += NT) tw[t] = twg[t];
-  const int b = blockIdx.y;
-  const int tile = blockIdx.x;
-  int64_t base;
-  int lstride, jstride, nl;
+// the lines of tile `tile` of an axis pass: first element, strides, count
+template <int N, int TL, int AXIS>
+__device__ __forceinline__ void ct_tile_geom(const Dims3 &d, int tile, int64_t &base, int &lstride, int &jstride,
+                                             int &nl) {
   if (AXIS == 0) {
     const int nlines = d.n1 * d.n2;
     const int l0 = tile * TL;
@@ -495,6 +492,23 @@ __global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, int sign, const C *__re
     lstride = 1;
     jstride = d.n0 * d.n1;
   }
+}
+
+template <typename C, int N, int TL, int AXIS, class Op>
+__global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, int sign, const C *__restrict__ twg, Op op) {
+  constexpr int NT = 256;
+  constexpr int LS = TL + 1;
+  static_assert(ct_nstage(N) > 0, "unsupported length");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *tw = reinterpret_cast<C *>(smem_raw);
+  C *bufa = tw + N;
+  C *bufb = bufa + N * LS;
+  for (int t = threadIdx.x; t < N; t += NT) tw[t] = twg[t];
+  const int b = blockIdx.y;
+  const int tile = blockIdx.x;
+  int64_t base;
+  int lstride, jstride, nl;
+  ct_tile_geom<N, TL, AXIS>(d, tile, base, lstride, jstride, nl);
   constexpr int TOT = TL * N;
   if constexpr (HasRaw<Op>::value) {
     const C *src = op.raw(b);
@@ -583,7 +597,7 @@ int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const
 // butterfly inputs in registers between two barriers and writes in place.
 // ------------------------------------------------------------------------
 template <typename C, int N, int NLINES, int LSL, int LSE, int NT, int S>
-__device__ __forceinline__ void xy_stage(C *__restrict__ buf, const C *tw, int sign) {
+__device__ __forceinline__ void xy_stage(C *__restrict__ buf, const C *tw, int sign, int tid) {
   constexpr int R = ct_radix(N, S);
   constexpr int P = ct_pre(N, S);
   constexpr int M = N / R;
@@ -593,7 +607,7 @@ __device__ __forceinline__ void xy_stage(C *__restrict__ buf, const C *tw, int s
   C u[B][R];
 #pragma unroll
   for (int k = 0; k < B; k++) {
-    const int bf = threadIdx.x + k * NT;
+    const int bf = tid + k * NT;
     if (bf < TOT) {
       const int line = bf % NLINES, i = bf / NLINES;
 #pragma unroll
@@ -603,7 +617,7 @@ __device__ __forceinline__ void xy_stage(C *__restrict__ buf, const C *tw, int s
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < B; k++) {
-    const int bf = threadIdx.x + k * NT;
+    const int bf = tid + k * NT;
     if (bf < TOT) {
       const int line = bf % NLINES, i = bf / NLINES;
       const int kk = i % P;
@@ -621,16 +635,17 @@ __device__ __forceinline__ void xy_stage(C *__restrict__ buf, const C *tw, int s
 }
 
 template <typename C, int N, int NLINES, int LSL, int LSE, int NT, int S> struct XyStages {
-  static __device__ __forceinline__ void run(C *buf, const C *tw, int sign) {
+  static __device__ __forceinline__ void run(C *buf, const C *tw, int sign, int tid = threadIdx.x) {
     if constexpr (S < ct_nstage(N)) {
-      xy_stage<C, N, NLINES, LSL, LSE, NT, S>(buf, tw, sign);
-      XyStages<C, N, NLINES, LSL, LSE, NT, S + 1>::run(buf, tw, sign);
+      xy_stage<C, N, NLINES, LSL, LSE, NT, S>(buf, tw, sign, tid);
+      XyStages<C, N, NLINES, LSL, LSE, NT, S + 1>::run(buf, tw, sign, tid);
     }
   }
 };
 
 template <typename C, int NX, int NY, class Op>
-__global__ void __launch_bounds__(384, 2) k_fft_xy(int sign, const C *__restrict__ twx, const C *__restrict__ twy, Op op) {
+__global__ void __launch_bounds__(384, 2)
+    k_fft_xy(int sign, const C *__restrict__ twx, const C *__restrict__ twy, Op op, int ahead) {
   constexpr int NT = 384;
   constexpr int LX = NX + 1;  // odd row stride
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -643,6 +658,18 @@ __global__ void __launch_bounds__(384, 2) k_fft_xy(int sign, const C *__restrict
   const int64_t base = (int64_t)blockIdx.x * NX * NY;
   constexpr int TOT = NX * NY;
   constexpr int CH = 8;  // elements per thread whose loads are issued together
+  if (threadIdx.x == 0) {
+    // L2 prefetch of the plane of the CTA that starts one resident wave later
+    // (CTAs start roughly in linear order)
+    if constexpr (HasRaw<Op>::value && !HasPre<Op>::value) {  // measured: helps plain copies only
+      const int nxt = blockIdx.y * gridDim.x + blockIdx.x + ahead;
+      if (ahead > 0 && nxt < (int)(gridDim.x * gridDim.y)) {
+        const int bn = nxt / gridDim.x;
+        const C *q = op.raw(bn) + (int64_t)(nxt - bn * gridDim.x) * TOT;
+        if (((uintptr_t)q & 15) == 0 && (TOT * sizeof(C)) % 16 == 0) l2_prefetch_bulk(q, TOT * sizeof(C));
+      }
+    }
+  }
   if constexpr (HasRaw<Op>::value) {
     const C *src = op.raw(b) + base;
 #pragma unroll 8
@@ -715,7 +742,7 @@ int launch_xy(opaw_ctx *c, const FFTAxis &ax, const FFTAxis &ay, int nz, int bat
     }
   }
   dim3 grid((unsigned)nz, (unsigned)batch);
-  kern<<<grid, 384, smem, c->stream>>>(sign, axis_tw<C>(ax), axis_tw<C>(ay), op);
+  kern<<<grid, 384, smem, c->stream>>>(sign, axis_tw<C>(ax), axis_tw<C>(ay), op, 2 * c->nsm);
   c->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {

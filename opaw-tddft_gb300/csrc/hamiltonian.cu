@@ -527,6 +527,7 @@ template <typename R> struct OpHFinal {
   const R *dv;
   static constexpr bool kMid = false;
   __device__ C load(int b, int64_t g) const { return src[b * bstride + g]; }
+  __device__ const C *raw(int b) const { return src + b * bstride; }
   // the epilogue operands of one element, loaded ahead of the stores
   struct Pre {
     C p, t;
