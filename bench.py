@@ -36,6 +36,11 @@ GAMMA = 1e-3
 DT = 0.05
 METRIC = "RK4 orbital-steps/s (mixed precision, stage-wise rebuild)"
 UNIT = "orbital-steps/s"
+# k_mix_dense per orbital (both sets) on the 96^3 / 40-atom workload:
+# DRAM bytes of one RK4-stage launch measured by ncu at 32 orbitals
+# (read 937.6 MB + write 743.4 MB), and that launch's algorithmic bytes
+DENSE_TRAFFIC_PER_ORB = (937.597696e6 + 743.37536e6) / 32
+DENSE_ALG_STAGE_PER_ORB = 1893.5e6 / 32
 CPU_SAMPLE_NORB = 2
 
 
@@ -204,8 +209,8 @@ def fp64_compare(ctx, pkg, torch, stream, fresh, ncmp, ipol, norb, mixed_ms):
 
 
 def roofline(ctx, pkg, torch, stream, s, psi0, norb):
-    """The batched FFT axis kernel on the complex64 orbital batch, timed
-    alone with CUDA events on the library's stream."""
+    """The batched 3D FFT (xy-plane pass + z pass) on the complex64 orbital
+    batch, timed alone with CUDA events on the library's stream."""
     peak, peak_kind = load_peaks()
     batch = torch.empty((norb, s.nn), dtype=torch.complex64, device="cuda")
     batch.copy_(torch.from_numpy(psi0.astype(np.complex64)).to("cuda"))
@@ -228,9 +233,8 @@ def roofline(ctx, pkg, torch, stream, s, psi0, norb):
     alg_bytes = 2.0 * norb * s.nn * 8  # read + write the complex64 batch once per axis pass
     achieved = alg_bytes / per_launch_s / 1e9
     del batch
-    return {"kernel": f"k_fft_axis<float2> (batched 3D FFT axis pass, {norb} x 96^3 complex64)",
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_kind": peak_kind, "traffic": None, "alg_bytes_per_launch": alg_bytes,
+    return {"kernel": f"k_fft_xy + k_fft_ct (forward 3D FFT: xy-plane pass and z pass, {norb} x 96^3 complex64)",
+            "achieved": achieved, "unit": "GB/s", "frac": achieved / peak, "alg_bytes_per_launch": alg_bytes,
             "avg_launch_ms": per_launch_s * 1e3}
 
 
@@ -346,6 +350,7 @@ def main():
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    ctx.ktime_begin()  # CUDA events around every launch of the dominant kernel
     e0.record(stream)
     # one call propagates the K steps, as the driver loop would issue a block
     # of steps (the dipole of every step is still computed and returned)
@@ -353,6 +358,7 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize()
     el_ms = e0.elapsed_time(e1)
+    kt_ms, kt_n, kt_bytes = ctx.ktime_end()
     launches = ctx.launches - l0
     clk = clocks.stop()
     barrier(dist)
@@ -364,9 +370,20 @@ def main():
     fp64 = None
     if not args.skip_fp64:
         fp64 = fp64_compare(ctx, pkg, torch, stream, fresh, args.compare_steps, ipol, norb, el_max / args.steps)
-    roof = None
+    peak, peak_kind = load_peaks()
+    roof = {"kernel": "k_mix_dense (fused RK4 accumulation / S^-1/2 / density pass over the grid points "
+                      "outside the projector boxes; the largest share of the step)",
+            "bound": "hbm", "achieved": kt_bytes / (kt_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": kt_bytes / (kt_ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
+            "traffic": DENSE_TRAFFIC_PER_ORB * norb,
+            "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage launch (RK4 stage 2 "
+                            "of 4) at 32 orbitals, scaled by orbitals; that launch's algorithmic bytes are "
+                            f"{DENSE_ALG_STAGE_PER_ORB * norb:.4g} (profiles/hot_kernels_96cube_32orb.md)",
+            "alg_bytes_per_launch": kt_bytes / max(kt_n, 1), "avg_launch_ms": kt_ms / max(kt_n, 1),
+            "launches_timed": kt_n, "timing": "CUDA events on the library stream around each launch, "
+                                              "inside the timed region"}
     if not args.no_roofline:
-        roof = roofline(ctx, pkg, torch, stream, s, psi0, norb)
+        roof["fft3d_pass_pair"] = roofline(ctx, pkg, torch, stream, s, psi0, norb)
 
     e2e = None
     if not args.no_e2e:

@@ -99,6 +99,15 @@ const char *opaw_last_error(void);
 void *opaw_stream(opaw_ctx *ctx);
 /* number of this library's kernels launched since the context was made */
 int64_t opaw_kernel_launches(opaw_ctx *ctx);
+/* live timing of the mixed step's dominant kernel (the fused RK4 / S^-1/2 /
+ * density pass over the grid points outside the projector boxes): between
+ * begin and end every launch of it is bracketed by CUDA events on the
+ * context's stream, and its algorithmic bytes (each array element it must
+ * read or write, once) are added up.  end waits for the stream and returns
+ * the summed device time, the launches and the bytes.  Measurement plumbing
+ * with no counterpart in the reference. */
+int opaw_ktime_begin(opaw_ctx *ctx);
+int opaw_ktime_end(opaw_ctx *ctx, double *ms, int *launches, double *bytes);
 /* waits for all work issued on the context's stream (the *_dev entry points
  * below are asynchronous on that stream) */
 int opaw_sync(opaw_ctx *ctx);

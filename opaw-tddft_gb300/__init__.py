@@ -62,6 +62,8 @@ SIGNATURES = {
     "opaw_last_error": (ct.c_char_p, []),
     "opaw_stream": (ct.c_void_p, [_P]),
     "opaw_kernel_launches": (ct.c_int64, [_P]),
+    "opaw_ktime_begin": (ct.c_int, [_P]),
+    "opaw_ktime_end": (ct.c_int, [_P, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int), ct.POINTER(ct.c_double)]),
     "opaw_sync": (ct.c_int, [_P]),
     "opaw_psi_upload": (ct.c_int, [_P, ct.c_int, _P, ct.c_int]),
     "opaw_psi_download": (ct.c_int, [_P, ct.c_int, _P, ct.c_int]),
@@ -190,6 +192,16 @@ class Context:
 
     def sync(self):
         _check(lib().opaw_sync(self.h))
+
+    def ktime_begin(self):
+        """Start live event timing of the fused dense pass (opaw_ktime_begin)."""
+        _check(lib().opaw_ktime_begin(self.h))
+
+    def ktime_end(self):
+        """(device ms summed over launches, launches, algorithmic bytes)."""
+        ms, n, b = ct.c_double(), ct.c_int(), ct.c_double()
+        _check(lib().opaw_ktime_end(self.h, ct.byref(ms), ct.byref(n), ct.byref(b)))
+        return ms.value, n.value, b.value
 
     # ---- orbitals
     def upload(self, set_, psi):

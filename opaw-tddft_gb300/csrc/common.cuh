@@ -155,6 +155,11 @@ struct opaw_ctx {
   double dx, dy, dz, dv, ekcut, rnel, dij_max;
   int scale_vh, periodic;
   int nsm = 0;  // multiprocessors of the context's device
+  // live timing of the fused dense pass (opaw_ktime_begin / _end)
+  bool ktime_on = false;
+  std::vector<cudaEvent_t> kev;  // start/stop pairs, reused
+  int kev_used = 0;
+  double kbytes = 0.0;
   int nxb, nyb, nzb;
   int64_t nnb;
   int natom;

@@ -359,6 +359,7 @@ static void destroy(opaw_ctx *c) {
   cudaFree(c->d_ovl_off);
   for (int k = 0; k < 4; k++) cudaFree(c->d_ovl[k]);
   for (auto &b : c->mix) cudaFree(b.p);
+  for (cudaEvent_t e : c->kev) cudaEventDestroy(e);
   cudaFree(c->red.p);
   cudaFree(c->g2part.p);
   if (c->h_red) cudaFreeHost(c->h_red);
@@ -502,6 +503,30 @@ int opaw_dev_free(opaw_ctx *c) {
 
 void *opaw_stream(opaw_ctx *c) { return c ? (void *)c->stream : nullptr; }
 int64_t opaw_kernel_launches(opaw_ctx *c) { return c ? c->launches : 0; }
+
+int opaw_ktime_begin(opaw_ctx *c) {
+  OPAW_CHECK(check_ctx(c));
+  c->ktime_on = true;
+  c->kev_used = 0;
+  c->kbytes = 0.0;
+  return OPAW_OK;
+}
+
+int opaw_ktime_end(opaw_ctx *c, double *ms, int *launches, double *bytes) {
+  OPAW_CHECK(check_ctx(c));
+  c->ktime_on = false;
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  double tot = 0.0;
+  for (int i = 0; i + 1 < c->kev_used; i += 2) {
+    float t = 0.f;
+    OPAW_CUDA(cudaEventElapsedTime(&t, c->kev[i], c->kev[i + 1]));
+    tot += t;
+  }
+  if (ms) *ms = tot;
+  if (launches) *launches = c->kev_used / 2;
+  if (bytes) *bytes = c->kbytes;
+  return OPAW_OK;
+}
 
 int opaw_sync(opaw_ctx *c) {
   OPAW_CHECK(check_ctx(c));

@@ -949,8 +949,31 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
   f.stage = stage;
   f.first = first;
   f.write_t = write_t;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (c->ktime_on) {  // live timing (opaw_ktime_begin): events from a reused pool
+    while ((int)c->kev.size() < c->kev_used + 2) {
+      cudaEvent_t e;
+      OPAW_CUDA(cudaEventCreate(&e));
+      c->kev.push_back(e);
+    }
+    ev0 = c->kev[c->kev_used];
+    ev1 = c->kev[c->kev_used + 1];
+    c->kev_used += 2;
+    OPAW_CUDA(cudaEventRecord(ev0, c->stream));
+  }
   k_mix_dense<<<grid1(c->nn, 256), 256, 0, c->stream>>>(f, c->d_uidx);
   MIX_LAUNCHED();
+  if (ev1) {
+    OPAW_CUDA(cudaEventRecord(ev1, c->stream));
+    // algorithmic bytes: the union index of every point; per point outside
+    // the boxes and orbital of both sets the arrays this mode reads or
+    // writes once (complex64), and the two FP64 densities
+    const double nd = (double)(c->nn - c->nunion);
+    double per = 0.0;  // bytes per (point, orbital), both sets
+    if (stage) per += 16.0 + (first ? 0.0 : 16.0) + 16.0;  // u', ks read, ks write
+    if (write_t) per += 32.0;                              // pf read, t write
+    c->kbytes += 4.0 * (double)c->nn + nd * (per * m.norb + (write_t ? 16.0 : 0.0));
+  }
   if (c->nunion > 0) {
     const float *P0 = c->d_p3d_f, *P1 = c->d_p3d1_f;
     const int ngroups = (m.norb + kBoxOrb - 1) / kBoxOrb;
