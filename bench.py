@@ -208,6 +208,56 @@ def fp64_compare(ctx, pkg, torch, stream, fresh, ncmp, ipol, norb, mixed_ms):
             "d_dip_mixed_first_last": [float(dm[0]), float(dm[-1])]}
 
 
+def h_apply_microbench(pkg, torch, s, psi0, norb):
+    """The Hamiltonian-apply microbenchmark of the 96^3 workload: H of the
+    128-orbital batch (hphi.f90 semantics, set 0, v_ks0 and D_init) in
+    complex128 and complex64 through opaw_h_apply_dev, timed with CUDA events
+    on the library's stream; GB/s against the compulsory bytes (read psi,
+    write H psi) and against the bytes of the passes this implementation makes;
+    error of the complex64 result against the complex128 one (which the
+    parity tests hold to the FP64 oracle at 1e-12)."""
+    peak, _ = load_peaks()
+    hc = pkg.Context(s)
+    hc.set_vks(0, s.vks0)
+    hc.set_dij(0, s.dij_init)
+    st = torch.cuda.ExternalStream(hc.stream)
+    out = {}
+    res = {}
+    nn = s.nn
+    nbox_tot = int(np.sum(np.prod(np.asarray(s.nrough).reshape(-1, 3), axis=1)))
+    for name, dt, tdt, E in (("fp64", pkg.OPAW_C128, torch.complex128, 16), ("fp32", pkg.OPAW_C64, torch.complex64, 8)):
+        x = torch.from_numpy(psi0.astype(np.complex128 if E == 16 else np.complex64)).to("cuda")
+        y = torch.empty_like(x)
+        torch.cuda.synchronize()
+        hc.h_apply_dev(0, dt, x.data_ptr(), y.data_ptr(), norb)
+        hc.sync()
+        reps = 3
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(st)
+        for _ in range(reps):
+            hc.h_apply_dev(0, dt, x.data_ptr(), y.data_ptr(), norb)
+        a1.record(st)
+        torch.cuda.synchronize()
+        t = a0.elapsed_time(a1) / reps / 1e3
+        comp = 2.0 * norb * nn * E
+        # passes: xy + z + xy(+ v_ks psi) FFT passes (read psi once more in the
+        # last), the box gather and the union scatter (read + write)
+        passes = norb * nn * E * (2 + 2 + 3) + norb * nbox_tot * E * 3
+        out[name] = {"ms": t * 1e3, "gbs_compulsory": comp / t / 1e9, "gbs_passes": passes / t / 1e9,
+                     "frac_passes_of_peak": passes / t / 1e9 / peak}
+        res[name] = y.to(torch.complex128)
+        del x, y
+    d = (res["fp32"] - res["fp64"]).abs()
+    ref = res["fp64"].abs()
+    out["fp32_vs_fp64_max_rel"] = float(d.max() / ref.max())
+    out["fp32_vs_fp64_rel_l2"] = float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(ref))
+    out["orbitals"] = norb
+    del res, d, ref
+    hc.close()
+    return out
+
+
 def roofline(ctx, pkg, torch, stream, s, psi0, norb):
     """The batched 3D FFT (xy-plane pass + z pass) on the complex64 orbital
     batch, timed alone with CUDA events on the library's stream."""
@@ -382,8 +432,10 @@ def main():
             "alg_bytes_per_launch": kt_bytes / max(kt_n, 1), "avg_launch_ms": kt_ms / max(kt_n, 1),
             "launches_timed": kt_n, "timing": "CUDA events on the library stream around each launch, "
                                               "inside the timed region"}
+    hbench = None
     if not args.no_roofline:
         roof["fft3d_pass_pair"] = roofline(ctx, pkg, torch, stream, s, psi0, norb)
+        hbench = h_apply_microbench(pkg, torch, s, psi0, norb)
 
     e2e = None
     if not args.no_e2e:
@@ -418,7 +470,7 @@ def main():
             "data": "synthetic (seeded)", "config": dict(workload_config(norb), **state),
             "parallelism": "replicas" if world > 1 else "single GPU",
             "fp64": fp64,
-            "roofline": roof,
+            "roofline": roof, "h_apply": hbench,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": launches,
