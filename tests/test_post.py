@@ -89,3 +89,45 @@ def test_first_peak_of_two_lines():
     w = np.linspace(0.02, 1.0, 1500)
     S = spectrum.strength_function(d, dt, w, tau=150.0, window="gauss")
     assert abs(spectrum.first_peak(w, S) - 0.2) < 3e-3
+
+
+def test_restart_roundtrip_and_layout(tmp_path):
+    """tddft_save/ as tddft_write_to_restart.f90 writes it: info = nb nodes it,
+    one complex*16 record per orbital, rank 0's orbitals first."""
+    from opaw_tddft_gb300 import restart
+
+    rng = np.random.default_rng(9)
+    psi = _orbitals(rng, ns=4)
+    pp = _orbitals(rng, ns=4)
+    d = tmp_path / "tddft_save"
+    restart.write_restart(d, psi, pp, it=37, nodes=2)
+    assert (d / "info").read_text().split() == ["2", "2", "37"]
+    b = (d / "phi_bar.bin").read_bytes()
+    nn = psi[0].size
+    assert struct.unpack_from("<i", b, 0)[0] == 16 * nn and len(b) == 4 * (16 * nn + 8)
+    assert np.array_equal(np.frombuffer(b[4:4 + 16 * nn], "<c16"), psi[0].reshape(-1))
+    a, c, it = restart.read_restart(d, nn)
+    assert it == 37 and np.array_equal(a, psi.reshape(4, -1)) and np.array_equal(c, pp.reshape(4, -1))
+    with pytest.raises(ValueError):
+        restart.read_restart(d, nn + 1)
+
+
+@pytest.mark.gpu
+def test_restart_through_context(tmp_path):
+    """Resident orbitals of both sets -> tddft_save/ -> a fresh context."""
+    import opaw_tddft_gb300 as pkg
+    from opaw_tddft_gb300 import restart, synthetic
+
+    s = synthetic.small_system("tiny", norb=3)
+    psi = synthetic.orbitals(s, 3, seed=5).reshape(3, -1)
+    c = pkg.Context(s)
+    c.upload(0, psi)
+    c.excite(1, 1e-3)
+    restart.save(c, tmp_path / "tddft_save", it=12, norb=3)
+    pp = c.download(1, 3).reshape(3, -1)
+    c.close()
+    c2 = pkg.Context(s)
+    assert restart.load(c2, tmp_path / "tddft_save") == 12
+    assert np.array_equal(c2.download(0, 3).reshape(3, -1), psi)
+    assert np.array_equal(c2.download(1, 3).reshape(3, -1), pp)
+    c2.close()
