@@ -598,11 +598,8 @@ template <typename R>
 int h_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>::C *hp, int norb) {
   typedef typename Tr<R>::C C;
   if (norb <= 0) return OPAW_OK;
-  const size_t bytes = sizeof(C) * (size_t)c->nn * norb;
-  OPAW_CHECK(ensure(c->work[0], bytes));
   OPAW_CHECK(ensure(c->coef[0], sizeof(double2) * (size_t)c->ns * norb + 16));
   OPAW_CHECK(ensure(c->coef[1], sizeof(double2) * (size_t)c->ns * norb + 16));
-  C *w = (C *)c->work[0].p;
   double2 *c0 = (double2 *)c->coef[0].p, *c1 = (double2 *)c->coef[1].p;
   // <p~|psi> and D c (addvnl, hphi.f90:40-47), from the unmodified input
   OPAW_CHECK(gather<R>(c, 0, pin, norb, c0));
@@ -614,15 +611,7 @@ int h_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>::
     OPAW_CUDA(cudaGetLastError());
   }
   // kinetic term through the 3D FFT (hphi.f90:14-18) and v_ks psi (:21)
-  Dims3 d{c->nx, c->ny, c->nz};
-  OpCopy<C> x_in{pin, w, c->nn};
-  OpCopy<C> inplace{w, w, c->nn};
-  OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, -1, x_in)));
-  OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, -1, inplace)));
-  OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, make_kin<R>(c, w))));
-  OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, +1, inplace)));
-  OpHFinal<R> fin{w, pin, VksOf<R>::get(c, set), hp, c->nn, nullptr, nullptr};
-  OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, +1, fin)));
+  OPAW_CHECK(h_fft<R>(c, VksOf<R>::get(c, set), pin, hp, norb, nullptr, nullptr));
   // nonlocal term (hphi.f90:42-60)
   OPAW_CHECK(union_scatter<R>(c, 0, hp, norb, c1));
   return OPAW_OK;

@@ -53,18 +53,22 @@ __global__ void k_mix_drhoij(const double2 *__restrict__ c0, const double2 *__re
                              const int *__restrict__ dslot, const int64_t *__restrict__ soff,
                              const int64_t *__restrict__ doff, const int *__restrict__ ms,
                              const double *__restrict__ rho0, double *__restrict__ drho, double *__restrict__ rho1) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);  // warp per entry
+  const int lane = threadIdx.x & 31;
   if (t >= nd) return;
   const int a = dslot[t];
   const int m = ms[a];
   const int loc = t - (int)doff[a];
   const int i = loc % m, j = loc / m;
   double acc = 0;
-  for (int o = 0; o < norb; o++) {
+  for (int o = lane; o < norb; o += 32) {
     const double2 ai = c0[(int64_t)o * ns + soff[a] + i], aj = c0[(int64_t)o * ns + soff[a] + j];
     const double2 bi = cd[(int64_t)o * ns + soff[a] + i], bj = cd[(int64_t)o * ns + soff[a] + j];
     acc += 2.0 * (ai.x * bj.x + ai.y * bj.y + bi.x * aj.x + bi.y * aj.y + bi.x * bj.x + bi.y * bj.y);
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);  // fixed order
+  if (lane != 0) return;
   drho[t] = acc;
   rho1[t] = rho0[t] + acc;
 }
@@ -1060,7 +1064,7 @@ static int mix_potentials(opaw_ctx *c, Mix &m) {
   OPAW_CHECK(rhoij_of(c, m.c0, norb, c->d_rhoij[0]));
   OPAW_CHECK(nhat_raw_of(c, c->d_rhoij[0], m.h0raw));
   if (c->nd > 0) {
-    k_mix_drhoij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(m.c0, m.cd, norb, c->ns, c->nd, c->d_dslot_atom,
+    k_mix_drhoij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(m.c0, m.cd, norb, c->ns, c->nd, c->d_dslot_atom,
                                                            c->d_soff, c->d_doff, c->d_ms, c->d_rhoij[0], m.drhoij,
                                                            c->d_rhoij[1]);
     MIX_LAUNCHED();

@@ -330,21 +330,31 @@ __global__ void k_density(const C *__restrict__ psi, int norb, int64_t nn, doubl
 }
 
 // ------------------------------------------------- rho_ij (A8) --
+// one warp per entry (atom, i, j); lanes stride over the orbitals, a
+// butterfly reduction in fixed order adds them (bit-reproducible)
+__device__ __forceinline__ double warp_allsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 __global__ void k_rhoij(const double2 *__restrict__ coef, int norb, int ns, int nd, const int *__restrict__ dslot,
                         const int64_t *__restrict__ soff, const int64_t *__restrict__ doff,
                         const int *__restrict__ ms, double *__restrict__ rho) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nd) return;
+  const int t = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (t >= nd) return;  // whole warps
   const int a = dslot[t];
   const int m = ms[a];
   const int loc = t - (int)doff[a];
   const int i = loc % m, j = loc / m;
   double acc = 0;
-  for (int o = 0; o < norb; o++) {
+  for (int o = lane; o < norb; o += 32) {
     const double2 ci = coef[(int64_t)o * ns + soff[a] + i], cj = coef[(int64_t)o * ns + soff[a] + j];
     acc += 2.0 * (ci.x * cj.x + ci.y * cj.y);  // Re(conj(c_i) c_j) * 2, tddft_rhoij.f90:35
   }
-  rho[t] = acc;
+  acc = warp_allsum(acc);
+  if (lane == 0) rho[t] = acc;
 }
 
 // ---------------------------------------------------- nhat (A11) --
@@ -352,20 +362,21 @@ __global__ void k_rhoij(const double2 *__restrict__ coef, int norb, int ns, int 
 __global__ void k_nhat_w(const double *__restrict__ rho, const double *__restrict__ q, const int *__restrict__ ms,
                          const int *__restrict__ nlm, const int64_t *__restrict__ doff,
                          const int64_t *__restrict__ qoff, int natom, int nlmmax, double *__restrict__ w) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);  // warp per (atom, lm)
+  const int lane = threadIdx.x & 31;
   if (t >= natom * nlmmax) return;
   const int a = t / nlmmax, l = t % nlmmax;
   const int L = nlm[a], m = ms[a];
   if (l >= L) {
-    w[t] = 0;
+    if (lane == 0) w[t] = 0;
     return;
   }
   const double *R = rho + doff[a];
   const double *Q = q + qoff[a];
   double acc = 0;
-  for (int j = 0; j < m; j++)
-    for (int i = 0; i < m; i++) acc += R[i + m * j] * Q[l + L * (i + m * j)];
-  w[t] = acc;
+  for (int e = lane; e < m * m; e += 32) acc += R[e] * Q[l + (int64_t)L * e];  // e = i + m j
+  acc = warp_allsum(acc);
+  if (lane == 0) w[t] = acc;
 }
 
 __global__ void k_nhat(const int *__restrict__ cpt, const int *__restrict__ cstart, const int *__restrict__ catom,
@@ -444,7 +455,8 @@ __global__ void k_dij(const double *__restrict__ prod, int nlmmax, const double 
                       const int *__restrict__ ms, const int *__restrict__ nlm, const int64_t *__restrict__ doff,
                       const int64_t *__restrict__ qoff, const int64_t *__restrict__ eoff,
                       const int *__restrict__ dslot, int nd, double dmax, double *__restrict__ dij) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);  // warp per entry
+  const int lane = threadIdx.x & 31;
   if (t >= nd) return;
   const int a = dslot[t];
   const int m = ms[a], L = nlm[a];
@@ -454,10 +466,13 @@ __global__ void k_dij(const double *__restrict__ prod, int nlmmax, const double 
   const double *R = rho + doff[a];
   const double *Ea = E + eoff[a];
   const double *Q = q + qoff[a];
-  double d = d0[doff[a] + i + m * j];
-  for (int l2 = 0; l2 < m; l2++)
-    for (int k = 0; k < m; k++) d += Ea[i + m * (j + m * (k + m * l2))] * R[k + m * l2];
-  for (int l = 0; l < L; l++) d += prod[a * nlmmax + l] * Q[l + L * (i + m * j)];
+  double d = 0;
+  for (int e = lane; e < m * m; e += 32)  // e = k + m l2: sum_kl E[i,j,k,l] rho_kl
+    d += Ea[i + m * (j + (int64_t)m * e)] * R[e];
+  for (int l = lane; l < L; l += 32) d += prod[a * nlmmax + l] * Q[l + L * (i + m * j)];
+  d = warp_allsum(d);
+  if (lane != 0) return;
+  d += d0[doff[a] + i + m * j];
   if (dmax > 0 && fabs(d) > dmax) d = d / fabs(d) * dmax;  // get_dij.f90:144
   dij[doff[a] + i + m * j] = d;
   dij[doff[a] + j + m * i] = d;
@@ -466,7 +481,7 @@ __global__ void k_dij(const double *__restrict__ prod, int nlmmax, const double 
 // ------------------------------------------------------ the chain --
 static int rhoij_from_coef(opaw_ctx *c, int set, const double2 *coef, int norb) {
   if (c->nd == 0) return OPAW_OK;
-  k_rhoij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(coef, norb, c->ns, c->nd, c->d_dslot_atom, c->d_soff, c->d_doff,
+  k_rhoij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(coef, norb, c->ns, c->nd, c->d_dslot_atom, c->d_soff, c->d_doff,
                                                     c->d_ms, c->d_rhoij[set]);
   c->launches++;
   OPAW_CUDA(cudaGetLastError());
@@ -490,7 +505,7 @@ int nhat_step(opaw_ctx *c, int set) {
   OPAW_CUDA(cudaMemsetAsync(c->d_nhat[set], 0, sizeof(double) * c->nn, c->stream));
   if (c->natom > 0 && c->nlmmax > 0) {
     const int nt = c->natom * c->nlmmax;
-    k_nhat_w<<<grid1(nt, 128), 128, 0, c->stream>>>(c->d_rhoij[set], c->d_qijlm, c->d_ms, c->d_nlm, c->d_doff,
+    k_nhat_w<<<grid1((int64_t)nt * 32, 256), 256, 0, c->stream>>>(c->d_rhoij[set], c->d_qijlm, c->d_ms, c->d_nlm, c->d_doff,
                                                      c->d_qoff, c->natom, c->nlmmax, w);
     c->launches++;
     if (c->ncunion > 0) {
@@ -547,7 +562,7 @@ int dij_step(opaw_ctx *c, int set) {
   const int L = c->nlmmax > 0 ? c->nlmmax : 1;
   k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(c->d_vks[set], c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off,
                                                 c->d_g3d, L, c->dv, prod);
-  k_dij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(prod, L, c->d_rhoij[set], c->d_qijlm, c->d_dij0, c->d_eijkl,
+  k_dij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(prod, L, c->d_rhoij[set], c->d_qijlm, c->d_dij0, c->d_eijkl,
                                                   c->d_ms, c->d_nlm, c->d_doff, c->d_qoff, c->d_eoff,
                                                   c->d_dslot_atom, c->nd, c->dij_max, c->d_dij[set]);
   c->launches += 2;
@@ -558,7 +573,7 @@ int dij_step(opaw_ctx *c, int set) {
 // ---- pointer-based pieces (used by the perturbation-difference propagation)
 int rhoij_of(opaw_ctx *c, const double2 *coef, int norb, double *out) {
   if (c->nd == 0) return OPAW_OK;
-  k_rhoij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(coef, norb, c->ns, c->nd, c->d_dslot_atom, c->d_soff, c->d_doff,
+  k_rhoij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(coef, norb, c->ns, c->nd, c->d_dslot_atom, c->d_soff, c->d_doff,
                                                     c->d_ms, out);
   c->launches++;
   OPAW_CUDA(cudaGetLastError());
@@ -581,7 +596,7 @@ int nhat_raw_of(opaw_ctx *c, const double *rhoij, double *out) {
   OPAW_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * c->nn, c->stream));
   if (c->natom > 0 && c->nlmmax > 0) {
     const int nt = c->natom * c->nlmmax;
-    k_nhat_w<<<grid1(nt, 128), 128, 0, c->stream>>>(rhoij, c->d_qijlm, c->d_ms, c->d_nlm, c->d_doff, c->d_qoff,
+    k_nhat_w<<<grid1((int64_t)nt * 32, 256), 256, 0, c->stream>>>(rhoij, c->d_qijlm, c->d_ms, c->d_nlm, c->d_doff, c->d_qoff,
                                                      c->natom, c->nlmmax, w);
     c->launches++;
     if (c->ncunion > 0) {
@@ -617,7 +632,7 @@ int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, double *out) {
   const int L = c->nlmmax > 0 ? c->nlmmax : 1;
   k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(vks, c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off, c->d_g3d, L,
                                                 c->dv, prod);
-  k_dij<<<grid1(c->nd, 128), 128, 0, c->stream>>>(prod, L, rhoij, c->d_qijlm, c->d_dij0, c->d_eijkl, c->d_ms, c->d_nlm,
+  k_dij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(prod, L, rhoij, c->d_qijlm, c->d_dij0, c->d_eijkl, c->d_ms, c->d_nlm,
                                                   c->d_doff, c->d_qoff, c->d_eoff, c->d_dslot_atom, c->nd, c->dij_max,
                                                   out);
   c->launches += 2;

@@ -14,7 +14,9 @@ operators of the library:
   S^-1/2 H0 S^-1/2 with H0 = T + v_ks0 + sum p~ D0 <p~|;
 * `stationary_system` — rebuilds rho, n^, v_ks and D_ij from those orbitals
   and shifts v_loc and D0 so that the rebuilt Hamiltonian is exactly H0: the
-  orbitals are then an exact stationary state of the TDDFT Hamiltonian.
+  orbitals are then an exact stationary state of the TDDFT Hamiltonian;
+* `scf` — the self-consistent ground state of the system as it is (the
+  reference's SCF loop, main.f90:67-96): rebuild, DIIS mixing, filtering.
 
 Device memory is handled with torch tensors (plumbing); every operator runs
 in libopaw_gb300.so.
@@ -220,3 +222,64 @@ def stationary_system(system, psi):
         ctx.close()
         s1 = dataclasses.replace(s1, vloc=s1.vloc + (target_v - vks), dij0=s1.dij0 + (target_d - dij))
     return s1
+
+
+def scf(ctx, psi0, max_iter=60, tol_v=1e-7, tol_res=1e-5, beta=0.3, ndiis=6, filter_iter=2, verbose=False):
+    """Self-consistent ground state on the device, the loop of main.f90:67-96:
+    each iteration rebuilds v_ks and D_ij from the current orbitals
+    (ncpaw_make_hamiltonian: rho_ij, density, n^, Hartree, LDA, D_ij, all
+    FP64 on the device), mixes the joint vector [v_ks, D_ij] with Pulay/DIIS
+    extrapolation of the residuals (diis.f90: residual = rebuilt - input,
+    a history of ndiis pairs, linear mixing beta), and runs `filter_iter`
+    warm-started Chebyshev filter passes with orthogonalisation and
+    Rayleigh-Ritz (chebyr_m.f90, orthog_phi.f90, diag.f90) in that potential.
+    Stops when the largest change of v_ks is below tol_v and the largest
+    eigen-residual below tol_res.  The orbitals live in set 0 of ctx; the
+    input potentials of the first iteration are the ones ctx holds.  Returns
+    (eigenvalues, orbitals complex128 [norb, nn], history of
+    (max |dv_ks|, max residual))."""
+    psi = np.ascontiguousarray(psi0, dtype=np.complex128)
+    norb = psi.shape[0]
+    nn = ctx.nn
+    x_in = np.concatenate([ctx.get_vks(0), ctx.get_dij(0)])
+    xs, rs = [], []
+    hist = []
+    w = res = None
+    for it in range(max_iter):
+        ctx.upload(0, psi)
+        ctx.rebuild(0, pkg.PREC_FP64)
+        x_out = np.concatenate([ctx.get_vks(0), ctx.get_dij(0)])
+        r = x_out - x_in
+        dv = float(np.abs(r[:nn]).max())
+        if res is not None:
+            hist.append((dv, float(res.max())))
+            if verbose:
+                print(f"scf iteration {it}: max |dv_ks| {dv:.3e}, max eigen-residual {res.max():.3e}")
+            if dv < tol_v and res.max() < tol_res:
+                break
+        xs.append(x_in)
+        rs.append(r)
+        xs, rs = xs[-ndiis:], rs[-ndiis:]
+        m = len(rs)
+        if m == 1:
+            x_next = x_in + beta * r
+        else:
+            B = np.empty((m + 1, m + 1))
+            for i in range(m):
+                for j in range(m):
+                    B[i, j] = float(np.dot(rs[i], rs[j]))
+            B[:m, m] = B[m, :m] = 1.0
+            B[m, m] = 0.0
+            rhs = np.zeros(m + 1)
+            rhs[m] = 1.0
+            cvec = np.linalg.lstsq(B, rhs, rcond=None)[0][:m]
+            x_next = sum(c * (xv + beta * rv) for c, xv, rv in zip(cvec, xs, rs))
+        ctx.set_vks(0, x_next[:nn])
+        ctx.set_dij(0, x_next[nn:])
+        x_in = x_next
+        w, psi, res = lowest_states(ctx, psi, n_iter=filter_iter, tol=0.0, fp64_polish=1,
+                                    seed=it, verbose=False)
+    else:
+        raise RuntimeError(f"SCF did not converge in {max_iter} iterations: last (max |dv|, residual) "
+                           f"{hist[-1] if hist else None}")
+    return w, psi, hist

@@ -99,3 +99,27 @@ def test_mixed_dipole_on_stationary_state():
     err = np.abs(out[pkg.PREC_MIXED] - out[pkg.PREC_FP64]).max() / np.abs(out[pkg.PREC_FP64]).max()
     assert err < 1e-6, err
     c.close()
+
+
+def test_scf_self_consistent():
+    """The device SCF (main.f90:67-96 loop: rebuild, DIIS mixing, Chebyshev
+    filtering) reaches a self-consistent state of the system as it is: the
+    Hamiltonian rebuilt from the final orbitals is the one they diagonalise,
+    and the density no longer moves under an unkicked propagation."""
+    s = synthetic.small_system("tiny", norb=4)
+    c = pkg.Context(s)
+    c.set_vks(0, s.vks0)
+    c.set_dij(0, s.dij_init)
+    w, psi, hist = groundstate.scf(c, synthetic.orbitals(s, 4, seed=3).reshape(4, -1), max_iter=80,
+                                   tol_v=1e-7, tol_res=1e-5)
+    v_in, d_in = c.get_vks(0), c.get_dij(0)
+    c.upload(0, psi)
+    c.rebuild(0, pkg.PREC_FP64)
+    assert np.abs(c.get_vks(0) - v_in).max() < 1e-6
+    assert np.all(np.diff(w) >= -1e-12)
+    rho0 = c.get_density(0)
+    c.excite(1, 0.0)
+    c.tddft_steps(5, 0.05, 1e-3, pkg.PREC_FP64)
+    c.rebuild(0, pkg.PREC_FP64)
+    assert rel(c.get_density(0), rho0) < 1e-4
+    c.close()
