@@ -452,7 +452,18 @@ def main():
         for _ in range(nh):
             ctx.tddft_steps_host(a, b, 1, DT, GAMMA, pkg.PREC_MIXED)
         el = max_over_ranks(dist, time.perf_counter() - t)
+        # the copy rates inside that call: one set up and one set down
+        nbytes = norb * s.nn * 16
+        t = time.perf_counter()
+        lib = pkg.lib()
+        import ctypes as _ct
+        pkg._check(lib.opaw_psi_upload(ctx.h, 0, a.ctypes.data_as(_ct.c_void_p), norb))
+        t_up = time.perf_counter() - t
+        t = time.perf_counter()
+        pkg._check(lib.opaw_psi_download(ctx.h, 0, a.ctypes.data_as(_ct.c_void_p), norb))
+        t_dn = time.perf_counter() - t
         e2e = {"value": sum_over_ranks(dist, 2.0 * norb * nh) / el, "unit": UNIT,
+               "h2d_gbs": nbytes / t_up / 1e9, "d2h_gbs": nbytes / t_dn / 1e9,
                "h2d_bytes_per_step": int(2 * norb * s.nn * 16),
                "d2h_bytes_per_step": int(2 * norb * s.nn * 16 + 3 * 8),
                "api": "opaw_tddft_steps_host (psi, psi_pert host arrays in/out each step)", "steps": nh}

@@ -444,20 +444,26 @@ __device__ __forceinline__ void fused_one(const FusedArgs &f, int64_t idx, float
   acc.add(tv0, tvd);
 }
 
-__global__ void __launch_bounds__(256) k_mix_dense(FusedArgs f, const int *__restrict__ uidx) {
+// every grid point; at the union points the box terms come from BG
+// ([kind B, G][set][orbital][union point], k_mix_boxcoef)
+__global__ void __launch_bounds__(256)
+    k_mix_dense(FusedArgs f, const int *__restrict__ uidx, const float2 *__restrict__ BG, int nunion) {
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (g >= f.nn || uidx[g] >= 0) return;
+  if (g >= f.nn) return;
+  const int u = uidx[g];
+  const int64_t su = (int64_t)f.norb * nunion;  // between the four (kind, set) blocks of BG
   const float2 zero = make_float2(0.f, 0.f);
-  const float2 B[2] = {zero, zero};
   DensAcc acc;
   for (int o = 0; o < f.norb; o += 2) {
     const int nj = (o + 1 < f.norb) ? 2 : 1;
-    float2 a0[2], ad[2], q0[2], qd[2], s0[2], sd[2];
+    float2 a0[2], ad[2], q0[2], qd[2], s0[2], sd[2], B[2][2], G[2][2];
 #pragma unroll
     for (int j = 0; j < 2; j++) {
       a0[j] = ad[j] = q0[j] = qd[j] = s0[j] = sd[j] = zero;
+      B[j][0] = B[j][1] = G[j][0] = G[j][1] = zero;
       if (j < nj) {
         const int64_t idx = (int64_t)(o + j) * f.nn + g;
+        const int64_t bi = (int64_t)(o + j) * nunion + u;
         if (f.stage) {
           a0[j] = f.u0[idx];
           ad[j] = f.ud[idx];
@@ -465,10 +471,18 @@ __global__ void __launch_bounds__(256) k_mix_dense(FusedArgs f, const int *__res
             s0[j] = f.ks0[idx];
             sd[j] = f.ksd[idx];
           }
+          if (u >= 0) {
+            B[j][0] = BG[bi];
+            B[j][1] = BG[su + bi];
+          }
         }
         if (f.write_t) {
           q0[j] = f.pf0[idx];
           qd[j] = f.pfd[idx];
+          if (u >= 0) {
+            G[j][0] = BG[2 * su + bi];
+            G[j][1] = BG[3 * su + bi];
+          }
         }
       }
     }
@@ -477,130 +491,61 @@ __global__ void __launch_bounds__(256) k_mix_dense(FusedArgs f, const int *__res
       if (j < nj && f.write_t) restore_pf(f, o + j, q0[j], qd[j], q0[j], qd[j]);
 #pragma unroll
     for (int j = 0; j < 2; j++)
-      if (j < nj) fused_one(f, (int64_t)(o + j) * f.nn + g, a0[j], ad[j], q0[j], qd[j], s0[j], sd[j], B, B, acc);
+      if (j < nj)
+        fused_one(f, (int64_t)(o + j) * f.nn + g, a0[j], ad[j], q0[j], qd[j], s0[j], sd[j], B[j], G[j], acc);
   }
   if (f.write_t) acc.store(f, g);
 }
 
-// union points: thread = (point, group of kBoxOrb orbitals); the group's
-// density sums (the same 16-orbital FP32 sums as above, kBoxOrb = 16) go to
-// bpart[group][u] and k_mix_box_dens adds them in group order in FP64
-constexpr int kBoxOrb = 16;
-
-template <int EMAX, int MSMAX>
+// The box terms of the fused pass at every union point u, orbital o and
+// set X (thread per (u, o)):
+//   B = sum_entries sum_i  P~_i (-i cD_i) + P~1_i (-i c2_i)      (of -i S^-1/2 H t)
+//   G = sum_entries sum_i  P~1_i c3_i                           (of S^-1/2 y)
+// entries in atom order; projector values from the FP32 tables,
+// coefficients packed by k_mc_k / k_mc_t.
 __global__ void __launch_bounds__(128)
-    k_mix_box(FusedArgs f, int nunion, const int *__restrict__ upt, const int *__restrict__ ustart,
-              const int *__restrict__ uatom, const int *__restrict__ ubox, const float *__restrict__ P0,
-              const float *__restrict__ P1, const int64_t *__restrict__ poff, const int *__restrict__ nrough,
-              const int *__restrict__ ms, const int64_t *__restrict__ soff, const float4 *__restrict__ cab,
-              const float2 *__restrict__ cg, int ns, double *__restrict__ bpart) {
+    k_mix_boxcoef(int nunion, int norb, int ns, const int *__restrict__ ustart, const int *__restrict__ uatom,
+                  const int *__restrict__ ubox, const float *__restrict__ P0, const float *__restrict__ P1,
+                  const int64_t *__restrict__ poff, const int *__restrict__ nrough, const int *__restrict__ ms,
+                  const int64_t *__restrict__ soff, const float4 *__restrict__ cab, const float2 *__restrict__ cg,
+                  int stage, int write_t, float2 *__restrict__ BG) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= nunion) return;
-  const int gy = blockIdx.y;
-  const int oa = gy * kBoxOrb, ob = min(f.norb, oa + kBoxOrb);
-  const int64_t g = upt[u];
-  const int e0 = ustart[u], ne = ustart[u + 1] - e0;
-  const bool fast = ne <= EMAX;
-  float pa[EMAX][MSMAX], pb[EMAX][MSMAX];
-  int so[EMAX], mm[EMAX];
+  const int o = blockIdx.y;
+  const int64_t kstride = (int64_t)norb * ns;
+  float2 B[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  float2 G[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  for (int e = ustart[u]; e < ustart[u + 1]; e++) {
+    const int a = uatom[e], b = ubox[e];
+    const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
+    const int m = ms[a];
+    const int64_t s0 = (int64_t)o * ns + soff[a];
+    for (int i = 0; i < m; i++) {
+      const float p = P0[poff[a] + (int64_t)i * nbox + b], q = P1[poff[a] + (int64_t)i * nbox + b];
 #pragma unroll
-  for (int e = 0; e < EMAX; e++) {
-    mm[e] = 0;
-    so[e] = 0;
-    if (fast && e < ne) {
-      const int a = uatom[e0 + e], b = ubox[e0 + e];
-      const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
-      mm[e] = ms[a];
-      so[e] = (int)soff[a];
-#pragma unroll
-      for (int i = 0; i < MSMAX; i++) {
-        pa[e][i] = (i < mm[e]) ? P0[poff[a] + (int64_t)i * nbox + b] : 0.f;
-        pb[e][i] = (i < mm[e]) ? P1[poff[a] + (int64_t)i * nbox + b] : 0.f;
-      }
-    }
-  }
-  const int64_t kstride = (int64_t)f.norb * ns;  // between the two sets
-  const float2 zero = make_float2(0.f, 0.f);
-  DensAcc acc;
-  for (int o = oa; o < ob; o++) {
-    const int64_t idx = (int64_t)o * f.nn + g;
-    // the grid values first: their loads overlap the coefficient sums below
-    float2 a0 = zero, ad = zero, q0 = zero, qd = zero, s0 = zero, sd = zero;
-    if (f.stage) {
-      a0 = f.u0[idx];
-      ad = f.ud[idx];
-      if (!f.first) {
-        s0 = f.ks0[idx];
-        sd = f.ksd[idx];
-      }
-    }
-    if (f.write_t) restore_pf(f, o, f.pf0[idx], f.pfd[idx], q0, qd);
-    float2 B[2] = {zero, zero}, Gt[2] = {zero, zero};
-#pragma unroll
-    for (int X = 0; X < 2; X++) {
-      const float4 *ab = cab + X * kstride + (int64_t)o * ns;
-      const float2 *gg = cg + X * kstride + (int64_t)o * ns;
-      if (fast) {
-#pragma unroll
-        for (int e = 0; e < EMAX; e++) {
-#pragma unroll
-          for (int i = 0; i < MSMAX; i++) {
-            if (i < mm[e]) {
-              const int sl = so[e] + i;
-              if (f.stage) {
-                const float4 q = ab[sl];
-                B[X].x += pa[e][i] * q.x + pb[e][i] * q.z;
-                B[X].y += pa[e][i] * q.y + pb[e][i] * q.w;
-              }
-              if (f.write_t) {
-                const float2 q = gg[sl];
-                Gt[X].x += pb[e][i] * q.x;
-                Gt[X].y += pb[e][i] * q.y;
-              }
-            }
-          }
+      for (int X = 0; X < 2; X++) {
+        if (stage) {
+          const float4 c = cab[X * kstride + s0 + i];
+          B[X].x += p * c.x + q * c.z;
+          B[X].y += p * c.y + q * c.w;
         }
-      } else {
-        for (int e = e0; e < e0 + ne; e++) {
-          const int a = uatom[e], b = ubox[e];
-          const int nbox = nrough[3 * a] * nrough[3 * a + 1] * nrough[3 * a + 2];
-          const int m = ms[a], s0i = (int)soff[a];
-          for (int i = 0; i < m; i++) {
-            const float p = P0[poff[a] + (int64_t)i * nbox + b], q1 = P1[poff[a] + (int64_t)i * nbox + b];
-            if (f.stage) {
-              const float4 q = ab[s0i + i];
-              B[X].x += p * q.x + q1 * q.z;
-              B[X].y += p * q.y + q1 * q.w;
-            }
-            if (f.write_t) {
-              const float2 q = gg[s0i + i];
-              Gt[X].x += q1 * q.x;
-              Gt[X].y += q1 * q.y;
-            }
-          }
+        if (write_t) {
+          const float2 c = cg[X * kstride + s0 + i];
+          G[X].x += q * c.x;
+          G[X].y += q * c.y;
         }
       }
     }
-    fused_one(f, idx, a0, ad, q0, qd, s0, sd, B, Gt, acc);
   }
-  if (f.write_t) {
-    acc.flush();  // the group's sums (already doubled)
-    bpart[(int64_t)(2 * gy) * nunion + u] = acc.total0();
-    bpart[(int64_t)(2 * gy + 1) * nunion + u] = acc.totald();
+  const int64_t su = (int64_t)norb * nunion, bi = (int64_t)o * nunion + u;
+  if (stage) {
+    BG[bi] = B[0];
+    BG[su + bi] = B[1];
   }
-}
-
-__global__ void k_mix_box_dens(const double *__restrict__ bpart, int ngroups, int nunion, const int *__restrict__ upt,
-                               double *__restrict__ r0raw, double *__restrict__ drraw) {
-  const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  if (u >= nunion) return;
-  double a0 = 0, ad = 0;
-  for (int q = 0; q < ngroups; q++) {
-    a0 += bpart[(int64_t)(2 * q) * nunion + u];
-    ad += bpart[(int64_t)(2 * q + 1) * nunion + u];
+  if (write_t) {
+    BG[2 * su + bi] = G[0];
+    BG[3 * su + bi] = G[1];
   }
-  r0raw[upt[u]] = a0;
-  drraw[upt[u]] = ad;
 }
 
 // Tail of the step.  FP64 arithmetic only where psi and delta are updated;
@@ -852,7 +797,7 @@ struct Mix {
   double2 *cnext;      // the other buffer of the pair
   double2 *G, *A;      // [set][table][orbital][slot]: gathers of u' and of pf
   double2 *cD, *q1, *c2, *c3, *pre;  // [set][orbital][slot]
-  double *bpart;       // [orbital group][2][union point]: density partials of the box pass
+  float2 *bg;          // [kind B, G][set][orbital][union point]: box terms of the fused pass
   float4 *cab;         // [set][orbital][slot]: (-i cD, -i c2) in FP32
   float2 *cg;          // [set][orbital][slot]: c3 in FP32
   double *r0raw, *h0raw, *drraw, *dhraw, *src0, *srcd, *ddens, *vh0, *dvh;
@@ -887,8 +832,8 @@ static int mix_bufs(opaw_ctx *c, int norb, Mix &m) {
   m.c2 = q + 16 * sv;
   m.c3 = q + 18 * sv;
   m.pre = q + 20 * sv;
-  OPAW_CHECK(ensure(c->mix[8], sizeof(double) * 2 * (size_t)((norb + kBoxOrb - 1) / kBoxOrb) * c->nunion + 64));
-  m.bpart = (double *)c->mix[8].p;
+  OPAW_CHECK(ensure(c->mix[8], sizeof(float2) * 4 * (size_t)norb * c->nunion + 64));
+  m.bg = (float2 *)c->mix[8].p;
   OPAW_CHECK(ensure(c->mix[14], sizeof(float4) * 2 * sv + 64));
   m.cab = (float4 *)c->mix[14].p;
   OPAW_CHECK(ensure(c->mix[15], sizeof(float2) * 2 * sv + 64));
@@ -953,6 +898,13 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
   f.stage = stage;
   f.first = first;
   f.write_t = write_t;
+  if (c->nunion > 0 && c->ns > 0) {
+    const dim3 nb(grid1(c->nunion, 128), m.norb);
+    k_mix_boxcoef<<<nb, 128, 0, c->stream>>>(c->nunion, m.norb, c->ns, c->d_ustart, c->d_uatom, c->d_ubox,
+                                             c->d_p3d_f, c->d_p3d1_f, c->d_poff, c->d_nrough, c->d_ms, c->d_soff,
+                                             m.cab, m.cg, stage, write_t, m.bg);
+    MIX_LAUNCHED();
+  }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (c->ktime_on) {  // live timing (opaw_ktime_begin): events from a reused pool
     while ((int)c->kev.size() < c->kev_used + 2) {
@@ -965,37 +917,20 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
     c->kev_used += 2;
     OPAW_CUDA(cudaEventRecord(ev0, c->stream));
   }
-  k_mix_dense<<<grid1(c->nn, 256), 256, 0, c->stream>>>(f, c->d_uidx);
+  k_mix_dense<<<grid1(c->nn, 256), 256, 0, c->stream>>>(f, c->d_uidx, m.bg, c->ns > 0 ? c->nunion : 0);
   MIX_LAUNCHED();
   if (ev1) {
     OPAW_CUDA(cudaEventRecord(ev1, c->stream));
-    // algorithmic bytes: the union index of every point; per point outside
-    // the boxes and orbital of both sets the arrays this mode reads or
-    // writes once (complex64), and the two FP64 densities
-    const double nd = (double)(c->nn - c->nunion);
-    double per = 0.0;  // bytes per (point, orbital), both sets
+    // algorithmic bytes: the union index of every point; per point and
+    // orbital of both sets the arrays this mode reads or writes once
+    // (complex64), the box terms at the union points, the two FP64 densities
+    double per = 0.0, perb = 0.0;  // bytes per (point, orbital), both sets
     if (stage) per += 16.0 + (first ? 0.0 : 16.0) + 16.0;  // u', ks read, ks write
     if (write_t) per += 32.0;                              // pf read, t write
-    c->kbytes += 4.0 * (double)c->nn + nd * (per * m.norb + (write_t ? 16.0 : 0.0));
-  }
-  if (c->nunion > 0) {
-    const float *P0 = c->d_p3d_f, *P1 = c->d_p3d1_f;
-    const int ngroups = (m.norb + kBoxOrb - 1) / kBoxOrb;
-    const dim3 nb(grid1(c->nunion, 128), ngroups);
-    if (c->msmax <= 8)
-      k_mix_box<2, 8><<<nb, 128, 0, c->stream>>>(f, c->nunion, c->d_upt, c->d_ustart, c->d_uatom, c->d_ubox, P0, P1,
-                                                 c->d_poff, c->d_nrough, c->d_ms, c->d_soff, m.cab, m.cg, c->ns,
-                                                 m.bpart);
-    else
-      k_mix_box<1, 16><<<nb, 128, 0, c->stream>>>(f, c->nunion, c->d_upt, c->d_ustart, c->d_uatom, c->d_ubox, P0, P1,
-                                                  c->d_poff, c->d_nrough, c->d_ms, c->d_soff, m.cab, m.cg, c->ns,
-                                                  m.bpart);
-    MIX_LAUNCHED();
-    if (write_t) {
-      k_mix_box_dens<<<grid1(c->nunion, 256), 256, 0, c->stream>>>(m.bpart, ngroups, c->nunion, c->d_upt, m.r0raw,
-                                                                   m.drraw);
-      MIX_LAUNCHED();
-    }
+    if (stage) perb += 16.0;
+    if (write_t) perb += 16.0;
+    c->kbytes += 4.0 * (double)c->nn + (double)c->nn * (per * m.norb + (write_t ? 16.0 : 0.0)) +
+                 (double)c->nunion * perb * m.norb;
   }
   return OPAW_OK;
 }
