@@ -36,11 +36,11 @@ GAMMA = 1e-3
 DT = 0.05
 METRIC = "RK4 orbital-steps/s (mixed precision, stage-wise rebuild)"
 UNIT = "orbital-steps/s"
-# k_mix_dense per orbital (both sets) on the 96^3 / 40-atom workload:
-# DRAM bytes of one RK4-stage launch measured by ncu at 32 orbitals
-# (read 937.6 MB + write 743.4 MB), and that launch's algorithmic bytes
-DENSE_TRAFFIC_PER_ORB = (937.597696e6 + 743.37536e6) / 32
-DENSE_ALG_STAGE_PER_ORB = 1893.5e6 / 32
+# k_mix_dense on the 96^3 / 40-atom workload with 128 orbitals per set: DRAM
+# bytes (read + write) of the five launches of one step (start, RK4 stages
+# 1-4) measured by ncu, averaged per launch, and their algorithmic bytes
+DENSE_TRAFFIC_128 = (3906464768 + 7840081664 + 9668237568 + 9672405248 + 5704129024) / 5
+DENSE_ALG_128 = (3.95e9 + 7.87e9 + 9.68e9 + 9.68e9 + 5.75e9) / 5
 CPU_SAMPLE_NORB = 2
 
 
@@ -421,14 +421,14 @@ def main():
     if not args.skip_fp64:
         fp64 = fp64_compare(ctx, pkg, torch, stream, fresh, args.compare_steps, ipol, norb, el_max / args.steps)
     peak, peak_kind = load_peaks()
-    roof = {"kernel": "k_mix_dense (fused RK4 accumulation / S^-1/2 / density pass over the grid points "
-                      "outside the projector boxes; the largest share of the step)",
+    roof = {"kernel": "k_mix_dense (fused RK4 accumulation / S^-1/2 / density pass over every grid point, "
+                      "box terms from k_mix_boxcoef; the largest share of the step)",
             "bound": "hbm", "achieved": kt_bytes / (kt_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
             "frac": kt_bytes / (kt_ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
-            "traffic": DENSE_TRAFFIC_PER_ORB * norb,
-            "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one stage launch (RK4 stage 2 "
-                            "of 4) at 32 orbitals, scaled by orbitals; that launch's algorithmic bytes are "
-                            f"{DENSE_ALG_STAGE_PER_ORB * norb:.4g} (profiles/hot_kernels_96cube_32orb.md)",
+            "traffic": DENSE_TRAFFIC_128 * norb / 128,
+            "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the five launches of one step at "
+                            "128 orbitals, per launch (algorithmic: "
+                            f"{DENSE_ALG_128 * norb / 128:.4g}; profiles/launches_tddft_step_96cube_128orb.md)",
             "alg_bytes_per_launch": kt_bytes / max(kt_n, 1), "avg_launch_ms": kt_ms / max(kt_n, 1),
             "launches_timed": kt_n, "timing": "CUDA events on the library stream around each launch, "
                                               "inside the timed region"}

@@ -27,6 +27,12 @@ struct AxisDev {
 struct Dims3 {
   int n0, n1, n2;
 };
+// a subset of the lines of an axis pass (see ct_tile_geom); full() = all
+struct LineSub {
+  int a0, na, b0, nb;
+  static LineSub full(const Dims3 &d) { return LineSub{0, d.n1, 0, d.n2}; }
+};
+
 
 template <typename C> struct CplxOf;
 template <> struct CplxOf<float2> { typedef float R; };
@@ -465,23 +471,26 @@ template <typename C, int N, int TL, int NT, int S> struct CtStages {
   }
 };
 
-// the lines of tile `tile` of an axis pass: first element, strides, count
+// the lines of tile `tile` of an axis pass: first element, strides, count.
+// sub restricts the lines: x lines with y in [a0, a0+na) and z in [b0, b0+nb);
+// y lines with z in [b0, b0+nb); z lines are always all of them.
 template <int N, int TL, int AXIS>
-__device__ __forceinline__ void ct_tile_geom(const Dims3 &d, int tile, int64_t &base, int &lstride, int &jstride,
-                                             int &nl) {
+__device__ __forceinline__ void ct_tile_geom(const Dims3 &d, const LineSub &sub, int tile, int64_t &base,
+                                             int &lstride, int &jstride, int &nl) {
   if (AXIS == 0) {
-    const int nlines = d.n1 * d.n2;
-    const int l0 = tile * TL;
-    nl = min(TL, nlines - l0);
-    base = (int64_t)l0 * N;
+    const int tpy = (sub.na + TL - 1) / TL;
+    const int zr = tile / tpy;
+    const int y0 = (tile - zr * tpy) * TL;
+    nl = min(TL, sub.na - y0);
+    base = ((int64_t)(sub.a0 + y0) + (int64_t)d.n1 * (sub.b0 + zr)) * N;
     lstride = N;
     jstride = 1;
   } else if (AXIS == 1) {
     const int tpz = (d.n0 + TL - 1) / TL;
-    const int z = tile / tpz;
-    const int x0 = (tile - z * tpz) * TL;
+    const int zr = tile / tpz;
+    const int x0 = (tile - zr * tpz) * TL;
     nl = min(TL, d.n0 - x0);
-    base = x0 + (int64_t)d.n0 * d.n1 * z;
+    base = x0 + (int64_t)d.n0 * d.n1 * (sub.b0 + zr);
     lstride = 1;
     jstride = d.n0;
   } else {
@@ -495,7 +504,7 @@ __device__ __forceinline__ void ct_tile_geom(const Dims3 &d, int tile, int64_t &
 }
 
 template <typename C, int N, int TL, int AXIS, class Op>
-__global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, int sign, const C *__restrict__ twg, Op op) {
+__global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, LineSub sub, int sign, const C *__restrict__ twg, Op op) {
   constexpr int NT = 256;
   constexpr int LS = TL + 1;
   static_assert(ct_nstage(N) > 0, "unsupported length");
@@ -508,7 +517,7 @@ __global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, int sign, const C *__re
   const int tile = blockIdx.x;
   int64_t base;
   int lstride, jstride, nl;
-  ct_tile_geom<N, TL, AXIS>(d, tile, base, lstride, jstride, nl);
+  ct_tile_geom<N, TL, AXIS>(d, sub, tile, base, lstride, jstride, nl);
   constexpr int TOT = TL * N;
   if constexpr (HasRaw<Op>::value) {
     const C *src = op.raw(b);
@@ -563,12 +572,14 @@ template <typename C, int N> constexpr int ct_tile() {
 }
 
 template <typename C, int N, int AXIS, class Op>
-int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op) {
+int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op, const LineSub *lsub) {
   constexpr int TL = ct_tile<C, N>();
+  const LineSub sub = lsub ? *lsub : LineSub::full(d);
   int64_t tiles;
-  if (AXIS == 0) tiles = ((int64_t)d.n1 * d.n2 + TL - 1) / TL;
-  else if (AXIS == 1) tiles = (int64_t)((d.n0 + TL - 1) / TL) * d.n2;
+  if (AXIS == 0) tiles = (int64_t)((sub.na + TL - 1) / TL) * sub.nb;
+  else if (AXIS == 1) tiles = (int64_t)((d.n0 + TL - 1) / TL) * sub.nb;
   else tiles = ((int64_t)d.n0 * d.n1 + TL - 1) / TL;
+  if (tiles == 0) return OPAW_OK;
   const size_t smem = sizeof(C) * ((size_t)N + 2 * (size_t)N * (TL + 1));
   auto kern = k_fft_ct<C, N, TL, AXIS, Op>;
   if (smem > 48 * 1024) {
@@ -579,7 +590,7 @@ int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const
     }
   }
   dim3 grid((unsigned)tiles, (unsigned)batch);
-  kern<<<grid, 256, smem, c->stream>>>(d, sign, axis_tw<C>(a), op);
+  kern<<<grid, 256, smem, c->stream>>>(d, sub, sign, axis_tw<C>(a), op);
   c->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -773,15 +784,18 @@ int launch_xy_if(opaw_ctx *c, const FFT3 &f, int batch, int sign, const Op &op, 
 
 // launch one axis pass over `batch` arrays of dims d
 template <typename C, int AXIS, class Op>
-int launch_axis(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op) {
+// sub: only these lines are needed (their results), the others may be left
+// unwritten; the generic kernel ignores it and transforms every line
+int launch_axis(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op,
+                const LineSub *sub = nullptr) {
   const int n = a.n;  // n == 1 runs zero stages: the fused operations still apply
   switch (n) {  // specialised lengths of the production grids and their 2x boxes
-    case 32: return launch_ct<C, 32, AXIS>(c, a, d, batch, sign, op);
-    case 48: return launch_ct<C, 48, AXIS>(c, a, d, batch, sign, op);
-    case 64: return launch_ct<C, 64, AXIS>(c, a, d, batch, sign, op);
-    case 96: return launch_ct<C, 96, AXIS>(c, a, d, batch, sign, op);
-    case 128: return launch_ct<C, 128, AXIS>(c, a, d, batch, sign, op);
-    case 192: return launch_ct<C, 192, AXIS>(c, a, d, batch, sign, op);
+    case 32: return launch_ct<C, 32, AXIS>(c, a, d, batch, sign, op, sub);
+    case 48: return launch_ct<C, 48, AXIS>(c, a, d, batch, sign, op, sub);
+    case 64: return launch_ct<C, 64, AXIS>(c, a, d, batch, sign, op, sub);
+    case 96: return launch_ct<C, 96, AXIS>(c, a, d, batch, sign, op, sub);
+    case 128: return launch_ct<C, 128, AXIS>(c, a, d, batch, sign, op, sub);
+    case 192: return launch_ct<C, 192, AXIS>(c, a, d, batch, sign, op, sub);
     default: break;
   }
   const int TL = tile_lines<C>(AXIS, n, 0);

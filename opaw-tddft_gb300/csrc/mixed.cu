@@ -665,7 +665,11 @@ __global__ void k_mix_final(float2 *__restrict__ xh, float2 *__restrict__ xl, fl
   double D[6] = {0, 0, 0, 0, 0, 0};
   float Df[6] = {0, 0, 0, 0, 0, 0};
   int nd = 0;
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
+  // grid coordinates carried along the grid-stride loop (no divisions per point)
+  const int64_t g0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  int gx = (int)(g0 % nx), gy = (int)((g0 / nx) % ny), gz = (int)(g0 / ((int64_t)nx * ny));
+  const int sx = (int)(stride % nx), sy = (int)((stride / nx) % ny), sz = (int)(stride / ((int64_t)nx * ny));
+  for (int64_t g = g0; g < nn; g += stride) {
     const int64_t i = (int64_t)o * nn + g;
     const float2 a = xh[i], al = xl[i], b = yh[i], bl = yl[i], s0 = ks0[i], sd = ksd[i];
     const FF Xx{a.x, al.x}, Xy{a.y, al.y}, Yx{b.x, bl.x}, Yy{b.y, bl.y};
@@ -681,9 +685,18 @@ __global__ void k_mix_final(float2 *__restrict__ xh, float2 *__restrict__ xl, fl
     acc.add(af, bf);
     const float rho = af.x * af.x + af.y * af.y;
     const float drho = 2.f * (af.x * bf.x + af.y * bf.y) + bf.x * bf.x + bf.y * bf.y;
-    const int gi = (int)g, gxy = gi / nx;
-    const int gx = gi - gxy * nx, gz = gxy / ny, gy = gxy - gz * ny;
     const float r[3] = {(float)(gx - nx / 2) * dx, (float)(gy - ny / 2) * dy, (float)(gz - nz / 2) * dz};
+    gx += sx;
+    if (gx >= nx) {
+      gx -= nx;
+      gy++;
+    }
+    gy += sy;
+    if (gy >= ny) {
+      gy -= ny;
+      gz++;
+    }
+    gz += sz;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       Df[k] += r[k] * rho;

@@ -160,12 +160,46 @@ template <typename R> struct OpEmbed {
   __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
 
+// in-place pass whose loads read zero outside [lo, hi) of one coordinate
+// (axis 1: y, axis 2: z): the lines there were never written (the
+// embedded source is zero there)
+template <typename C> struct OpMasked {
+  C *wb;
+  int64_t div;  // nxb (y) or nxb*nyb (z)
+  int nmod, lo, hi;
+  static constexpr bool kMid = false;
+  __device__ C load(int, int64_t g) const {
+    const int q = (int)((g / div) % nmod);
+    if (q < lo || q >= hi) {
+      C z;
+      z.x = 0;
+      z.y = 0;
+      return z;
+    }
+    return wb[g];
+  }
+  __device__ void store(int, int64_t g, C v) const { wb[g] = v; }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ C mid(int, int64_t, double, int, C v) const { return v; }
+};
+
 template <typename R> struct OpVk {
   typedef typename Tr<R>::C C;
   C *wb;
   const R *vk;
+  int64_t zdiv;  // nxb*nyb; loads outside z in [zlo, zhi) read zero
+  int zlo, zhi;
   static constexpr bool kMid = true;
-  __device__ C load(int, int64_t g) const { return wb[g]; }
+  __device__ C load(int, int64_t g) const {
+    const int z = (int)(g / zdiv);
+    if (z < zlo || z >= zhi) {
+      C v;
+      v.x = 0;
+      v.y = 0;
+      return v;
+    }
+    return wb[g];
+  }
   __device__ void store(int, int64_t g, C v) const { wb[g] = v; }
   __device__ double line(int64_t) const { return 0.0; }
   __device__ C mid(int, int64_t g, double, int, C v) const {
@@ -210,15 +244,21 @@ int hartree_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0
   Embed e{c->nx, c->ny, c->nz, c->nxb, c->nyb, c->nxb / 2 - c->nx / 2, c->nyb / 2 - c->ny / 2, c->nzb / 2 - c->nz / 2};
   Dims3 d{c->nxb, c->nyb, c->nzb};
   const double nbd = (double)c->nxb * (double)c->nyb * (double)c->nzb;
+  // The source fills only the inner nx x ny x nz block and only that block
+  // is kept: x passes need the lines with y and z inside it, y passes the
+  // planes with z inside it (3 of the 5 passes shrink to 1/4 or 1/2).  Lines
+  // left unwritten are masked to zero where a later pass reads them.
+  const LineSub xlines{e.my, c->ny, e.mz, c->nz}, ylines{0, c->nyb, e.mz, c->nz};
   OpEmbed<R> emb{e, dens0, dens1, wb};
+  OpMasked<C> yfwd{wb, (int64_t)c->nxb, c->nyb, e.my, e.my + c->ny};
   OpCopy<C> inplace{wb, wb, c->nnb};
-  OpVk<R> vkop{wb, VkOf<R>::get(c)};
+  OpVk<R> vkop{wb, VkOf<R>::get(c), (int64_t)c->nxb * c->nyb, e.mz, e.mz + c->nz};
   OpCrop<R> crop{e, wb, vh0, vh1, 1.0 / nbd, nbd};
-  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 1, -1, emb)));
-  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, 1, -1, inplace)));
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 1, -1, emb, &xlines)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, 1, -1, yfwd, &ylines)));
   OPAW_CHECK((launch_axis<C, 2>(c, c->fftb.ax[2], d, 1, 0, vkop)));
-  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, 1, +1, inplace)));
-  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 1, +1, crop)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, 1, +1, inplace, &ylines)));
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 1, +1, crop, &xlines)));
   return OPAW_OK;
 }
 
