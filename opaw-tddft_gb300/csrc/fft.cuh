@@ -458,6 +458,99 @@ __device__ __forceinline__ void ct_stage(const C *__restrict__ in, C *__restrict
   }
 }
 
+// ---- stages with explicit element accessors (shared tile or global memory)
+// Element j (along the transformed axis) of line l of the tile.
+template <typename C, int TL> struct SmemAcc {
+  C *p;
+  __device__ __forceinline__ C get(int j, int l) const { return p[j * (TL + 1) + l]; }
+  __device__ __forceinline__ void put(int j, int l, C v) const { p[j * (TL + 1) + l] = v; }
+};
+template <typename C, class Op> struct GlobIn {  // the op's load; lines past nl read zero
+  Op op;
+  int b, lstride, jstride, nl;
+  int64_t base;
+  __device__ __forceinline__ C get(int j, int l) const {
+    C v;
+    v.x = 0;
+    v.y = 0;
+    if (l < nl) v = op.load(b, base + (int64_t)l * lstride + (int64_t)j * jstride);
+    return v;
+  }
+};
+template <typename C, int TL, class Op, typename L> struct MidAcc {  // k-space hook on the way into the tile
+  C *p;
+  Op op;
+  int b, lstride, jstride, nl;
+  int64_t base;
+  const L *lvs;
+  __device__ __forceinline__ void put(int j, int l, C v) const {
+    if (l < nl) v = op.mid(b, base + (int64_t)l * lstride + (int64_t)j * jstride, lvs[l], j, v);
+    p[j * (TL + 1) + l] = v;
+  }
+};
+template <typename C, class Op> struct GlobOut {  // the op's store; lines past nl skipped
+  Op op;
+  int b, lstride, jstride, nl;
+  int64_t base;
+  __device__ __forceinline__ void put(int j, int l, C v) const {
+    if (l < nl) op.store(b, base + (int64_t)l * lstride + (int64_t)j * jstride, v);
+  }
+};
+
+template <typename C, int N, int TL, int NT, int S, class In, class Out>
+__device__ __forceinline__ void ct_stage_io(const In &in, const Out &out, const C *tw, int sign) {
+  constexpr int R = ct_radix(N, S);
+  constexpr int P = ct_pre(N, S);
+  constexpr int M = N / R;
+  constexpr int NB = TL * M;
+  constexpr int TSTEP = N / (P * R);
+#pragma unroll 1
+  for (int idx = threadIdx.x; idx < NB; idx += NT) {
+    const int l = idx % TL;
+    const int i = idx / TL;
+    const int k = i % P;
+    C u[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) u[q] = in.get(i + q * M, l);
+    if (P > 1) {
+#pragma unroll
+      for (int q = 1; q < R; q++) u[q] = cmul(u[q], twid(tw, q * k * TSTEP, sign));
+    }
+    Butterfly<C, R>::run(u, tw, N, sign);
+    const int j = (i - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; q++) out.put(j + q * P, l, u[q]);
+  }
+}
+
+// forward stages S..: the first reads `in`, the last writes through the
+// k-space hook into buffer `dst`; returns the buffer holding the result
+template <typename C, int N, int TL, int NT, int S, class In, class Mid>
+__device__ __forceinline__ C *ct_fwd_mid(const In &in, C *dst, C *oth, const C *tw, Mid mo) {
+  if constexpr (S == ct_nstage(N) - 1) {
+    mo.p = dst;
+    ct_stage_io<C, N, TL, NT, S>(in, mo, tw, -1);
+    __syncthreads();
+    return dst;
+  } else {
+    ct_stage_io<C, N, TL, NT, S>(in, SmemAcc<C, TL>{dst}, tw, -1);
+    __syncthreads();
+    return ct_fwd_mid<C, N, TL, NT, S + 1>(SmemAcc<C, TL>{dst}, oth, dst, tw, mo);
+  }
+}
+
+// inverse stages S.. from shared buffer src; the last writes through `out`
+template <typename C, int N, int TL, int NT, int S, class Out>
+__device__ __forceinline__ void ct_inv_out(C *src, C *oth, const C *tw, const Out &out) {
+  if constexpr (S == ct_nstage(N) - 1) {
+    ct_stage_io<C, N, TL, NT, S>(SmemAcc<C, TL>{src}, out, tw, +1);
+  } else {
+    ct_stage_io<C, N, TL, NT, S>(SmemAcc<C, TL>{src}, SmemAcc<C, TL>{oth}, tw, +1);
+    __syncthreads();
+    ct_inv_out<C, N, TL, NT, S + 1>(oth, src, tw, out);
+  }
+}
+
 template <typename C, int N, int TL, int NT, int S> struct CtStages {
   // runs stages S.. and returns the buffer holding the result
   static __device__ __forceinline__ C *run(C *a, C *b, const C *tw, int sign) {
@@ -519,6 +612,20 @@ __global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, LineSub sub, int sign, 
   int lstride, jstride, nl;
   ct_tile_geom<N, TL, AXIS>(d, sub, tile, base, lstride, jstride, nl);
   constexpr int TOT = TL * N;
+  if constexpr (Op::kMid) {
+    // forward transform -> k-space hook -> inverse transform: the first stage
+    // reads global memory, the hook rides on the last forward stage's
+    // writes, the last inverse stage writes global memory
+    typedef decltype(op.line(0)) L;
+    __shared__ L lvs[TL];
+    if (threadIdx.x < nl) lvs[threadIdx.x] = op.line(base + threadIdx.x * lstride);
+    __syncthreads();  // twiddles and line values
+    GlobIn<C, Op> gin{op, b, lstride, jstride, nl, base};
+    MidAcc<C, TL, Op, L> mo{bufa, op, b, lstride, jstride, nl, base, lvs};
+    C *res = ct_fwd_mid<C, N, TL, NT, 0>(gin, bufa, bufb, tw, mo);
+    ct_inv_out<C, N, TL, NT, 0>(res, res == bufa ? bufb : bufa, tw, GlobOut<C, Op>{op, b, lstride, jstride, nl, base});
+    return;
+  }
   if constexpr (HasRaw<Op>::value) {
     const C *src = op.raw(b);
 #pragma unroll 4
@@ -542,21 +649,7 @@ __global__ void __launch_bounds__(256) k_fft_ct(Dims3 d, LineSub sub, int sign, 
   }
   __syncthreads();
   C *res;
-  if constexpr (Op::kMid) {
-    // per-line value of the k-space hook (e.g. kx^2 + ky^2 of a z-line)
-    __shared__ decltype(op.line(0)) lvs[TL];
-    if (threadIdx.x < nl) lvs[threadIdx.x] = op.line(base + threadIdx.x * lstride);
-    res = CtStages<C, N, TL, NT, 0>::run(bufa, bufb, tw, -1);
-#pragma unroll 4
-    for (int e = threadIdx.x; e < TOT; e += NT) {
-      const int j = e / TL, l = e - j * TL;
-      if (l < nl) res[j * LS + l] = op.mid(b, base + l * lstride + j * jstride, lvs[l], j, res[j * LS + l]);
-    }
-    __syncthreads();
-    res = CtStages<C, N, TL, NT, 0>::run(res, res == bufa ? bufb : bufa, tw, +1);
-  } else {
-    res = CtStages<C, N, TL, NT, 0>::run(bufa, bufb, tw, sign);
-  }
+  res = CtStages<C, N, TL, NT, 0>::run(bufa, bufb, tw, sign);
 #pragma unroll 4
   for (int e = threadIdx.x; e < TOT; e += NT) {
     int l, j;
