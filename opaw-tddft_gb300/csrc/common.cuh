@@ -12,6 +12,9 @@
 
 namespace opaw {
 
+// union points per tile of the box-coefficient pass
+constexpr int kUTile = 128;
+
 // ---------------------------------------------------------------- errors --
 void set_error(const std::string &msg);
 const char *get_error();
@@ -186,6 +189,15 @@ struct opaw_ctx {
   // union of projector boxes: CSR over grid points
   int nunion = 0, nuent = 0;
   int *d_upt = nullptr, *d_ustart = nullptr, *d_uatom = nullptr, *d_ubox = nullptr;
+  // per union entry: {projector-table offset of the box point, index of the
+  // atom among the distinct atoms of its tile of kUTile union points,
+  // projector count, box size}; per tile its atoms' first slots and projector
+  // counts (utile_na atoms, at most uamax); null when the table offsets
+  // exceed int32
+  int4 *d_uent = nullptr;
+  int2 *d_utile = nullptr;
+  int *d_utile_na = nullptr;
+  int uamax = 0;
   int *d_boxg = nullptr;         // per atom and box point: the wrapped linear grid index
   int64_t *d_boff = nullptr;     // per atom offset into d_boxg
   int *d_uidx = nullptr;         // per grid point: its union index, -1 outside every box

@@ -178,6 +178,35 @@ static int build(opaw_ctx *c, const opaw_system *s) {
     OPAW_CHECK(upload(&c->d_ustart, ustart.data(), ustart.size()));
     OPAW_CHECK(upload(&c->d_uatom, uatom.data(), uatom.size()));
     OPAW_CHECK(upload(&c->d_ubox, ubox.data(), ubox.size()));
+    if (c->h_poff[na] < INT32_MAX) {
+      // distinct atoms of every tile of kUTile union points, in order of
+      // first appearance, and each entry's index among them
+      const int nu = (int)upt.size(), ntile = (nu + kUTile - 1) / kUTile;
+      std::vector<int4> uent(ents.size());
+      std::vector<std::vector<int>> tat(ntile);
+      for (int u = 0; u < nu; u++) {
+        std::vector<int> &ta = tat[u / kUTile];
+        for (int e = ustart[u]; e < ustart[u + 1]; e++) {
+          const int a = ents[e].a;
+          int la = (int)(std::find(ta.begin(), ta.end(), a) - ta.begin());
+          if (la == (int)ta.size()) ta.push_back(a);
+          const int nbox = s->nrough[3 * a] * s->nrough[3 * a + 1] * s->nrough[3 * a + 2];
+          uent[e] = make_int4((int)(c->h_poff[a] + ents[e].b), la, s->ms[a], nbox);
+        }
+      }
+      int amax = 1;
+      for (const auto &ta : tat) amax = std::max(amax, (int)ta.size());
+      std::vector<int2> ut((size_t)ntile * amax, make_int2(0, 0));
+      std::vector<int> utn(ntile);
+      for (int t = 0; t < ntile; t++) {
+        utn[t] = (int)tat[t].size();
+        for (int k = 0; k < utn[t]; k++) ut[(size_t)t * amax + k] = make_int2((int)c->h_soff[tat[t][k]], s->ms[tat[t][k]]);
+      }
+      c->uamax = amax;
+      OPAW_CHECK(upload(&c->d_uent, uent.data(), uent.size()));
+      OPAW_CHECK(upload(&c->d_utile, ut.data(), ut.size()));
+      OPAW_CHECK(upload(&c->d_utile_na, utn.data(), utn.size()));
+    }
     std::vector<int> uidx((size_t)c->nn, -1);
     for (int u = 0; u < c->nunion; u++) uidx[upt[u]] = u;
     OPAW_CHECK(upload(&c->d_uidx, uidx.data(), uidx.size()));
@@ -332,7 +361,7 @@ static int build(opaw_ctx *c, const opaw_system *s) {
 static void destroy(opaw_ctx *c) {
   void *ptrs[] = {c->d_ms, c->d_nrough, c->d_ir0, c->d_poff, c->d_soff, c->d_doff, c->d_p3d, c->d_p3d1,
                   c->d_p3d_f, c->d_p3d1_f, c->d_s, c->d_sinv, c->d_slot_atom, c->d_dslot_atom, c->d_upt,
-                  c->d_ustart, c->d_uatom, c->d_ubox, c->d_ngrid, c->d_nlm, c->d_goff, c->d_g3off, c->d_qoff,
+                  c->d_ustart, c->d_uatom, c->d_ubox, c->d_uent, c->d_utile, c->d_utile_na, c->d_ngrid, c->d_nlm, c->d_goff, c->d_g3off, c->d_qoff,
                   c->d_eoff, c->d_gpt, c->d_g3d, c->d_qijlm, c->d_dij0, c->d_eijkl, c->d_cpt, c->d_cstart,
                   c->d_catom, c->d_cig, c->d_vloc, c->d_ncoret, c->d_vk, c->d_vk_f};
   for (void *p : ptrs) cudaFree(p);

@@ -548,6 +548,108 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+// The same terms by tiles of kUTile union points and OG orbitals.  The CTA
+// first copies the coefficients of its tile's atoms (utile) for its orbitals
+// into shared memory, three float4 per (atom, orbital, projector):
+// -i cD and -i c2 of set 0, of set 1, then c3 of both sets.  A thread then
+// takes one union point: per entry (uent: table offset, tile-local atom,
+// projector count, box size) it loads the projector values once and reads
+// the coefficients as shared-memory broadcasts.  The sums run in the order
+// of the generic kernel above.  MODE bit 0: the B terms (stage), bit 1: the
+// G terms (write_t).
+template <int MODE, int MS, int OG>
+__global__ void __launch_bounds__(kUTile, 6)
+    k_mix_boxcoef_t(int nunion, int norb, int ns, int amax, const int *__restrict__ ustart,
+                    const int4 *__restrict__ uent, const int2 *__restrict__ utile, const int *__restrict__ utile_na,
+                    const float *__restrict__ P0, const float *__restrict__ P1, const float4 *__restrict__ cab,
+                    const float2 *__restrict__ cg, float2 *__restrict__ BG) {
+  constexpr bool kB = (MODE & 1) != 0, kG = (MODE & 2) != 0;
+  extern __shared__ float4 cs[];  // [tile atom][OG][MS][3]
+  const int tile = blockIdx.x;
+  const int o0 = blockIdx.y * OG;
+  const int64_t kstride = (int64_t)norb * ns;
+  const int na = utile_na[tile];
+  for (int t = threadIdx.x; t < na * OG * MS; t += kUTile) {
+    const int la = t / (OG * MS), r = t - la * (OG * MS), j = r / MS, i = r - j * MS;
+    const int2 at = utile[(int64_t)tile * amax + la];
+    float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, g = a0;
+    if (i < at.y) {
+      const int64_t k = (int64_t)min(o0 + j, norb - 1) * ns + at.x + i;
+      if (kB) {
+        a0 = cab[k];
+        a1 = cab[kstride + k];
+      }
+      if (kG) {
+        const float2 g0 = cg[k], g1 = cg[kstride + k];
+        g = make_float4(g0.x, g0.y, g1.x, g1.y);
+      }
+    }
+    cs[3 * t] = a0;
+    cs[3 * t + 1] = a1;
+    cs[3 * t + 2] = g;
+  }
+  __syncthreads();
+  const int u = tile * kUTile + threadIdx.x;
+  if (u >= nunion) return;
+  float2 B[OG][2], G[OG][2];
+#pragma unroll
+  for (int j = 0; j < OG; j++)
+#pragma unroll
+    for (int X = 0; X < 2; X++) B[j][X] = G[j][X] = make_float2(0.f, 0.f);
+  const int e1 = ustart[u + 1];
+  for (int e = ustart[u]; e < e1; e++) {
+    const int4 E = uent[e];
+    float p[MS], q[MS];
+#pragma unroll
+    for (int i = 0; i < MS; i++) {
+      p[i] = q[i] = 0.f;
+      if (i < E.z) {
+        if (kB) p[i] = P0[E.x + i * E.w];
+        q[i] = P1[E.x + i * E.w];
+      }
+    }
+    const float4 *cb = cs + (int64_t)E.y * (OG * MS * 3);
+#pragma unroll
+    for (int j = 0; j < OG; j++) {
+#pragma unroll
+      for (int i = 0; i < MS; i++) {
+        if (i < E.z) {
+          const float4 *cc = cb + (j * MS + i) * 3;
+          if (kB) {
+            const float4 c0 = cc[0], c1 = cc[1];
+            B[j][0].x += p[i] * c0.x + q[i] * c0.z;
+            B[j][0].y += p[i] * c0.y + q[i] * c0.w;
+            B[j][1].x += p[i] * c1.x + q[i] * c1.z;
+            B[j][1].y += p[i] * c1.y + q[i] * c1.w;
+          }
+          if (kG) {
+            const float4 c2 = cc[2];
+            G[j][0].x += q[i] * c2.x;
+            G[j][0].y += q[i] * c2.y;
+            G[j][1].x += q[i] * c2.z;
+            G[j][1].y += q[i] * c2.w;
+          }
+        }
+      }
+    }
+  }
+  const int64_t su = (int64_t)norb * nunion;
+#pragma unroll
+  for (int j = 0; j < OG; j++) {
+    if (o0 + j < norb) {
+      const int64_t bi = (int64_t)(o0 + j) * nunion + u;
+      if (kB) {
+        BG[bi] = B[j][0];
+        BG[su + bi] = B[j][1];
+      }
+      if (kG) {
+        BG[2 * su + bi] = G[j][0];
+        BG[3 * su + bi] = G[j][1];
+      }
+    }
+  }
+}
+
 // Tail of the step.  FP64 arithmetic only where psi and delta are updated;
 // the norms and the dipole take FP32 products of the rounded values, summed
 // in FP32 over chunks of 32 points and in FP64 across chunks (their relative
@@ -911,7 +1013,16 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
   f.stage = stage;
   f.first = first;
   f.write_t = write_t;
-  if (c->nunion > 0 && c->ns > 0) {
+  constexpr int OG = 4, MS = 8;
+  const size_t bsmem = sizeof(float4) * 3 * OG * MS * (size_t)c->uamax;
+  if (c->nunion > 0 && c->ns > 0 && c->d_uent && c->msmax <= MS && bsmem <= 48 * 1024 && (stage || write_t)) {
+    const dim3 nb((c->nunion + kUTile - 1) / kUTile, (m.norb + OG - 1) / OG);
+    const int mode = (stage ? 1 : 0) | (write_t ? 2 : 0);
+    auto kern = mode == 1 ? k_mix_boxcoef_t<1, MS, OG> : mode == 2 ? k_mix_boxcoef_t<2, MS, OG> : k_mix_boxcoef_t<3, MS, OG>;
+    kern<<<nb, kUTile, bsmem, c->stream>>>(c->nunion, m.norb, c->ns, c->uamax, c->d_ustart, c->d_uent, c->d_utile,
+                                          c->d_utile_na, c->d_p3d_f, c->d_p3d1_f, m.cab, m.cg, m.bg);
+    MIX_LAUNCHED();
+  } else if (c->nunion > 0 && c->ns > 0) {
     const dim3 nb(grid1(c->nunion, 128), m.norb);
     k_mix_boxcoef<<<nb, 128, 0, c->stream>>>(c->nunion, m.norb, c->ns, c->d_ustart, c->d_uatom, c->d_ubox,
                                              c->d_p3d_f, c->d_p3d1_f, c->d_poff, c->d_nrough, c->d_ms, c->d_soff,
