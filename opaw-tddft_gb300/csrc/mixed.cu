@@ -771,9 +771,19 @@ __global__ void k_mix_final(float2 *__restrict__ xh, float2 *__restrict__ xl, fl
   const int64_t g0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
   int gx = (int)(g0 % nx), gy = (int)((g0 / nx) % ny), gz = (int)(g0 / ((int64_t)nx * ny));
   const int sx = (int)(stride % nx), sy = (int)((stride / nx) % ny), sz = (int)(stride / ((int64_t)nx * ny));
+  // the six operands of the next point are loaded while this one is combined
+  const int64_t ob = (int64_t)o * nn;
+  float2 na = make_float2(0.f, 0.f), nal = na, nb = na, nbl = na, ns0 = na, nsd = na;
+  if (g0 < nn) {
+    na = xh[ob + g0], nal = xl[ob + g0], nb = yh[ob + g0], nbl = yl[ob + g0], ns0 = ks0[ob + g0], nsd = ksd[ob + g0];
+  }
   for (int64_t g = g0; g < nn; g += stride) {
-    const int64_t i = (int64_t)o * nn + g;
-    const float2 a = xh[i], al = xl[i], b = yh[i], bl = yl[i], s0 = ks0[i], sd = ksd[i];
+    const int64_t i = ob + g;
+    const float2 a = na, al = nal, b = nb, bl = nbl, s0 = ns0, sd = nsd;
+    if (g + stride < nn) {
+      const int64_t k = i + stride;
+      na = xh[k], nal = xl[k], nb = yh[k], nbl = yl[k], ns0 = ks0[k], nsd = ksd[k];
+    }
     const FF Xx{a.x, al.x}, Xy{a.y, al.y}, Yx{b.x, bl.x}, Yy{b.y, bl.y};
     const FF nxx = ff_add(ff_mul(f0, Xx), ff_mulf(hh, s0.x));
     const FF nxy = ff_add(ff_mul(f0, Xy), ff_mulf(hh, s0.y));
