@@ -39,8 +39,8 @@ UNIT = "orbital-steps/s"
 # k_mix_dense on the 96^3 / 40-atom workload with 128 orbitals per set: DRAM
 # bytes (read + write) of the five launches of one step (start, RK4 stages
 # 1-4) measured by ncu, averaged per launch, and their algorithmic bytes
-DENSE_TRAFFIC_128 = (3906464768 + 7840081664 + 9668237568 + 9672405248 + 5704129024) / 5
-DENSE_ALG_128 = (3.95e9 + 7.87e9 + 9.68e9 + 9.68e9 + 5.75e9) / 5
+DENSE_TRAFFIC_128 = (3907100928 + 7840902144 + 9668066304 + 9667104000 + 5704336896) / 5
+DENSE_ALG_128 = (3.951e9 + 7.884e9 + 9.696e9 + 9.696e9 + 5.749e9) / 5
 CPU_SAMPLE_NORB = 2
 
 
@@ -422,13 +422,13 @@ def main():
         fp64 = fp64_compare(ctx, pkg, torch, stream, fresh, args.compare_steps, ipol, norb, el_max / args.steps)
     peak, peak_kind = load_peaks()
     roof = {"kernel": "k_mix_dense (fused RK4 accumulation / S^-1/2 / density pass over every grid point, "
-                      "box terms from k_mix_boxcoef; the largest share of the step)",
+                      "box terms from k_mix_boxcoef_t; the largest share of the step)",
             "bound": "hbm", "achieved": kt_bytes / (kt_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
             "frac": kt_bytes / (kt_ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
             "traffic": DENSE_TRAFFIC_128 * norb / 128,
             "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the five launches of one step at "
                             "128 orbitals, per launch (algorithmic: "
-                            f"{DENSE_ALG_128 * norb / 128:.4g}; profiles/launches_tddft_step_96cube_128orb.md)",
+                            f"{DENSE_ALG_128 * norb / 128:.4g}; profiles/dram_traffic_k_mix_dense_96cube_128orb.md)",
             "alg_bytes_per_launch": kt_bytes / max(kt_n, 1), "avg_launch_ms": kt_ms / max(kt_n, 1),
             "launches_timed": kt_n, "timing": "CUDA events on the library stream around each launch, "
                                               "inside the timed region"}

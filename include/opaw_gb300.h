@@ -226,6 +226,10 @@ int opaw_dipole(opaw_ctx *ctx, double gamma, double *dip, double *dip_pert, doub
  * receives 3*nsteps values (may be NULL). */
 int opaw_tddft_steps(opaw_ctx *ctx, int nsteps, double dt, double gamma, int precision,
                      double *d_dip_out);
+/* the same with everything plot_dip writes per step (tddft_plot.f90:101-104):
+ * dip, dip_pert and d_dip, 3*nsteps values each (any may be NULL) */
+int opaw_tddft_steps_dip(opaw_ctx *ctx, int nsteps, double dt, double gamma, int precision,
+                         double *dip_out, double *dip_pert_out, double *d_dip_out);
 /* the same, with psi uploaded from and downloaded to host arrays around the
  * steps (the propdt boundary with Fortran-resident phi_bar/phi_bar_pert) */
 int opaw_tddft_steps_host(opaw_ctx *ctx, double *psi, double *psi_pert, int norb, int nsteps,

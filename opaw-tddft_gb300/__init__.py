@@ -100,6 +100,7 @@ SIGNATURES = {
     "opaw_excite": (ct.c_int, [_P, ct.c_int, ct.c_double]),
     "opaw_dipole": (ct.c_int, [_P, ct.c_double, _P, _P, _P]),
     "opaw_tddft_steps": (ct.c_int, [_P, ct.c_int, ct.c_double, ct.c_double, ct.c_int, _P]),
+    "opaw_tddft_steps_dip": (ct.c_int, [_P, ct.c_int, ct.c_double, ct.c_double, ct.c_int, _P, _P, _P]),
     "opaw_tddft_steps_host": (ct.c_int, [_P, _P, _P, ct.c_int, ct.c_int, ct.c_double, ct.c_double,
                                          ct.c_int, _P]),
 }
@@ -353,6 +354,15 @@ class Context:
         _check(lib().opaw_tddft_steps(self.h, nsteps, float(dt), float(gamma), precision,
                                       _ptr(out) if want_dipoles else None))
         return out[:nsteps] if want_dipoles else None
+
+    def tddft_steps_dip(self, nsteps, dt, gamma, precision=PREC_FP64):
+        """nsteps steps; returns (dip, dip_pert, d_dip), each [nsteps, 3]: the
+        values plot_dip writes to dip.dat and d_dip.dat."""
+        n = max(nsteps, 1)
+        dip, dpp, dd = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3))
+        _check(lib().opaw_tddft_steps_dip(self.h, nsteps, float(dt), float(gamma), precision, _ptr(dip),
+                                          _ptr(dpp), _ptr(dd)))
+        return dip[:nsteps], dpp[:nsteps], dd[:nsteps]
 
     def tddft_steps_host(self, psi, psi_pert, nsteps, dt, gamma, precision=PREC_FP64):
         """Uploads both orbital sets from host arrays, propagates, downloads

@@ -277,7 +277,8 @@ static int need_psi(opaw_ctx *c, int set) {
   return OPAW_OK;
 }
 
-int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, double *d_dip_out) {
+int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, double *d_dip_out, double *dip_out,
+                double *dip_pert_out) {
   OPAW_CHECK(need_psi(c, 0));
   OPAW_CHECK(need_psi(c, 1));
   OPAW_ARG(c->norb[0] == c->norb[1], "both sets must hold the same number of orbitals");
@@ -298,12 +299,16 @@ int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, doub
     }
     OPAW_CHECK(dipole_dev(c, gamma, dd + 9 * (size_t)it));  // plot_dip (tddft.f90:84)
   }
-  if (d_dip_out && nsteps > 0) {
+  if ((d_dip_out || dip_out || dip_pert_out) && nsteps > 0) {
     std::vector<double> h(9 * (size_t)nsteps);
     OPAW_CUDA(cudaMemcpyAsync(h.data(), dd, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
     OPAW_CUDA(cudaStreamSynchronize(c->stream));
     for (int it = 0; it < nsteps; it++)
-      for (int k = 0; k < 3; k++) d_dip_out[3 * it + k] = h[9 * (size_t)it + 6 + k];
+      for (int k = 0; k < 3; k++) {
+        if (dip_out) dip_out[3 * it + k] = h[9 * (size_t)it + k];
+        if (dip_pert_out) dip_pert_out[3 * it + k] = h[9 * (size_t)it + 3 + k];
+        if (d_dip_out) d_dip_out[3 * it + k] = h[9 * (size_t)it + 6 + k];
+      }
   }
   return OPAW_OK;
 }
@@ -494,7 +499,14 @@ int opaw_dipole(opaw_ctx *c, double gamma, double *dip, double *dip_pert, double
 
 int opaw_tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int precision, double *d_dip_out) {
   OPAW_CHECK(check_cs(c, 0));
-  OPAW_CHECK(tddft_steps(c, nsteps, dt, gamma, precision, d_dip_out));
+  OPAW_CHECK(tddft_steps(c, nsteps, dt, gamma, precision, d_dip_out, nullptr, nullptr));
+  return finish(c);
+}
+
+int opaw_tddft_steps_dip(opaw_ctx *c, int nsteps, double dt, double gamma, int precision, double *dip_out,
+                         double *dip_pert_out, double *d_dip_out) {
+  OPAW_CHECK(check_cs(c, 0));
+  OPAW_CHECK(tddft_steps(c, nsteps, dt, gamma, precision, d_dip_out, dip_out, dip_pert_out));
   return finish(c);
 }
 
@@ -504,7 +516,7 @@ int opaw_tddft_steps_host(opaw_ctx *c, double *psi, double *psi_pert, int norb, 
   OPAW_ARG(psi && psi_pert && norb > 0, "bad buffers");
   OPAW_CHECK(opaw_psi_upload(c, 0, psi, norb));
   OPAW_CHECK(opaw_psi_upload(c, 1, psi_pert, norb));
-  OPAW_CHECK(tddft_steps(c, nsteps, dt, gamma, precision, d_dip_out));
+  OPAW_CHECK(tddft_steps(c, nsteps, dt, gamma, precision, d_dip_out, nullptr, nullptr));
   OPAW_CHECK(opaw_psi_download(c, 0, psi, norb));
   OPAW_CHECK(opaw_psi_download(c, 1, psi_pert, norb));
   return OPAW_OK;

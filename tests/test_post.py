@@ -131,3 +131,79 @@ def test_restart_through_context(tmp_path):
     assert np.array_equal(c2.download(0, 3).reshape(3, -1), psi)
     assert np.array_equal(c2.download(1, 3).reshape(3, -1), pp)
     c2.close()
+
+
+def test_fortran_e_format():
+    """Ew.d output of format 888 (' ',4e18.8) in tddft_plot.f90."""
+    from opaw_tddft_gb300.dipfile import fortran_e, format_d_dip_line
+
+    assert fortran_e(1.5) == "    0.15000000E+01"
+    assert fortran_e(-0.0123456789) == "   -0.12345679E-01"
+    assert fortran_e(0.0) == "    0.00000000E+00"
+    assert fortran_e(9.9999999999) == "    0.10000000E+02"
+    assert fortran_e(2.5e-120) == "    0.25000000-119"
+    line = format_d_dip_line(0.05, [1.0, -2.0, 3.0e-5])
+    assert line == " " + "    0.50000000E-01    0.10000000E+01   -0.20000000E+01    0.30000000E-04\n"
+
+
+def test_dipole_log_restart_chain(tmp_path):
+    """plot_dip's files over a fresh run, a first restart (d_dip_cont.dat
+    seeded from d_dip.dat) and a second restart (appended)."""
+    from opaw_tddft_gb300.dipfile import DipoleLog, read_series
+
+    rng = np.random.default_rng(3)
+    dt = 0.05
+    dd, dp, dq = rng.standard_normal((9, 3)), rng.standard_normal((9, 3)), rng.standard_normal((9, 3))
+    with DipoleLog(dt, tmp_path) as log:  # fresh run, steps 1-5
+        log.write_steps(0, dp[:5], dq[:5], dd[:5])
+    a = read_series(tmp_path / "d_dip.dat")
+    assert a.shape == (5, 4)
+    assert np.allclose(a[:, 0], dt * np.arange(5), atol=1e-12)
+    assert np.allclose(a[:, 1:], dd[:5], rtol=1e-7, atol=0)
+    b = read_series(tmp_path / "dip.dat")
+    assert b.shape == (5, 7) and np.allclose(b[:, 1:4], dp[:5], rtol=1e-15) and np.allclose(b[:, 4:], dq[:5], rtol=1e-15)
+    with DipoleLog(dt, tmp_path, it_restart=3) as log:  # restarted from step 3's checkpoint
+        with pytest.raises(ValueError):
+            log.write(5, dd[4], dp[4], dq[4])
+        log.write_steps(3, dp[3:6], dq[3:6], dd[3:6])
+    c = read_series(tmp_path / "d_dip_cont.dat")
+    assert c.shape == (6, 4)
+    assert np.array_equal(c[:3], a[:3])  # copied through the same format
+    assert np.allclose(c[3:, 1:], dd[3:6], rtol=1e-7, atol=0)
+    e = read_series(tmp_path / "dip_cont.dat")
+    assert e.shape == (6, 7)
+    assert np.all(np.isnan(e[:3, 4:])) and np.allclose(e[:3, :4], b[:3, :4], rtol=1e-15)  # t, dip only
+    assert np.allclose(e[3:, 4:], dq[3:6], rtol=1e-15)
+    with DipoleLog(dt, tmp_path, it_restart=6) as log:  # second restart: appended
+        log.write_steps(6, dp[6:9], dq[6:9], dd[6:9])
+    f = read_series(tmp_path / "d_dip_cont.dat")
+    assert f.shape == (9, 4) and np.array_equal(f[:6], c)
+    assert np.allclose(f[6:, 0], dt * np.arange(6, 9), atol=1e-12)
+    assert read_series(tmp_path / "d_dip.dat").shape == (5, 4)  # untouched
+
+
+@pytest.mark.gpu
+def test_steps_dip_matches_steps(tmp_path):
+    """opaw_tddft_steps_dip returns what plot_dip writes: d_dip = (dip_pert -
+    dip) / gamma, and the same d_dip as opaw_tddft_steps from the same state."""
+    import opaw_tddft_gb300 as pkg
+    from opaw_tddft_gb300 import synthetic
+    from opaw_tddft_gb300.dipfile import DipoleLog, read_series
+
+    s = synthetic.small_system("tiny", norb=3)
+    psi = synthetic.orbitals(s, 3, seed=5).reshape(3, -1)
+    gamma = 1e-3
+    c = pkg.Context(s)
+    for prec in (pkg.PREC_FP64, pkg.PREC_MIXED):
+        c.upload(0, psi)
+        c.excite(1, gamma)
+        dip, dpp, dd = c.tddft_steps_dip(3, 0.05, gamma, prec)
+        assert np.allclose(dd, (dpp - dip) / gamma, rtol=1e-6, atol=1e-9 * np.abs(dip).max() / gamma)
+        c.upload(0, psi)
+        c.excite(1, gamma)
+        dd2 = c.tddft_steps(3, 0.05, gamma, prec)
+        assert np.array_equal(dd, dd2)
+    with DipoleLog(0.05, tmp_path) as log:
+        log.write_steps(0, dip, dpp, dd)
+    assert np.allclose(read_series(tmp_path / "d_dip.dat")[:, 1:], dd, rtol=1e-7, atol=0)
+    c.close()
