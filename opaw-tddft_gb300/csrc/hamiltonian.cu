@@ -148,6 +148,25 @@ int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, doubl
 // with values L*PER .. L*PER+PER-1 of the shuffle tree (fixed order).
 constexpr int kG2Warps = 16;
 
+// rows i < m of both tables for box points [c0, c0 + CH) into dst
+// [table][i][point] by cp.async, zeros past the segment end or past m
+template <typename R, int MSMAX, int CH, int NT>
+__device__ __forceinline__ void g2_stage_rows(R *dst, const R *Pa, const R *Qa, int m, int nbox, int c0, int b1) {
+  for (int e = threadIdx.x; e < 2 * MSMAX * CH; e += NT) {
+    const int tab = e / (MSMAX * CH), r = e - tab * (MSMAX * CH);
+    const int i = r / CH, j = r - i * CH;
+    const int b = c0 + j;
+    const bool ok = i < m && b < b1;
+    const R *src = ok ? (tab ? Qa : Pa) + (int64_t)i * nbox + b : Pa;
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + e);
+    const int n = ok ? (int)sizeof(R) : 0;  // 0: the destination is zero-filled
+    if constexpr (sizeof(R) == 4)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(src), "r"(n) : "memory");
+    else
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(src), "r"(n) : "memory");
+  }
+}
+
 template <typename R, int MSMAX>
 __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) ? 2 : 1)
     k_gather2(const typename Tr<R>::C *__restrict__ psi, int64_t nn, int norb, const R *__restrict__ P0,
@@ -159,10 +178,13 @@ __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) 
   constexpr int H = 2 * MSMAX;  // values per table: 2 i + re/im
   constexpr int NV = 2 * H;
   constexpr int PER = NV / 32;
-  constexpr int kG2Chunk = sizeof(R) == 4 ? 256 : 128;  // at most 32 KB of staged rows
+  constexpr int kG2Chunk = sizeof(R) == 4 ? 128 : 64;  // points per chunk
   constexpr int U = kG2Chunk / 32;  // points per lane and chunk
+  constexpr int NT = 32 * kG2Warps;
+  constexpr int RV = 2 * MSMAX * kG2Chunk;  // staged row values per chunk
   static_assert(NV == 32 || NV == 64, "8 or 16 projectors per atom");
-  __shared__ R sp[2][MSMAX][kG2Chunk];
+  // the rows of two chunks: chunk c + 1 is copied in (cp.async) while chunk c is summed
+  __shared__ __align__(16) R sp[2][2][MSMAX][kG2Chunk];
   const int a = blockIdx.x / nseg, seg = blockIdx.x - a * nseg;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int o = blockIdx.y * kG2Warps + warp;
@@ -179,28 +201,37 @@ __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) 
   R v[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) v[k] = 0;
-  for (int c0 = b0; c0 < b1; c0 += kG2Chunk) {
+  C zn[U];  // the orbital at the lane's points of the next chunk
+#pragma unroll
+  for (int k = 0; k < U; k++) {
+    const int b = b0 + lane + 32 * k;
+    zn[k].x = zn[k].y = (R)0;
+    if (live && b < b1) zn[k] = po[bg[b]];
+  }
+  if (b0 < b1) g2_stage_rows<R, MSMAX, kG2Chunk, NT>(&sp[0][0][0][0], Pa, Qa, m, nbox, b0, b1);
+  int buf = 0;
+  for (int c0 = b0; c0 < b1; c0 += kG2Chunk, buf ^= 1) {
     C z[U];
 #pragma unroll
-    for (int k = 0; k < U; k++) {
-      const int b = c0 + lane + 32 * k;
-      z[k].x = z[k].y = (R)0;
-      if (live && b < b1) z[k] = po[bg[b]];
+    for (int k = 0; k < U; k++) z[k] = zn[k];
+    cp_async_wait_all();
+    __syncthreads();  // this chunk's rows landed; the other buffer's last reader is done
+    const int c1 = c0 + kG2Chunk;
+    if (c1 < b1) {
+#pragma unroll
+      for (int k = 0; k < U; k++) {
+        const int b = c1 + lane + 32 * k;
+        zn[k].x = zn[k].y = (R)0;
+        if (live && b < b1) zn[k] = po[bg[b]];
+      }
+      g2_stage_rows<R, MSMAX, kG2Chunk, NT>(&sp[buf ^ 1][0][0][0], Pa, Qa, m, nbox, c1, b1);
     }
-    __syncthreads();  // the previous chunk's rows are no longer read
-    for (int e = threadIdx.x; e < 2 * MSMAX * kG2Chunk; e += blockDim.x) {
-      const int tab = e / (MSMAX * kG2Chunk), r = e - tab * (MSMAX * kG2Chunk);
-      const int i = r / kG2Chunk, j = r - i * kG2Chunk;
-      const int b = c0 + j;
-      sp[tab][i][j] = (i < m && b < b1) ? (tab ? Qa : Pa)[(int64_t)i * nbox + b] : (R)0;
-    }
-    __syncthreads();
 #pragma unroll
     for (int k = 0; k < U; k++) {
       const int j = lane + 32 * k;
 #pragma unroll
       for (int i = 0; i < MSMAX; i++) {
-        const R p = sp[0][i][j], q = sp[1][i][j];
+        const R p = sp[buf][0][i][j], q = sp[buf][1][i][j];
         v[2 * i] += p * z[k].x;
         v[2 * i + 1] += p * z[k].y;
         v[H + 2 * i] += q * z[k].x;
