@@ -312,6 +312,8 @@ int fft3d(opaw_ctx *c, const FFT3 &f, typename Tr<R>::C *data, int batch, int si
 int hartree(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1);
 template <typename R>
 int hartree_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1);
+template <typename R>
+int hartree_pair_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1);
 int rhoij_of(opaw_ctx *c, const double2 *coef, int norb, double *out);
 template <typename R> int density_raw(opaw_ctx *c, const typename Tr<R>::C *psit, int norb, double *out);
 int nhat_raw_of(opaw_ctx *c, const double *rhoij, double *out);

@@ -1150,8 +1150,7 @@ static int mix_potentials(opaw_ctx *c, Mix &m) {
   // Hartree of n0 + n^0 and of the difference: two complex64 transforms, so
   // the difference keeps its own relative precision (packing it with the
   // ~1e3 times larger n0 into one transform would round it relative to n0)
-  OPAW_CHECK(hartree_t<float>(c, m.src0, nullptr, m.vh0, nullptr));
-  OPAW_CHECK(hartree_t<float>(c, m.srcd, nullptr, m.dvh, nullptr));
+  OPAW_CHECK(hartree_pair_t<float>(c, m.src0, m.srcd, m.vh0, m.dvh));
   const double *mean = nullptr;
   if (c->periodic) {  // tddft_pot.f90:42-45
     OPAW_CHECK(sums2(c, m.vh0, nullptr, m.part0));

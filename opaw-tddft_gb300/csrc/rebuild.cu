@@ -144,18 +144,24 @@ template <typename R> struct OpEmbed {
   Embed e;
   const double *d0, *d1;
   C *wb;
+  int64_t bs = 0;  // batch stride of wb
+  int pair = 0;    // 1: batch b transforms d0 (b = 0) or d1 (b = 1) alone; 0: d0 + i d1
   static constexpr bool kMid = false;
-  __device__ C load(int, int64_t g) const {
+  __device__ C load(int b, int64_t g) const {
     int64_t i;
     C v;
     v.x = 0;
     v.y = 0;
     if (!e.inner(g, i)) return v;
+    if (pair) {
+      v.x = (R)(b ? d1 : d0)[i];
+      return v;
+    }
     v.x = (R)d0[i];
     v.y = d1 ? (R)d1[i] : (R)0;
     return v;
   }
-  __device__ void store(int, int64_t g, C v) const { wb[g] = v; }
+  __device__ void store(int b, int64_t g, C v) const { wb[b * bs + g] = v; }
   __device__ double line(int64_t) const { return 0.0; }
   __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
@@ -167,8 +173,9 @@ template <typename C> struct OpMasked {
   C *wb;
   int64_t div;  // nxb (y) or nxb*nyb (z)
   int nmod, lo, hi;
+  int64_t bs = 0;  // batch stride of wb
   static constexpr bool kMid = false;
-  __device__ C load(int, int64_t g) const {
+  __device__ C load(int b, int64_t g) const {
     const int q = (int)((g / div) % nmod);
     if (q < lo || q >= hi) {
       C z;
@@ -176,9 +183,9 @@ template <typename C> struct OpMasked {
       z.y = 0;
       return z;
     }
-    return wb[g];
+    return wb[b * bs + g];
   }
-  __device__ void store(int, int64_t g, C v) const { wb[g] = v; }
+  __device__ void store(int b, int64_t g, C v) const { wb[b * bs + g] = v; }
   __device__ double line(int64_t) const { return 0.0; }
   __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
@@ -189,8 +196,9 @@ template <typename R> struct OpVk {
   const R *vk;
   int64_t zdiv;  // nxb*nyb; loads outside z in [zlo, zhi) read zero
   int zlo, zhi;
+  int64_t bs = 0;  // batch stride of wb
   static constexpr bool kMid = true;
-  __device__ C load(int, int64_t g) const {
+  __device__ C load(int b, int64_t g) const {
     const int z = (int)(g / zdiv);
     if (z < zlo || z >= zhi) {
       C v;
@@ -198,9 +206,9 @@ template <typename R> struct OpVk {
       v.y = 0;
       return v;
     }
-    return wb[g];
+    return wb[b * bs + g];
   }
-  __device__ void store(int, int64_t g, C v) const { wb[g] = v; }
+  __device__ void store(int b, int64_t g, C v) const { wb[b * bs + g] = v; }
   __device__ double line(int64_t) const { return 0.0; }
   __device__ C mid(int, int64_t g, double, int, C v) const {
     const R k = vk[g];
@@ -216,11 +224,17 @@ template <typename R> struct OpCrop {
   const C *wb;
   double *v0, *v1;
   double cn, nbd;
+  int64_t bs = 0;  // batch stride of wb
+  int pair = 0;    // 1: batch b holds the potential of v0 (b = 0) or v1 (b = 1)
   static constexpr bool kMid = false;
-  __device__ C load(int, int64_t g) const { return wb[g]; }
-  __device__ void store(int, int64_t g, C v) const {
+  __device__ C load(int b, int64_t g) const { return wb[b * bs + g]; }
+  __device__ void store(int b, int64_t g, C v) const {
     int64_t i;
     if (!e.inner(g, i)) return;
+    if (pair) {
+      (b ? v1 : v0)[i] = ((double)v.x * cn) * nbd;
+      return;
+    }
     v0[i] = ((double)v.x * cn) * nbd;  // rconv :29, get_vcon :20
     if (v1) v1[i] = ((double)v.y * cn) * nbd;
   }
@@ -261,6 +275,33 @@ int hartree_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0
   OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 1, +1, crop, &xlines)));
   return OPAW_OK;
 }
+
+// two independent real sources in one batch of two complex transforms (each
+// keeps its own relative precision): vh0 from dens0, vh1 from dens1
+template <typename R>
+int hartree_pair_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1) {
+  typedef typename Tr<R>::C C;
+  OPAW_CHECK(ensure(c->work[3], 2 * sizeof(C) * c->nnb));
+  C *wb = (C *)c->work[3].p;
+  Embed e{c->nx, c->ny, c->nz, c->nxb, c->nyb, c->nxb / 2 - c->nx / 2, c->nyb / 2 - c->ny / 2, c->nzb / 2 - c->nz / 2};
+  Dims3 d{c->nxb, c->nyb, c->nzb};
+  const double nbd = (double)c->nxb * (double)c->nyb * (double)c->nzb;
+  const int64_t bs = c->nnb;
+  const LineSub xlines{e.my, c->ny, e.mz, c->nz}, ylines{0, c->nyb, e.mz, c->nz};
+  OpEmbed<R> emb{e, dens0, dens1, wb, bs, 1};
+  OpMasked<C> yfwd{wb, (int64_t)c->nxb, c->nyb, e.my, e.my + c->ny, bs};
+  OpCopy<C> inplace{wb, wb, bs};
+  OpVk<R> vkop{wb, VkOf<R>::get(c), (int64_t)c->nxb * c->nyb, e.mz, e.mz + c->nz, bs};
+  OpCrop<R> crop{e, wb, vh0, vh1, 1.0 / nbd, nbd, bs, 1};
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 2, -1, emb, &xlines)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, 2, -1, yfwd, &ylines)));
+  OPAW_CHECK((launch_axis<C, 2>(c, c->fftb.ax[2], d, 2, 0, vkop)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, 2, +1, inplace, &ylines)));
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, 2, +1, crop, &xlines)));
+  return OPAW_OK;
+}
+template int hartree_pair_t<float>(opaw_ctx *, const double *, const double *, double *, double *);
+template int hartree_pair_t<double>(opaw_ctx *, const double *, const double *, double *, double *);
 
 int hartree(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1) {
   return hartree_t<double>(c, dens0, dens1, vh0, vh1);
