@@ -37,10 +37,11 @@ DT = 0.05
 METRIC = "RK4 orbital-steps/s (mixed precision, stage-wise rebuild)"
 UNIT = "orbital-steps/s"
 # k_mix_dense on the 96^3 / 40-atom workload with 128 orbitals per set: DRAM
-# bytes (read + write) of the five launches of one step (start, RK4 stages
-# 1-4) measured by ncu, averaged per launch, and their algorithmic bytes
-DENSE_TRAFFIC_128 = (3907100928 + 7840902144 + 9668066304 + 9667104000 + 5704336896) / 5
-DENSE_ALG_128 = (3.951e9 + 7.884e9 + 9.696e9 + 9.696e9 + 5.749e9) / 5
+# bytes (read + write) of the four launches of one step (start, RK4 stages
+# 1-3; the last stage's grid part runs inside k_mix_final) measured by ncu,
+# averaged per launch, and their algorithmic bytes
+DENSE_TRAFFIC_128 = (3907100928 + 7840902144 + 9668066304 + 9667104000) / 4
+DENSE_ALG_128 = (3.951e9 + 7.884e9 + 9.696e9 + 9.696e9) / 4
 CPU_SAMPLE_NORB = 2
 
 
@@ -426,7 +427,7 @@ def main():
             "bound": "hbm", "achieved": kt_bytes / (kt_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
             "frac": kt_bytes / (kt_ms / 1e3) / 1e9 / peak, "peak_kind": peak_kind,
             "traffic": DENSE_TRAFFIC_128 * norb / 128,
-            "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the five launches of one step at "
+            "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the four launches of one step at "
                             "128 orbitals, per launch (algorithmic: "
                             f"{DENSE_ALG_128 * norb / 128:.4g}; profiles/dram_traffic_k_mix_dense_96cube_128orb.md)",
             "alg_bytes_per_launch": kt_bytes / max(kt_n, 1), "avg_launch_ms": kt_ms / max(kt_n, 1),

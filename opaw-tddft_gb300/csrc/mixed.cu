@@ -756,10 +756,15 @@ __global__ void k_mix_fac_init(double *__restrict__ fac, float *__restrict__ fac
 // values: x' = f0 x + h6 ks0, y' = df x + f1 y + h6 ksd (float-float), with
 // the norm partials and the dipole partials (tddft_plot.f90:40-57) of x', y':
 // per orbital sum r |x'|^2 and sum r (2 Re conj(x') y' + |y'|^2)
-__global__ void k_mix_final(float2 *__restrict__ xh, float2 *__restrict__ xl, float2 *__restrict__ yh,
+// With u0 non-null it also finishes the last RK4 stage first (the fused pass
+// of that stage has no sum over orbitals): sum k = ks + k4, k4 = -i u' + B
+// with the box terms B of both sets at the union points.
+__global__ void __launch_bounds__(256, 3) k_mix_final(float2 *__restrict__ xh, float2 *__restrict__ xl, float2 *__restrict__ yh,
                             float2 *__restrict__ yl, const float2 *__restrict__ ks0, const float2 *__restrict__ ksd,
                             const double *__restrict__ fac, double h6, int64_t nn, int nx, int ny, int nz, float dx,
-                            float dy, float dz, double *__restrict__ npart, double *__restrict__ dpart) {
+                            float dy, float dz, double *__restrict__ npart, double *__restrict__ dpart,
+                            const float2 *__restrict__ u0, const float2 *__restrict__ ud, const int *__restrict__ uidx,
+                            const float2 *__restrict__ BG, int nunion) {
   __shared__ double sh[8];
   const int o = blockIdx.y;
   const FF f0 = ff_of(fac[3 * o]), f1 = ff_of(fac[3 * o + 1]), df = ff_of(fac[3 * o + 2]), hh = ff_of(h6);
@@ -773,16 +778,32 @@ __global__ void k_mix_final(float2 *__restrict__ xh, float2 *__restrict__ xl, fl
   const int sx = (int)(stride % nx), sy = (int)((stride / nx) % ny), sz = (int)(stride / ((int64_t)nx * ny));
   // the six operands of the next point are loaded while this one is combined
   const int64_t ob = (int64_t)o * nn;
-  float2 na = make_float2(0.f, 0.f), nal = na, nb = na, nbl = na, ns0 = na, nsd = na;
+  float2 na = make_float2(0.f, 0.f), nal = na, nb = na, nbl = na, ns0 = na, nsd = na, np0 = na, npd = na;
+  int nu = -1;
   if (g0 < nn) {
     na = xh[ob + g0], nal = xl[ob + g0], nb = yh[ob + g0], nbl = yl[ob + g0], ns0 = ks0[ob + g0], nsd = ksd[ob + g0];
+    if (u0) np0 = u0[ob + g0], npd = ud[ob + g0], nu = uidx[g0];
   }
+  const int64_t bo = (int64_t)o * nunion, su = (int64_t)gridDim.y * nunion;
   for (int64_t g = g0; g < nn; g += stride) {
     const int64_t i = ob + g;
-    const float2 a = na, al = nal, b = nb, bl = nbl, s0 = ns0, sd = nsd;
+    const float2 a = na, al = nal, b = nb, bl = nbl;
+    float2 s0 = ns0, sd = nsd;
+    const float2 p0 = np0, pd = npd;
+    const int u = nu;
+    float2 B0 = make_float2(0.f, 0.f), B1 = B0;
+    if (u >= 0) {
+      B0 = BG[bo + u];
+      B1 = BG[su + bo + u];
+    }
     if (g + stride < nn) {
       const int64_t k = i + stride;
       na = xh[k], nal = xl[k], nb = yh[k], nbl = yl[k], ns0 = ks0[k], nsd = ksd[k];
+      if (u0) np0 = u0[k], npd = ud[k], nu = uidx[g + stride];
+    }
+    if (u0) {  // k4 = -i u' + B, sum k = ks + 1 k4 (the w = 1 update of the stage pass)
+      s0 = make_float2((p0.y + B0.x) + s0.x, (-p0.x + B0.y) + s0.y);
+      sd = make_float2((pd.y + B1.x) + sd.x, (-pd.x + B1.y) + sd.y);
     }
     const FF Xx{a.x, al.x}, Xy{a.y, al.y}, Yx{b.x, bl.x}, Yy{b.y, bl.y};
     const FF nxx = ff_add(ff_mul(f0, Xx), ff_mulf(hh, s0.x));
@@ -1003,7 +1024,8 @@ static void mix_swap(Mix &m, size_t sv) {
 }
 
 // the fused grid pass (start of a step: stage = 0)
-static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, float w, float dts) {
+static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, float w, float dts,
+                     bool box_only = false) {
   FusedArgs f;
   f.u0 = m.u0;
   f.ud = m.ud;
@@ -1039,6 +1061,7 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
                                              m.cab, m.cg, stage, write_t, m.bg);
     MIX_LAUNCHED();
   }
+  if (box_only) return OPAW_OK;  // the last stage's grid part runs inside k_mix_final
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (c->ktime_on) {  // live timing (opaw_ktime_begin): events from a reused pool
     while ((int)c->kev.size() < c->kev_used + 2) {
@@ -1121,7 +1144,7 @@ static int mix_stage(opaw_ctx *c, Mix &m, int st, float w, double dts) {
       mix_swap(m, sv);
     }
   }
-  return mix_fused(c, m, 1, st == 0, write_t, w, (float)dts);
+  return mix_fused(c, m, 1, st == 0, write_t, w, (float)dts, st == 3);
 }
 
 // the rest of the rebuild (ncpaw_make_hamiltonian.f90:119-129) from <p~|t>
@@ -1195,8 +1218,10 @@ int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev
       OPAW_CHECK(mix_stage(c, m, st, wts[st], dts[st]));
       if (st < 3) OPAW_CHECK(mix_potentials(c, m));  // rk4.f90:53-55
     }
+    // the last stage's grid part (k4 and the complete sum k) and the final combination
     k_mix_final<<<gn, 256, 0, c->stream>>>(m.pf0, m.xl, m.pfd, m.yl, m.ks0, m.ksd, m.nfac, dt / 6.0, c->nn, c->nx,
-                                           c->ny, c->nz, (float)c->dx, (float)c->dy, (float)c->dz, m.npart1, m.dpart);
+                                           c->ny, c->nz, (float)c->dx, (float)c->dy, (float)c->dz, m.npart1, m.dpart,
+                                           m.u0, m.ud, c->d_uidx, m.bg, c->ns > 0 ? c->nunion : 0);
     MIX_LAUNCHED();
     k_mix_nfac<<<grid1(norb, 128), 128, 0, c->stream>>>(m.npart0, m.npart1, kMixNormBlocks, norb, m.nfac, m.facf);
     MIX_LAUNCHED();
