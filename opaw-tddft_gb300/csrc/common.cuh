@@ -300,6 +300,9 @@ __global__ void k_coef_dij2(const double2 *__restrict__ cin, const double2 *__re
 template <typename R>
 int h_fft(opaw_ctx *c, const R *vks, const typename Tr<R>::C *pin, typename Tr<R>::C *hp, int norb,
           const typename Tr<R>::C *t0, const R *dv);
+template <typename R>
+int h_fft2(opaw_ctx *c, const R *v0, const R *v1, const typename Tr<R>::C *t0, const typename Tr<R>::C *td,
+           typename Tr<R>::C *u0, typename Tr<R>::C *ud, const R *dv, int norb, int *ran);
 // <p~|pin> and <p~1|pin> in one pass over the boxes
 template <typename R>
 int gather2(opaw_ctx *c, const typename Tr<R>::C *pin, int norb, double2 *c0, double2 *c1);

@@ -589,6 +589,70 @@ template <typename R> struct OpHFinal {
   __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
 
+// Both orbital sets of a stage in one batch, interleaved: batch entry
+// b = 2 o + set.  The forward plane pass reads t (set 0) or t_d (set 1) of
+// orbital o; the epilogue of set 1 reads t_0 of the same orbital and plane
+// that the set-0 CTA one row of CTAs earlier has just read, so that read is
+// served by L2.
+template <typename C> struct OpCopy2 {
+  const C *src0, *src1;
+  C *dst;
+  int64_t nn;
+  static constexpr bool kMid = false;
+  __device__ const C *raw(int b) const { return ((b & 1) ? src1 : src0) + (int64_t)(b >> 1) * nn; }
+  __device__ C load(int b, int64_t g) const { return raw(b)[g]; }
+  __device__ void store(int b, int64_t g, C v) const { dst[b * nn + g] = v; }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ C mid(int, int64_t, double, int, C v) const { return v; }
+};
+
+template <typename R> struct OpHFinal2 {
+  typedef typename Tr<R>::C C;
+  const C *src;        // the transformed batch, 2 norb entries
+  const C *p0, *pd;    // t_0, t_d
+  const R *v0, *v1;    // v_ks of set 0, of set 1
+  C *h0, *hd;          // outputs u'_0, u'_d
+  const R *dv;         // v_1 - v_0
+  int64_t nn;
+  static constexpr bool kMid = false;
+  __device__ C load(int b, int64_t g) const { return src[b * nn + g]; }
+  __device__ const C *raw(int b) const { return src + b * nn; }
+  struct Pre {
+    C p, t;
+    R w, d;
+  };
+  __device__ Pre pre(int b, int64_t g) const {
+    Pre q;
+    const int64_t i = (int64_t)(b >> 1) * nn + g;
+    if (b & 1) {
+      q.p = pd[i];
+      q.w = v1[g];
+      q.t = p0[i];
+      q.d = dv[g];
+    } else {
+      q.p = p0[i];
+      q.w = v0[g];
+    }
+    return q;
+  }
+  __device__ void fin(int b, int64_t g, C v, const Pre &q) const {
+    C r;
+    r.x = v.x + q.p.x * q.w;
+    r.y = v.y + q.p.y * q.w;
+    const int64_t i = (int64_t)(b >> 1) * nn + g;
+    if (b & 1) {
+      r.x += q.t.x * q.d;
+      r.y += q.t.y * q.d;
+      hd[i] = r;
+    } else {
+      h0[i] = r;
+    }
+  }
+  __device__ void store(int b, int64_t g, C v) const { fin(b, g, v, pre(b, g)); }
+  __device__ double line(int64_t) const { return 0.0; }
+  __device__ C mid(int, int64_t, double, int, C v) const { return v; }
+};
+
 template <typename R> struct VksOf;
 template <> struct VksOf<float> {
   static const float *get(const opaw_ctx *c, int set) { return c->d_vks_f[set]; }
@@ -709,6 +773,30 @@ int h_fft(opaw_ctx *c, const R *vks, const typename Tr<R>::C *pin, typename Tr<R
   return OPAW_OK;
 }
 
+// the grid part of H of both sets of a stage (set 1 as the difference form
+// H' t_d + dv t_0) in one interleaved batch of 2 norb; returns 0 when the
+// grid has no plane kernel (the caller then runs h_fft per set)
+template <typename R>
+int h_fft2(opaw_ctx *c, const R *v0, const R *v1, const typename Tr<R>::C *t0, const typename Tr<R>::C *td,
+           typename Tr<R>::C *u0, typename Tr<R>::C *ud, const R *dv, int norb, int *ran) {
+  typedef typename Tr<R>::C C;
+  *ran = 0;
+  if (norb <= 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->work[0], sizeof(C) * (size_t)c->nn * 2 * norb));
+  C *w = (C *)c->work[0].p;
+  Dims3 d{c->nx, c->ny, c->nz};
+  OpCopy2<C> fwd{t0, td, w, c->nn};
+  OpHFinal2<R> fin{w, t0, td, v0, v1, u0, ud, dv, c->nn};
+  int st;
+  if (!launch_xy_if<C>(c, c->fft, 2 * norb, -1, fwd, &st)) return OPAW_OK;
+  OPAW_CHECK(st);
+  OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, 2 * norb, 0, make_kin<R>(c, w))));
+  launch_xy_if<C>(c, c->fft, 2 * norb, +1, fin, &st);
+  OPAW_CHECK(st);
+  *ran = 1;
+  return OPAW_OK;
+}
+
 // sigma table for sn_phi's exponent n: cached for n = -1, -1/2, 1/2, 1
 static int sigma_table(opaw_ctx *c, double n, const double **out) {
   int slot;
@@ -766,6 +854,8 @@ int shs_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>
   template int h_apply_ex<R>(opaw_ctx *, const R *, const double *, const Tr<R>::C *, Tr<R>::C *, int,  \
                              const double2 *, const Tr<R>::C *, const R *, const double2 *, const double *); \
   template int h_fft<R>(opaw_ctx *, const R *, const Tr<R>::C *, Tr<R>::C *, int, const Tr<R>::C *, const R *); \
+  template int h_fft2<R>(opaw_ctx *, const R *, const R *, const Tr<R>::C *, const Tr<R>::C *, Tr<R>::C *,         \
+                         Tr<R>::C *, const R *, int, int *);                                                        \
   template int gather2<R>(opaw_ctx *, const Tr<R>::C *, int, double2 *, double2 *);
 OPAW_INST(float)
 OPAW_INST(double)

@@ -1118,8 +1118,12 @@ static int mix_stage(opaw_ctx *c, Mix &m, int st, float w, double dts) {
   const int norb = m.norb;
   const size_t sv = (size_t)c->ns * norb;
   const int write_t = st < 3;
-  OPAW_CHECK(h_fft<float>(c, c->d_vks_f[0], m.t0, m.u0, norb, nullptr, nullptr));
-  OPAW_CHECK(h_fft<float>(c, c->d_vks_f[1], m.td, m.ud, norb, m.t0, m.dvf));
+  int both;
+  OPAW_CHECK(h_fft2<float>(c, c->d_vks_f[0], c->d_vks_f[1], m.t0, m.td, m.u0, m.ud, m.dvf, norb, &both));
+  if (!both) {
+    OPAW_CHECK(h_fft<float>(c, c->d_vks_f[0], m.t0, m.u0, norb, nullptr, nullptr));
+    OPAW_CHECK(h_fft<float>(c, c->d_vks_f[1], m.td, m.ud, norb, m.t0, m.dvf));
+  }
   if (c->ns > 0) {
     OPAW_CHECK(gather2<float>(c, m.u0, norb, m.G, m.G + sv));
     OPAW_CHECK(gather2<float>(c, m.ud, norb, m.G + 2 * sv, m.G + 3 * sv));
