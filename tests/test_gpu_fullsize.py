@@ -63,3 +63,28 @@ def test_hermiticity_fullsize(big):
         lhs = np.vdot(a, c.shs(b, 0, dt))
         rhs = np.vdot(c.shs(a, 0, dt), b)
         assert abs(lhs - rhs) / abs(lhs) < (1e-12 if dt == pkg.OPAW_C128 else 1e-5)
+
+
+def test_tddft_step_fullsize(big):
+    """One TDDFT step (rebuild, RK4 with stage-wise rebuilds, dipole) of both
+    sets at the benchmark's size against the oracle, FP64 and mixed: the
+    kernels of the benchmark's step (plane passes over both sets, tiled box
+    terms, pipelined gathers, the final combination with the last stage)."""
+    s, psi, o, c = big
+    g = 1e-3
+    pp = o.excite(psi, 1, g)
+    p1, pp1, dref = o.tddft_steps(psi, pp, 1, 0.05, g)
+    c.upload(0, psi)
+    c.excite(1, g)
+    d64 = c.tddft_steps(1, 0.05, g, pkg.PREC_FP64)
+    assert rel(c.download(0, 2).reshape(p1.shape), p1) < 1e-10
+    assert rel(c.download(1, 2).reshape(pp1.shape), pp1) < 1e-10
+    assert np.allclose(d64, dref, rtol=1e-8, atol=1e-9 * np.abs(dref).max())
+    c.upload(0, psi)
+    c.excite(1, g)
+    dmx = c.tddft_steps(1, 0.05, g, pkg.PREC_MIXED)
+    q0 = c.download(0, 2).reshape(p1.shape)
+    q1 = c.download(1, 2).reshape(pp1.shape)
+    assert rel(q0, p1) < 1e-5
+    assert rel(q1 - q0, pp1 - p1) < 1e-5  # the kicked set's difference keeps FP32 relative precision
+    assert np.abs(dmx - dref).max() < 1e-6 * np.abs(dref).max()
