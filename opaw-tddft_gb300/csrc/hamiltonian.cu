@@ -201,12 +201,15 @@ __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) 
   R v[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) v[k] = 0;
-  C zn[U];  // the orbital at the lane's points of the next chunk
+  // software pipeline: grid indices two chunks ahead, orbital values one ahead
+  C zn[U];   // the orbital at the lane's points of the next chunk
+  int gn[U]; // grid indices of the lane's points of the chunk after it (-1: none)
 #pragma unroll
   for (int k = 0; k < U; k++) {
-    const int b = b0 + lane + 32 * k;
+    const int b = b0 + lane + 32 * k, b2 = b + kG2Chunk;
     zn[k].x = zn[k].y = (R)0;
     if (live && b < b1) zn[k] = po[bg[b]];
+    gn[k] = (live && b2 < b1) ? bg[b2] : -1;
   }
   if (b0 < b1) g2_stage_rows<R, MSMAX, kG2Chunk, NT>(&sp[0][0][0][0], Pa, Qa, m, nbox, b0, b1);
   int buf = 0;
@@ -220,9 +223,10 @@ __global__ void __launch_bounds__(32 * kG2Warps, (sizeof(R) == 4 && MSMAX <= 8) 
     if (c1 < b1) {
 #pragma unroll
       for (int k = 0; k < U; k++) {
-        const int b = c1 + lane + 32 * k;
         zn[k].x = zn[k].y = (R)0;
-        if (live && b < b1) zn[k] = po[bg[b]];
+        if (gn[k] >= 0) zn[k] = po[gn[k]];
+        const int b2 = c1 + kG2Chunk + lane + 32 * k;
+        gn[k] = (live && b2 < b1) ? bg[b2] : -1;
       }
       g2_stage_rows<R, MSMAX, kG2Chunk, NT>(&sp[buf ^ 1][0][0][0], Pa, Qa, m, nbox, c1, b1);
     }
