@@ -40,7 +40,7 @@ UNIT = "orbital-steps/s"
 # bytes (read + write) of the four launches of one step (start, RK4 stages
 # 1-3; the last stage's grid part runs inside k_mix_final) measured by ncu,
 # averaged per launch, and their algorithmic bytes
-DENSE_TRAFFIC_128 = (3907100928 + 7840902144 + 9668066304 + 9667104000) / 4
+DENSE_TRAFFIC_128 = (3906272000 + 7843464192 + 9668494080 + 9670806272) / 4
 DENSE_ALG_128 = (3.951e9 + 7.884e9 + 9.696e9 + 9.696e9) / 4
 CPU_SAMPLE_NORB = 2
 
