@@ -358,11 +358,10 @@ __global__ void k_mc_t(Ovl v, const double2 *__restrict__ pre, const double2 *__
 // and the raw densities of t' (tddft_dens.f90:56-77): 2 sum |t0|^2 and the
 // difference 2 sum (2 Re conj(t0) td + |td|^2), orbital partial sums of 16 in
 // FP32 added with a compensated FP32 sum (DensAcc).  At the start of a step
-// (stage = 0) it only forms t = pf + P1 c3 and the densities.  Two kernels
-// split the grid: the points
-// outside every projector box (no box terms, two orbitals' loads in flight)
-// and the union points (projector values in registers, coefficients
-// through L1); together they write every point once.
+// (stage = 0) it only forms t = pf + P1 c3 and the densities.  The box
+// terms at the union points come precomputed from k_mix_boxcoef_t through
+// the union index; two orbitals' loads are in flight per thread.  The last
+// stage (no t', no densities) runs inside k_mix_final instead.
 struct FusedArgs {
   const float2 *u0, *ud, *pf0, *pfd;  // pf: the hi arrays x, y of the state, restored on read
   const float *facf;                  // per orbital f0, f1, df: psi = f0 x, delta = df x + f1 y
