@@ -747,6 +747,50 @@ template <typename C, int N, int NLINES, int LSL, int LSE, int NT, int S> struct
   }
 };
 
+// stages [S, END) of one axis (see XyStages)
+template <typename C, int N, int NLINES, int LSL, int LSE, int NT, int S, int END> struct XyStagesTo {
+  static __device__ __forceinline__ void run(C *buf, const C *tw, int sign, int tid = threadIdx.x) {
+    if constexpr (S < END) {
+      xy_stage<C, N, NLINES, LSL, LSE, NT, S>(buf, tw, sign, tid);
+      XyStagesTo<C, N, NLINES, LSL, LSE, NT, S + 1, END>::run(buf, tw, sign, tid);
+    }
+  }
+};
+
+// The last x stage of an inverse plane transform with the epilogue of Op
+// applied on the way out: outputs go straight to global memory (no write-back
+// to shared memory, no barrier after it).  Lanes take consecutive butterflies
+// of a row, so the shared-memory reads and, for a first stage radix that
+// leaves P > 1, the global accesses run along x.  The epilogue operands of a
+// butterfly's outputs are loaded before its shared-memory reads.
+template <typename C, int NX, int NY, int LX, int NT, class Op>
+__device__ __forceinline__ void xy_last_x_epi(const C *__restrict__ pl, const C *tw, int sign, const Op &op, int b,
+                                              int64_t base) {
+  constexpr int S = ct_nstage(NX) - 1;
+  constexpr int R = ct_radix(NX, S), P = ct_pre(NX, S), M = NX / R;
+  constexpr int TOT = NY * M, TSTEP = NX / (P * R);
+#pragma unroll 1
+  for (int bf = threadIdx.x; bf < TOT; bf += NT) {
+    const int i = bf % M, row = bf / M;
+    const int kk = i % P;
+    const int j = (i - kk) * R + kk;
+    const int64_t g0 = base + (int64_t)row * NX + j;
+    decltype(op.pre(0, int64_t(0))) pr[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) pr[q] = op.pre(b, g0 + q * P);
+    C u[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) u[q] = pl[row * LX + i + q * M];
+    if (P > 1) {
+#pragma unroll
+      for (int q = 1; q < R; q++) u[q] = cmul(u[q], twid(tw, q * kk * TSTEP, sign));
+    }
+    Butterfly<C, R>::run(u, tw, NX, sign);
+#pragma unroll
+    for (int q = 0; q < R; q++) op.fin(b, g0 + q * P, u[q], pr[q]);
+  }
+}
+
 template <typename C, int NX, int NY, class Op>
 __global__ void __launch_bounds__(384, 2)
     k_fft_xy(int sign, const C *__restrict__ twx, const C *__restrict__ twy, Op op, int ahead) {
@@ -801,36 +845,24 @@ __global__ void __launch_bounds__(384, 2)
     }
   }
   __syncthreads();
-  if (sign < 0) {
+  if constexpr (HasPre<Op>::value) {
+    // y lines, then x lines with the epilogue riding on the last x stage
+    // (either direction: the two axes' transforms commute)
+    XyStages<C, NY, NX, 1, LX, NT, 0>::run(pl, ty, sign);
+    XyStagesTo<C, NX, NY, LX, 1, NT, 0, ct_nstage(NX) - 1>::run(pl, tx, sign);
+    xy_last_x_epi<C, NX, NY, LX, NT>(pl, tx, sign, op, b, base);
+    return;
+  } else if (sign < 0) {
     XyStages<C, NX, NY, LX, 1, NT, 0>::run(pl, tx, sign);   // x lines (rows)
     XyStages<C, NY, NX, 1, LX, NT, 0>::run(pl, ty, sign);   // y lines (columns)
   } else {
     XyStages<C, NY, NX, 1, LX, NT, 0>::run(pl, ty, sign);
     XyStages<C, NX, NY, LX, 1, NT, 0>::run(pl, tx, sign);
   }
-  if constexpr (HasPre<Op>::value) {
-    for (int e0 = threadIdx.x; e0 < TOT; e0 += NT * CH) {
-      decltype(op.pre(0, int64_t(0))) q[CH];
-#pragma unroll
-      for (int j = 0; j < CH; j++) {
-        const int e = e0 + j * NT;
-        if (e < TOT) q[j] = op.pre(b, base + e);
-      }
-#pragma unroll
-      for (int j = 0; j < CH; j++) {
-        const int e = e0 + j * NT;
-        if (e < TOT) {
-          const int y = e / NX, x = e - y * NX;
-          op.fin(b, base + e, pl[y * LX + x], q[j]);
-        }
-      }
-    }
-  } else {
 #pragma unroll 4
-    for (int e = threadIdx.x; e < TOT; e += NT) {
-      const int y = e / NX, x = e - y * NX;
-      op.store(b, base + e, pl[y * LX + x]);
-    }
+  for (int e = threadIdx.x; e < TOT; e += NT) {
+    const int y = e / NX, x = e - y * NX;
+    op.store(b, base + e, pl[y * LX + x]);
   }
 }
 
