@@ -1,7 +1,7 @@
 /*
  * opaw_oracle.c — CPU FP64 restatement of the OPAW-TDDFT propagation path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU library is
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the GPU library is
  * compared against; it is never linked into, loaded by, or called from the
  * product library.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline leg may load it.

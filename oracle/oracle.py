@@ -1,6 +1,6 @@
 """ctypes front end of the FP64 CPU oracle (oracle/opaw_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: the checker the GPU library is compared against.
+TEST INFRASTRUCTURE ONLY: the oracle the GPU library is compared against.
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
 """
 from __future__ import annotations

@@ -196,7 +196,7 @@ def test_launch_counter_counts_kernels():
 def test_mixed_dipole_signal_vs_fp64():
     """Mixed-precision d_dip(t) against the FP64 path over 6 steps: the
     difference formulation keeps the error near FP32 rounding of the signal
-    (the benchmark spec's bound is 1e-6 relative)."""
+    (the target bound is 1e-6 relative)."""
     s, psi, o, c = make("spec", norb=4)
     g = 1e-3
     c.upload(0, psi)
