@@ -298,6 +298,7 @@ def run_reference(args):
         return 0
     import __graft_entry__ as ge
 
+    ge.build_oracle()  # current already when build() ran
     ge.load_package()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
@@ -357,7 +358,9 @@ def main():
     dist = init_dist(world)
     import __graft_entry__ as ge
 
-    ge.build()
+    if rank == 0:  # one rank compiles (or finds the build current); the others wait for it
+        ge.build()
+    barrier(dist)
     pkg = ge.load_package()
     from opaw_tddft_gb300 import synthetic
 
