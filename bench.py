@@ -443,7 +443,7 @@ def main():
 
     e2e = None
     if not args.no_e2e:
-        nh = min(args.steps, 3)
+        nh = min(args.steps, 5)
         a = torch.empty((norb, s.nn), dtype=torch.complex128, pin_memory=True).numpy()
         b = torch.empty((norb, s.nn), dtype=torch.complex128, pin_memory=True).numpy()
         a[:] = psi0
@@ -453,8 +453,11 @@ def main():
         ctx.tddft_steps_host(a, b, 1, DT, GAMMA, pkg.PREC_MIXED)  # warm
         barrier(dist)
         t = time.perf_counter()
+        calls = []
         for _ in range(nh):
+            tc = time.perf_counter()
             ctx.tddft_steps_host(a, b, 1, DT, GAMMA, pkg.PREC_MIXED)
+            calls.append(1e3 * (time.perf_counter() - tc))
         el = max_over_ranks(dist, time.perf_counter() - t)
         # the copy rates inside that call: one set up and one set down
         nbytes = norb * s.nn * 16
@@ -470,7 +473,8 @@ def main():
                "h2d_gbs": nbytes / t_up / 1e9, "d2h_gbs": nbytes / t_dn / 1e9,
                "h2d_bytes_per_step": int(2 * norb * s.nn * 16),
                "d2h_bytes_per_step": int(2 * norb * s.nn * 16 + 3 * 8),
-               "api": "opaw_tddft_steps_host (psi, psi_pert host arrays in/out each step)", "steps": nh}
+               "api": "opaw_tddft_steps_host (psi, psi_pert host arrays in/out each step)", "steps": nh,
+               "call_ms": [round(x, 2) for x in calls]}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
