@@ -91,3 +91,31 @@ def test_start_from_wf_bar(tmp_path):
     assert ("excite", 1, 1e-3) in c.calls
     with pytest.raises(ValueError):
         driver.opaw_tddft(FakeContext(12), nt=2, dt=0.05, gamma=1e-3, workdir=tmp_path / "x")
+
+
+@pytest.mark.gpu
+def test_driver_on_device_matches_straight_run(tmp_path):
+    """FP64: 4 steps with a checkpoint every 2, then a restarted run to step 6,
+    give the d_dip series of one straight 6-step call from the same state."""
+    import opaw_tddft_gb300 as pkg
+    from opaw_tddft_gb300 import synthetic
+
+    s = synthetic.small_system("tiny", norb=3)
+    psi = synthetic.orbitals(s, 3, seed=5).reshape(3, -1)
+    c = pkg.Context(s)
+    c.upload(0, psi)
+    c.excite(1, 1e-3)
+    ref = c.tddft_steps(6, 0.05, 1e-3, pkg.PREC_FP64)
+    c.close()
+    c = pkg.Context(s)
+    _, d1 = driver.opaw_tddft(c, nt=4, dt=0.05, gamma=1e-3, workdir=tmp_path, psi0=psi, n_restart=2,
+                              precision=pkg.PREC_FP64)
+    c.close()
+    c = pkg.Context(s)
+    it0, d2 = driver.opaw_tddft(c, nt=6, dt=0.05, gamma=1e-3, workdir=tmp_path, n_restart=2,
+                                precision=pkg.PREC_FP64)
+    c.close()
+    assert it0 == 5
+    assert np.array_equal(np.concatenate([d1, d2]), ref)
+    cont = dipfile.read_series(tmp_path / "d_dip_cont.dat")
+    assert cont.shape == (6, 4) and np.allclose(cont[:, 1:], ref, rtol=1e-7)
