@@ -123,3 +123,29 @@ def test_scf_self_consistent():
     c.rebuild(0, pkg.PREC_FP64)
     assert rel(c.get_density(0), rho0) < 1e-4
     c.close()
+
+
+def test_lowest_states_against_oracle():
+    """The device eigensolver's eigenpairs checked with the oracle's operator:
+    the Rayleigh-Ritz eigenvalues of S^-1/2 H S^-1/2 (oracle shs) on the
+    returned orbitals equal the returned eigenvalues within 1e-6 Ha, and the
+    oracle's residuals |shs x_i - w_i x_i| stay at the solver's tolerance."""
+    import oracle as orc
+
+    s = synthetic.small_system("spec", norb=4)
+    c = pkg.Context(s)
+    c.set_vks(0, s.vks0)
+    c.set_dij(0, s.dij_init)
+    w, psi, res = groundstate.lowest_states(c, synthetic.orbitals(s, 4, seed=8).reshape(4, -1), n_iter=80, tol=1e-5)
+    c.close()
+    o = orc.Oracle(s)
+    o.set_vks(0, s.vks0)
+    o.set_dij(0, s.dij_init)
+    X = np.asarray(psi).reshape(4, -1)
+    HX = np.asarray(o.shs(X)).reshape(4, -1)
+    Hs = X.conj() @ HX.T * s.dv
+    assert np.abs(Hs - Hs.conj().T).max() < 1e-9 * np.abs(Hs).max()
+    ev = np.linalg.eigvalsh(0.5 * (Hs + Hs.conj().T))
+    assert np.abs(ev - np.sort(w)).max() < 1e-6, (ev, w)
+    r = np.sqrt((np.abs(HX - w[:, None] * X) ** 2).sum(axis=1) * s.dv)
+    assert r.max() < 1e-4, r
