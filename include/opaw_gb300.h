@@ -145,6 +145,13 @@ int opaw_shs_apply_dev(opaw_ctx *ctx, int set, int dtype, const void *pin, void 
  * complex128 host output, which = 0 raw p~, 1 orthogonalised p1 */
 int opaw_proj_dev(opaw_ctx *ctx, int which, int dtype, const void *pin, int norb, double *ca);
 
+/* Teter-Payne-Allan kinetic preconditioner of the ground-state eigensolver
+ * (no reference counterpart: the reference's Chebyshev-filtered SCF,
+ * chebyr_m.f90, uses none): out_b = F^-1 [K(|k|^2/2 / ekin[b]) F pin_b] with
+ * K(x) = (27+18x+12x^2+8x^3)/(27+18x+12x^2+8x^3+16x^4), ekin a host array of
+ * norb positive kinetic energies; asynchronous on the context's stream
+ * (the host array is consumed before the call returns); out may equal pin */
+int opaw_precond_kinetic_dev(opaw_ctx *ctx, int dtype, const void *pin, const double *ekin, void *out, int norb);
 /* fft3d_forward / fft3d_backward (lib/library_fftw_v3.f90:56-83): in-place
  * unnormalised 3D DFT of norb device arrays, sign -1 forward, +1 backward */
 int opaw_fft3d_dev(opaw_ctx *ctx, int dtype, void *data, int norb, int sign);
@@ -195,22 +202,23 @@ int opaw_rconv(int n0, int n1, int n2, const double *gin, const double *bk, doub
 /* rconv for callers that cannot allocate device memory (no counterpart in
  * the reference; it exists because some callers of this library cannot call
  * cudaMalloc: a host program that fixed its device memory budget at start-up,
- * code running while a stream is captured into a CUDA graph, or a process
- * whose allocator a library must not touch).  gin, bk and gout are device
- * arrays of n0*n1*n2 doubles owned by the caller; the work runs on `stream`
- * (NULL: the legacy default stream) and the call returns after it finished.
- * No cudaMalloc, cudaFree or allocating library routine is called: the
- * scratch is a fixed file-scope device array, so
+ * or a process whose device allocator belongs to another runtime that a
+ * library must not touch).  gin, bk and gout are device arrays of n0*n1*n2
+ * doubles owned by the caller; the work runs on `stream` (NULL: the legacy
+ * default stream).  The twiddle tables are computed on the device, and the
+ * call synchronises `stream` before it returns.  No cudaMalloc, cudaFree or
+ * allocating library routine is called: the scratch is a fixed file-scope
+ * device array, so
  *   - each extent must be <= 256 with prime factors 2, 3, 5, 7 and
  *     n0*n1*n2 <= 262144 (4 MiB of complex128 scratch, plus 12 KiB of
  *     twiddles, held by every GPU that loads the library until exit);
  *     larger sizes are rejected with OPAW_ERR_ARG;
- *   - the first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress) for that device; make that first call before
- *     any stream capture;
- *   - all calls share the one scratch array: calls that overlap on the GPU
- *     (different host threads or streams) race and must not be issued
- *     concurrently. */
+ *   - the first call on a device (and the first after that device's context
+ *     changed) looks up the array's device address (cudaGetSymbolAddress);
+ *     make that first call before any stream capture;
+ *   - all calls share the one scratch array, which keeps the last call's
+ *     contents: calls that overlap on the GPU (different host threads or
+ *     streams) race and must not be issued concurrently. */
 int opaw_rconv_noalloc(int n0, int n1, int n2, const double *gin, const double *bk, double *gout, void *stream);
 /* LDA v_xc (libxc LDA_X + LDA_C_PW, vxc_libxc.f90:15-23), host arrays */
 int opaw_vxc_lda(opaw_ctx *ctx, const double *dens, double *vxc, int64_t n);
@@ -221,6 +229,33 @@ int opaw_vxc_lda(opaw_ctx *ctx, const double *dens, double *vxc, int64_t n);
 int opaw_excite(opaw_ctx *ctx, int ipol, double gamma);
 /* plot_dip (tddft_plot.f90:1-155): dip, dip_pert (3 each) and d_dip = (dip_pert-dip)/gamma */
 int opaw_dipole(opaw_ctx *ctx, double gamma, double *dip, double *dip_pert, double *d_dip);
+/* excite_psi_bar_pert (tddft_excite.f90:1-16) for nkick kicks at once: kicked
+ * set k = set 0 * exp(-i gamma[k] r_{ipol[k]}), k = 0 .. nkick-1.  The kicked
+ * sets live in set 1's storage ([kick][orbital][point]; kick 0 is what the
+ * set-1 entry points see) and are all propagated against the one unperturbed
+ * set: the reference propagates one phi_bar_pert per run (rk4.f90:25-33), and
+ * the unkicked propagation does not depend on the kick, so a run per kick
+ * repeats the same unperturbed set. */
+int opaw_excite_kicks(opaw_ctx *ctx, int nkick, const int *ipol, const double *gamma);
+/* copies kicked set `kick` (norb orbitals) to a host array */
+int opaw_kick_download(opaw_ctx *ctx, int kick, double *psi, int norb);
+/* nsteps iterations of the opaw_tddft loop body (tddft.f90:67-91) for the
+ * unperturbed set and every kicked set of opaw_excite_kicks: dip_out
+ * [nsteps][3] (the unperturbed dipole), dip_pert_out and d_dip_out
+ * [nsteps][nkick][3], d_dip of kick k = (dip'_k - dip) / gamma[k]
+ * (tddft_plot.f90:57); any output may be NULL */
+int opaw_tddft_steps_kicks(opaw_ctx *ctx, int nsteps, double dt, int precision, double *dip_out,
+                           double *dip_pert_out, double *d_dip_out);
+/* the mixed-precision form of opaw_tddft_steps_kicks for nctx contexts at
+ * once (molecules on their own grids, each with its own kicked sets): after
+ * one plain step, two steps of every context are captured once into a CUDA
+ * graph with a branch per context and the graph is replayed, so the
+ * molecules' kernels overlap and each replay is one launch.  Outputs per
+ * context i as for opaw_tddft_steps_kicks (dip_out[i], dip_pert_out[i],
+ * d_dip_out[i]; any of the arrays or entries may be NULL).  The reference
+ * runs one molecule and one kick per job (tddft.f90:1-95). */
+int opaw_ensemble_steps(opaw_ctx *const *ctx, int nctx, int nsteps, double dt, double *const *dip_out,
+                        double *const *dip_pert_out, double *const *d_dip_out);
 /* nsteps iterations of the opaw_tddft loop body (tddft.f90:67-91):
  * rebuild both sets, rk4_prop_shs (rk4.f90:1-103), plot_dip.  d_dip_out
  * receives 3*nsteps values (may be NULL). */

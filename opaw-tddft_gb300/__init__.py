@@ -103,6 +103,11 @@ SIGNATURES = {
     "opaw_tddft_steps_dip": (ct.c_int, [_P, ct.c_int, ct.c_double, ct.c_double, ct.c_int, _P, _P, _P]),
     "opaw_tddft_steps_host": (ct.c_int, [_P, _P, _P, ct.c_int, ct.c_int, ct.c_double, ct.c_double,
                                          ct.c_int, _P]),
+    "opaw_excite_kicks": (ct.c_int, [_P, ct.c_int, _P, _P]),
+    "opaw_kick_download": (ct.c_int, [_P, ct.c_int, _P, ct.c_int]),
+    "opaw_tddft_steps_kicks": (ct.c_int, [_P, ct.c_int, ct.c_double, ct.c_int, _P, _P, _P]),
+    "opaw_precond_kinetic_dev": (ct.c_int, [_P, ct.c_int, _P, _P, _P, ct.c_int]),
+    "opaw_ensemble_steps": (ct.c_int, [_P, ct.c_int, ct.c_int, ct.c_double, _P, _P, _P]),
 }
 
 _lib = None
@@ -164,6 +169,7 @@ class Context:
         )
         self._sys = st
         self._norb = [0, 0]
+        self.nkick = 1
         h = ct.c_void_p()
         _check(lib().opaw_dev_init(ct.byref(st), ct.byref(h)))
         self.h = h
@@ -210,6 +216,8 @@ class Context:
         norb = a.size // self.nn
         _check(lib().opaw_psi_upload(self.h, set_, _ptr(a), norb))
         self._norb[set_] = norb
+        if set_ == 1:
+            self.nkick = 1
 
     def download(self, set_, norb):
         out = np.empty((norb,) + self.system.shape_f, np.complex128)
@@ -277,6 +285,12 @@ class Context:
     def sn_apply_dev(self, dtype, n, pin_ptr, out_ptr, norb):
         _check(lib().opaw_sn_apply_dev(self.h, dtype, float(n), ct.c_void_p(pin_ptr), ct.c_void_p(out_ptr), norb))
 
+    def precond_kinetic_dev(self, dtype, pin_ptr, ekin, out_ptr, norb):
+        """Teter-Payne-Allan kinetic preconditioner (opaw_precond_kinetic_dev)."""
+        e = _arr(ekin, np.float64)
+        _check(lib().opaw_precond_kinetic_dev(self.h, dtype, ct.c_void_p(pin_ptr), _ptr(e), ct.c_void_p(out_ptr),
+                                              norb))
+
     def fft3d_dev(self, dtype, ptr, norb, sign):
         _check(lib().opaw_fft3d_dev(self.h, dtype, ct.c_void_p(ptr), norb, sign))
 
@@ -341,6 +355,31 @@ class Context:
     def excite(self, ipol, gamma):
         _check(lib().opaw_excite(self.h, ipol, float(gamma)))
         self._norb[1] = self._norb[0]
+        self.nkick = 1
+
+    def excite_kicks(self, ipol, gamma):
+        """Kicked sets k = psi exp(-i gamma[k] r_ipol[k]) for every (ipol, gamma)
+        pair, all propagated against the one unperturbed set."""
+        ip = _arr(np.atleast_1d(ipol), np.int32)
+        ga = _arr(np.atleast_1d(gamma), np.float64)
+        assert ip.size == ga.size
+        _check(lib().opaw_excite_kicks(self.h, int(ip.size), _ptr(ip), _ptr(ga)))
+        self._norb[1] = self._norb[0]
+        self.nkick = int(ip.size)
+
+    def kick_download(self, kick, norb):
+        out = np.empty((norb,) + self.system.shape_f, np.complex128)
+        _check(lib().opaw_kick_download(self.h, kick, _ptr(out), norb))
+        return out
+
+    def tddft_steps_kicks(self, nsteps, dt, precision=PREC_FP64):
+        """nsteps steps of every set; returns (dip [nsteps, 3],
+        dip_pert [nsteps, nkick, 3], d_dip [nsteps, nkick, 3])."""
+        n = max(nsteps, 1)
+        K = self.nkick
+        dip, dpp, dd = np.zeros((n, 3)), np.zeros((n, K, 3)), np.zeros((n, K, 3))
+        _check(lib().opaw_tddft_steps_kicks(self.h, nsteps, float(dt), precision, _ptr(dip), _ptr(dpp), _ptr(dd)))
+        return dip[:nsteps], dpp[:nsteps], dd[:nsteps]
 
     def dipole(self, gamma):
         d0 = np.zeros(3)
@@ -374,6 +413,21 @@ class Context:
         _check(lib().opaw_tddft_steps_host(self.h, _ptr(psi), _ptr(psi_pert), norb, nsteps, float(dt),
                                            float(gamma), precision, _ptr(out)))
         return out[:nsteps]
+
+
+def ensemble_steps(contexts, nsteps, dt):
+    """opaw_ensemble_steps: nsteps mixed-precision steps of every context (each
+    with its kicked sets from excite_kicks) through one replayed CUDA graph.
+    Returns per context (dip [nsteps, 3], dip_pert [nsteps, nkick, 3],
+    d_dip [nsteps, nkick, 3])."""
+    n = len(contexts)
+    outs = [(np.zeros((max(nsteps, 1), 3)), np.zeros((max(nsteps, 1), c.nkick, 3)),
+             np.zeros((max(nsteps, 1), c.nkick, 3))) for c in contexts]
+    H = (ct.c_void_p * n)(*[c.h.value for c in contexts])
+    P = [(ct.c_void_p * n)(*[o[j].ctypes.data for o in outs]) for j in range(3)]
+    _check(lib().opaw_ensemble_steps(ct.cast(H, ct.c_void_p), n, nsteps, float(dt), ct.cast(P[0], ct.c_void_p),
+                                     ct.cast(P[1], ct.c_void_p), ct.cast(P[2], ct.c_void_p)))
+    return [(a[:nsteps], b[:nsteps], d[:nsteps]) for a, b, d in outs]
 
 
 def rconv(gin, bk):

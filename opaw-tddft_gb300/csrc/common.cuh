@@ -245,9 +245,16 @@ struct opaw_ctx {
   // FFT plans
   opaw::FFT3 fft, fftb;
 
-  // resident orbitals (complex128)
+  // resident orbitals (complex128); set 1 holds nkick kicked sets of
+  // norb[1] orbitals each, [kick][orbital][point], all propagated against the
+  // one unperturbed set 0; the per-set state arrays of set 1 (d_vks[1],
+  // d_vks_f[1], d_dij[1], d_rhoij[1], d_dens[1], d_nhat[1], d_vh[1],
+  // d_vxc[1]) have room for kcap kicks, [kick][...]
   double2 *d_psi[2] = {nullptr, nullptr};
   int norb[2] = {0, 0};
+  int nkick = 1, kcap = 1;
+  double *d_kgamma = nullptr;     // [kcap] kick strengths on the device
+  std::vector<double> h_kgamma;   // [nkick] and on the host
 
   // scratch (grown on demand)
   // 0 FFT work, 1 shs intermediate, 2 Hartree source, 3 Hartree 2x box,
@@ -258,6 +265,7 @@ struct opaw_ctx {
   opaw::DeviceBuf gram, gramout; // Gram partials, small matrices
   opaw::DeviceBuf mix[16];       // buffers of the mixed-precision difference step
   opaw::DeviceBuf red;           // reductions
+  opaw::DeviceBuf pre;           // per-orbital arguments of the preconditioners
   opaw::DeviceBuf g2part;        // segment partials of the two-table gather
   double *h_red = nullptr;       // pinned host mirror of small reductions
 };
@@ -265,6 +273,11 @@ struct opaw_ctx {
 namespace opaw {
 
 int ensure(DeviceBuf &b, size_t bytes);
+// room for K kicked sets in the set-1 state arrays (ctx.cu); the contents of
+// kick 0 are kept
+int kick_capacity(opaw_ctx *c, int K);
+// the kick strengths of the context's kicked sets, to the device (ctx.cu)
+int upload_kgamma(opaw_ctx *c);
 
 inline int grid1(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
@@ -301,8 +314,13 @@ template <typename R>
 int h_fft(opaw_ctx *c, const R *vks, const typename Tr<R>::C *pin, typename Tr<R>::C *hp, int norb,
           const typename Tr<R>::C *t0, const R *dv);
 template <typename R>
-int h_fft2(opaw_ctx *c, const R *v0, const R *v1, const typename Tr<R>::C *t0, const typename Tr<R>::C *td,
-           typename Tr<R>::C *u0, typename Tr<R>::C *ud, const R *dv, int norb, int *ran);
+int h_fftk(opaw_ctx *c, const R *v0, const R *v1, const typename Tr<R>::C *t0, const typename Tr<R>::C *td,
+           typename Tr<R>::C *u0, typename Tr<R>::C *ud, const R *dv, int norb, int nkick, int *ran);
+// Teter-Payne-Allan kinetic preconditioner of norb orbitals (inv_ekin: device
+// [norb] inverse kinetic energies); out may equal pin
+template <typename R>
+int precond_kinetic(opaw_ctx *c, const typename Tr<R>::C *pin, const double *inv_ekin, typename Tr<R>::C *out,
+                    int norb);
 // <p~|pin> and <p~1|pin> in one pass over the boxes
 template <typename R>
 int gather2(opaw_ctx *c, const typename Tr<R>::C *pin, int norb, double2 *c0, double2 *c1);
@@ -317,6 +335,10 @@ template <typename R>
 int hartree_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1);
 template <typename R>
 int hartree_pair_t(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1);
+// nsrc independent sources src[b] = src + b nn in one batch of complex
+// transforms (each keeps its own relative precision): vh + b nn
+template <typename R>
+int hartree_batch_t(opaw_ctx *c, const double *src, int nsrc, double *vh);
 int rhoij_of(opaw_ctx *c, const double2 *coef, int norb, double *out);
 template <typename R> int density_raw(opaw_ctx *c, const typename Tr<R>::C *psit, int norb, double *out);
 int nhat_raw_of(opaw_ctx *c, const double *rhoij, double *out);
@@ -324,8 +346,10 @@ int sums2(opaw_ctx *c, const double *a, const double *b, double *part);
 constexpr int kRedBlocks = 1024;
 int vxc_of(opaw_ctx *c, const double *dens, const double *core, double *out);
 int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, double *out);
-// (mixed.cu) nsteps mixed-precision TDDFT steps; 9 doubles per step into dd_dev
-int mixed_steps(opaw_ctx *c, int nsteps, double dt, double gamma, double *dd_dev);
+// (mixed.cu) nsteps mixed-precision TDDFT steps of the unperturbed set and
+// the c->nkick kicked sets (strengths gamma_dev[k]); 3 + 6 nkick doubles per
+// step into dd_dev: dip, then dip'_k and d_dip_k of every kick
+int mixed_steps(opaw_ctx *c, int nsteps, double dt, const double *gamma_dev, double *dd_dev);
 // LDA potential of n points (device arrays)
 int vxc_points(opaw_ctx *c, const double *dens, double *vxc, int64_t n);
 // gout = 1/N ifft(bk fft(a)) on the context's main FFT plan; a is overwritten

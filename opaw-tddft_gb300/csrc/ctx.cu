@@ -375,6 +375,7 @@ static void destroy(opaw_ctx *c) {
                   c->d_nhat[st], c->d_vh[st], c->d_vxc[st], c->d_psi[st]};
     for (void *p : sp) cudaFree(p);
   }
+  cudaFree(c->d_kgamma);
   for (auto &b : c->work) cudaFree(b.p);
   for (auto &b : c->coef) cudaFree(b.p);
   cudaFree(c->coefr.p);
@@ -390,12 +391,53 @@ static void destroy(opaw_ctx *c) {
   for (auto &b : c->mix) cudaFree(b.p);
   for (cudaEvent_t e : c->kev) cudaEventDestroy(e);
   cudaFree(c->red.p);
+  cudaFree(c->pre.p);
   cudaFree(c->g2part.p);
   if (c->h_red) cudaFreeHost(c->h_red);
   fft3_free(c->fft);
   fft3_free(c->fftb);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+// a device array of n elements of T with room for K kicks: slot 0 keeps the
+// old contents, the new slots start at zero
+template <typename T> static int grow_kicks(T **p, size_t n, int K) {
+  T *q = nullptr;
+  OPAW_CUDA(cudaMalloc(&q, sizeof(T) * n * (size_t)K));
+  OPAW_CUDA(cudaMemset(q, 0, sizeof(T) * n * (size_t)K));
+  if (*p) OPAW_CUDA(cudaMemcpy(q, *p, sizeof(T) * n, cudaMemcpyDeviceToDevice));
+  cudaFree(*p);
+  *p = q;
+  return OPAW_OK;
+}
+
+int kick_capacity(opaw_ctx *c, int K) {
+  if (K <= c->kcap && c->d_kgamma) return OPAW_OK;
+  if (K > c->kcap) {
+    OPAW_CUDA(cudaStreamSynchronize(c->stream));
+    OPAW_CHECK(grow_kicks(&c->d_vks[1], c->nn, K));
+    OPAW_CHECK(grow_kicks(&c->d_vks_f[1], c->nn, K));
+    OPAW_CHECK(grow_kicks(&c->d_dij[1], c->nd, K));
+    OPAW_CHECK(grow_kicks(&c->d_rhoij[1], c->nd, K));
+    OPAW_CHECK(grow_kicks(&c->d_dens[1], c->nn, K));
+    OPAW_CHECK(grow_kicks(&c->d_nhat[1], c->nn, K));
+    OPAW_CHECK(grow_kicks(&c->d_vh[1], c->nn, K));
+    OPAW_CHECK(grow_kicks(&c->d_vxc[1], c->nn, K));
+    c->kcap = K;
+    cudaFree(c->d_kgamma);
+    c->d_kgamma = nullptr;
+  }
+  OPAW_CUDA(cudaMalloc(&c->d_kgamma, sizeof(double) * (size_t)c->kcap));
+  return OPAW_OK;
+}
+
+int upload_kgamma(opaw_ctx *c) {
+  OPAW_CHECK(kick_capacity(c, c->nkick));
+  OPAW_ARG((int)c->h_kgamma.size() >= c->nkick, "kick strengths missing");
+  OPAW_CUDA(cudaMemcpyAsync(c->d_kgamma, c->h_kgamma.data(), sizeof(double) * c->nkick, cudaMemcpyHostToDevice,
+                            c->stream));
+  return OPAW_OK;
 }
 
 // float twin of v_ks for the mixed-precision operators
@@ -567,12 +609,14 @@ int opaw_psi_upload(opaw_ctx *c, int set, const double *psi, int norb) {
   OPAW_CHECK(check_ctx(c));
   OPAW_CHECK(check_set(set));
   OPAW_ARG(psi && norb > 0, "psi must be non-null with norb > 0");
-  if (c->norb[set] != norb) {
+  if (c->norb[set] != norb || (set == 1 && c->nkick != 1)) {
+    OPAW_CUDA(cudaStreamSynchronize(c->stream));
     cudaFree(c->d_psi[set]);
     c->d_psi[set] = nullptr;
     OPAW_CUDA(cudaMalloc(&c->d_psi[set], sizeof(double2) * (size_t)c->nn * norb));
     c->norb[set] = norb;
   }
+  if (set == 1) c->nkick = 1;  // one kicked set, uploaded as it is
   OPAW_CUDA(cudaMemcpyAsync(c->d_psi[set], psi, sizeof(double2) * (size_t)c->nn * norb, cudaMemcpyHostToDevice,
                             c->stream));
   OPAW_CUDA(cudaStreamSynchronize(c->stream));
@@ -649,6 +693,25 @@ int opaw_h_apply_dev(opaw_ctx *c, int set, int dtype, const void *pin, void *hp,
   OPAW_ARG(pin && hp && norb >= 0, "bad buffers");
   if (dtype == OPAW_C128) return h_apply<double>(c, set, (const double2 *)pin, (double2 *)hp, norb);
   if (dtype == OPAW_C64) return h_apply<float>(c, set, (const float2 *)pin, (float2 *)hp, norb);
+  set_error("dtype must be OPAW_C128 or OPAW_C64");
+  return OPAW_ERR_ARG;
+}
+
+int opaw_precond_kinetic_dev(opaw_ctx *c, int dtype, const void *pin, const double *ekin, void *out, int norb) {
+  OPAW_CHECK(check_ctx(c));
+  OPAW_ARG(pin && out && ekin && norb >= 0, "bad buffers");
+  if (norb == 0) return OPAW_OK;
+  std::vector<double> inv(norb);
+  for (int i = 0; i < norb; i++) {
+    OPAW_ARG(ekin[i] > 0.0 && std::isfinite(ekin[i]), "kinetic energies must be positive and finite");
+    inv[i] = 1.0 / ekin[i];
+  }
+  OPAW_CHECK(ensure(c->pre, sizeof(double) * (size_t)norb));
+  OPAW_CUDA(cudaMemcpyAsync(c->pre.p, inv.data(), sizeof(double) * norb, cudaMemcpyHostToDevice, c->stream));
+  if (dtype == OPAW_C128)
+    return precond_kinetic<double>(c, (const double2 *)pin, (const double *)c->pre.p, (double2 *)out, norb);
+  if (dtype == OPAW_C64)
+    return precond_kinetic<float>(c, (const float2 *)pin, (const double *)c->pre.p, (float2 *)out, norb);
   set_error("dtype must be OPAW_C128 or OPAW_C64");
   return OPAW_ERR_ARG;
 }

@@ -548,6 +548,37 @@ template <> struct OpKin<float> {
   }
 };
 
+// Teter-Payne-Allan kinetic preconditioner (Phys. Rev. B 40, 12255 (1989))
+// as the k-space hook of the z pass: with x = (|k|^2 / 2) / Ekin_b, the
+// kinetic energy of orbital b,
+//   K(x) = (27 + 18 x + 12 x^2 + 8 x^3) / (27 + 18 x + 12 x^2 + 8 x^3 + 16 x^4),
+// applied with the 1/N of the unnormalised inverse transform folded in
+template <typename R> struct OpTPA {
+  typedef typename Tr<R>::C C;
+  C *buf;
+  int64_t bstride;
+  const R *k2x, *k2y, *k2z;
+  int nx;
+  const double *inv_ekin;  // [batch] 1 / Ekin
+  R invn;
+  static constexpr bool kMid = true;
+  __device__ C load(int b, int64_t g) const { return buf[b * bstride + g]; }
+  __device__ const C *raw(int b) const { return buf + b * bstride; }
+  __device__ void store(int b, int64_t g, C v) const { buf[b * bstride + g] = v; }
+  __device__ R line(int64_t gl) const {
+    const int t = (int)gl;
+    return k2x[t % nx] + k2y[t / nx];
+  }
+  __device__ C mid(int b, int64_t, R kxy, int z, C v) const {
+    const R x = (R)0.5 * (kxy + k2z[z]) * (R)inv_ekin[b];
+    const R num = (R)27 + x * ((R)18 + x * ((R)12 + x * (R)8));
+    const R f = num / (num + (R)16 * x * x * x * x) * invn;
+    v.x *= f;
+    v.y *= f;
+    return v;
+  }
+};
+
 // last inverse pass of h_phi: hp = F^-1[...] + pin * v_ks   (hphi.f90:21);
 // with t0/dv set it also adds the local part of (H' - H) t0 = dv * t0 (the
 // source term of the perturbation-difference propagation)
@@ -593,31 +624,37 @@ template <typename R> struct OpHFinal {
   __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
 
-// Both orbital sets of a stage in one batch, interleaved: batch entry
-// b = 2 o + set.  The forward plane pass reads t (set 0) or t_d (set 1) of
-// orbital o; the epilogue of set 1 reads t_0 of the same orbital and plane
-// that the set-0 CTA one row of CTAs earlier has just read, so that read is
-// served by L2.
-template <typename C> struct OpCopy2 {
-  const C *src0, *src1;
+// All orbital sets of a stage in one batch, interleaved: batch entry
+// b = nset o + X, X = 0 the unperturbed set, X = 1 + k the difference of kick
+// k.  The forward plane pass reads t (set 0) or t_d of kick k (X > 0) of
+// orbital o; the epilogue of a difference set reads t_0 of the same orbital
+// and plane that the set-0 CTA a few rows of CTAs earlier has just read, so
+// that read is served by L2.
+template <typename C> struct OpCopyK {
+  const C *src0, *src1;  // t_0 [orbital][point], t_d [kick][orbital][point]
   C *dst;
   int64_t nn;
+  int nset, norb;
   static constexpr bool kMid = false;
-  __device__ const C *raw(int b) const { return ((b & 1) ? src1 : src0) + (int64_t)(b >> 1) * nn; }
+  __device__ const C *raw(int b) const {
+    const int o = b / nset, X = b - o * nset;
+    return X == 0 ? src0 + (int64_t)o * nn : src1 + ((int64_t)(X - 1) * norb + o) * nn;
+  }
   __device__ C load(int b, int64_t g) const { return raw(b)[g]; }
   __device__ void store(int b, int64_t g, C v) const { dst[b * nn + g] = v; }
   __device__ double line(int64_t) const { return 0.0; }
   __device__ C mid(int, int64_t, double, int, C v) const { return v; }
 };
 
-template <typename R> struct OpHFinal2 {
+template <typename R> struct OpHFinalK {
   typedef typename Tr<R>::C C;
-  const C *src;        // the transformed batch, 2 norb entries
-  const C *p0, *pd;    // t_0, t_d
-  const R *v0, *v1;    // v_ks of set 0, of set 1
-  C *h0, *hd;          // outputs u'_0, u'_d
-  const R *dv;         // v_1 - v_0
+  const C *src;        // the transformed batch, nset norb entries
+  const C *p0, *pd;    // t_0, t_d of every kick
+  const R *v0, *v1;    // v_ks of set 0, of every kicked set [kick][point]
+  C *h0, *hd;          // outputs u'_0, u'_d of every kick
+  const R *dv;         // v_1 - v_0 of every kick [kick][point]
   int64_t nn;
+  int nset, norb;
   static constexpr bool kMid = false;
   __device__ C load(int b, int64_t g) const { return src[b * nn + g]; }
   __device__ const C *raw(int b) const { return src + b * nn; }
@@ -627,12 +664,14 @@ template <typename R> struct OpHFinal2 {
   };
   __device__ Pre pre(int b, int64_t g) const {
     Pre q;
-    const int64_t i = (int64_t)(b >> 1) * nn + g;
-    if (b & 1) {
-      q.p = pd[i];
-      q.w = v1[g];
+    const int o = b / nset, X = b - o * nset;
+    const int64_t i = (int64_t)o * nn + g;
+    if (X) {
+      const int64_t kp = (int64_t)(X - 1) * nn;
+      q.p = pd[kp * norb + i];
+      q.w = v1[kp + g];
       q.t = p0[i];
-      q.d = dv[g];
+      q.d = dv[kp + g];
     } else {
       q.p = p0[i];
       q.w = v0[g];
@@ -643,11 +682,12 @@ template <typename R> struct OpHFinal2 {
     C r;
     r.x = v.x + q.p.x * q.w;
     r.y = v.y + q.p.y * q.w;
-    const int64_t i = (int64_t)(b >> 1) * nn + g;
-    if (b & 1) {
+    const int o = b / nset, X = b - o * nset;
+    const int64_t i = (int64_t)o * nn + g;
+    if (X) {
       r.x += q.t.x * q.d;
       r.y += q.t.y * q.d;
-      hd[i] = r;
+      hd[(int64_t)(X - 1) * norb * nn + i] = r;
     } else {
       h0[i] = r;
     }
@@ -777,29 +817,69 @@ int h_fft(opaw_ctx *c, const R *vks, const typename Tr<R>::C *pin, typename Tr<R
   return OPAW_OK;
 }
 
-// the grid part of H of both sets of a stage (set 1 as the difference form
-// H' t_d + dv t_0) in one interleaved batch of 2 norb; returns 0 when the
-// grid has no plane kernel (the caller then runs h_fft per set)
+// the grid part of H of every set of a stage (the kicked sets in the
+// difference form H' t_d + dv t_0) in one interleaved batch of (1 + nkick)
+// norb; returns 0 when the grid has no plane kernel (the caller then runs
+// h_fft per set)
 template <typename R>
-int h_fft2(opaw_ctx *c, const R *v0, const R *v1, const typename Tr<R>::C *t0, const typename Tr<R>::C *td,
-           typename Tr<R>::C *u0, typename Tr<R>::C *ud, const R *dv, int norb, int *ran) {
+int h_fftk(opaw_ctx *c, const R *v0, const R *v1, const typename Tr<R>::C *t0, const typename Tr<R>::C *td,
+           typename Tr<R>::C *u0, typename Tr<R>::C *ud, const R *dv, int norb, int nkick, int *ran) {
   typedef typename Tr<R>::C C;
   *ran = 0;
   if (norb <= 0) return OPAW_OK;
-  OPAW_CHECK(ensure(c->work[0], sizeof(C) * (size_t)c->nn * 2 * norb));
+  const int nset = 1 + nkick;
+  OPAW_CHECK(ensure(c->work[0], sizeof(C) * (size_t)c->nn * nset * norb));
   C *w = (C *)c->work[0].p;
   Dims3 d{c->nx, c->ny, c->nz};
-  OpCopy2<C> fwd{t0, td, w, c->nn};
-  OpHFinal2<R> fin{w, t0, td, v0, v1, u0, ud, dv, c->nn};
+  OpCopyK<C> fwd{t0, td, w, c->nn, nset, norb};
+  OpHFinalK<R> fin{w, t0, td, v0, v1, u0, ud, dv, c->nn, nset, norb};
   int st;
-  if (!launch_xy_if<C>(c, c->fft, 2 * norb, -1, fwd, &st)) return OPAW_OK;
+  if (!launch_xy_if<C>(c, c->fft, nset * norb, -1, fwd, &st)) return OPAW_OK;
   OPAW_CHECK(st);
-  OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, 2 * norb, 0, make_kin<R>(c, w))));
-  launch_xy_if<C>(c, c->fft, 2 * norb, +1, fin, &st);
+  OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, nset * norb, 0, make_kin<R>(c, w))));
+  launch_xy_if<C>(c, c->fft, nset * norb, +1, fin, &st);
   OPAW_CHECK(st);
   *ran = 1;
   return OPAW_OK;
 }
+
+// out = F^-1 [K(x) F pin] per orbital (OpTPA); inv_ekin: device [norb]
+template <typename R>
+int precond_kinetic(opaw_ctx *c, const typename Tr<R>::C *pin, const double *inv_ekin, typename Tr<R>::C *out,
+                    int norb) {
+  typedef typename Tr<R>::C C;
+  if (norb <= 0) return OPAW_OK;
+  Dims3 d{c->nx, c->ny, c->nz};
+  OpCopy<C> x_in{pin, out, c->nn};
+  OpCopy<C> inplace{out, out, c->nn};
+  OpTPA<R> tpa{out, c->nn, nullptr, nullptr, nullptr, c->nx, inv_ekin,
+               (R)(1.0 / ((double)c->nx * (double)c->ny * (double)c->nz))};
+  if constexpr (sizeof(R) == 8) {
+    tpa.k2x = c->d_k2[0];
+    tpa.k2y = c->d_k2[1];
+    tpa.k2z = c->d_k2[2];
+  } else {
+    tpa.k2x = c->d_k2f[0];
+    tpa.k2y = c->d_k2f[1];
+    tpa.k2z = c->d_k2f[2];
+  }
+  int st;
+  if (launch_xy_if<C>(c, c->fft, norb, -1, x_in, &st)) {
+    OPAW_CHECK(st);
+    OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, tpa)));
+    launch_xy_if<C>(c, c->fft, norb, +1, inplace, &st);
+    OPAW_CHECK(st);
+  } else {
+    OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, -1, x_in)));
+    OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, -1, inplace)));
+    OPAW_CHECK((launch_axis<C, 2>(c, c->fft.ax[2], d, norb, 0, tpa)));
+    OPAW_CHECK((launch_axis<C, 1>(c, c->fft.ax[1], d, norb, +1, inplace)));
+    OPAW_CHECK((launch_axis<C, 0>(c, c->fft.ax[0], d, norb, +1, inplace)));
+  }
+  return OPAW_OK;
+}
+template int precond_kinetic<float>(opaw_ctx *, const float2 *, const double *, float2 *, int);
+template int precond_kinetic<double>(opaw_ctx *, const double2 *, const double *, double2 *, int);
 
 // sigma table for sn_phi's exponent n: cached for n = -1, -1/2, 1/2, 1
 static int sigma_table(opaw_ctx *c, double n, const double **out) {
@@ -858,8 +938,8 @@ int shs_apply(opaw_ctx *c, int set, const typename Tr<R>::C *pin, typename Tr<R>
   template int h_apply_ex<R>(opaw_ctx *, const R *, const double *, const Tr<R>::C *, Tr<R>::C *, int,  \
                              const double2 *, const Tr<R>::C *, const R *, const double2 *, const double *); \
   template int h_fft<R>(opaw_ctx *, const R *, const Tr<R>::C *, Tr<R>::C *, int, const Tr<R>::C *, const R *); \
-  template int h_fft2<R>(opaw_ctx *, const R *, const R *, const Tr<R>::C *, const Tr<R>::C *, Tr<R>::C *,         \
-                         Tr<R>::C *, const R *, int, int *);                                                        \
+  template int h_fftk<R>(opaw_ctx *, const R *, const R *, const Tr<R>::C *, const Tr<R>::C *, Tr<R>::C *,         \
+                         Tr<R>::C *, const R *, int, int, int *);                                                   \
   template int gather2<R>(opaw_ctx *, const Tr<R>::C *, int, double2 *, double2 *);
 OPAW_INST(float)
 OPAW_INST(double)

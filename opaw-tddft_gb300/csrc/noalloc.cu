@@ -2,15 +2,19 @@
 // cannot allocate device memory.
 //
 // opaw_rconv allocates its work arrays and FFT tables on every call.  Some
-// callers cannot do that: a host program that hands this library a memory
-// budget fixed at start-up (for example a Fortran code that sized all device
-// memory once), code running while a CUDA stream is being captured into a
-// graph (cudaMalloc is not allowed there), or a process whose allocator must
-// not be touched from a library.  opaw_rconv_noalloc takes caller-allocated
-// device buffers for the input, the kernel and the output, and keeps its
-// scratch (the complex work array and the twiddle tables) in file-scope
-// device arrays of fixed size that every GPU which loads this library holds
-// until the process exits.
+// callers cannot do that: a host program that hands this library a device
+// memory budget fixed at start-up (for example a Fortran code that sized all
+// device memory once and runs close to it), or a process whose allocator a
+// library must not touch (a memory pool owned by another runtime).
+// opaw_rconv_noalloc takes caller-allocated device buffers for the input, the
+// kernel and the output, and keeps its scratch (the complex work array and
+// the twiddle tables) in file-scope device arrays of fixed size that every
+// GPU which loads this library holds until the process exits.  The twiddles
+// are computed on the device by a kernel, so nothing is copied from host
+// memory; the call waits for its stream before it returns, so the scratch is
+// free for the next call once it has returned.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "fft.cuh"
@@ -24,20 +28,46 @@ constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) double2 g_noalloc_work[kNoAllocMaxPoints];
 static __device__ __align__(256) double2 g_noalloc_tw[3 * kNoAllocMaxExtent];
 
+// Device addresses of the two arrays, looked up once per device and context
+// (host code must not use the symbols themselves): a device reset or a new
+// primary context gives the arrays new addresses, so the context handle the
+// lookup was made under is kept with them.
 struct NoAllocPtrs {
+  CUcontext ctx = nullptr;
   double2 *work = nullptr;
   double2 *tw = nullptr;
 };
 static NoAllocPtrs g_na_ptrs[kNoAllocMaxDevices];
 static std::mutex g_na_mutex;
 
-// Set-up, once per device with that device current: the device addresses of
-// the two arrays (host code must not use the symbols themselves).
+// cuCtxGetCurrent through the runtime's driver entry-point query, so that
+// the library does not link libcuda itself (it loads on hosts without a GPU)
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+static CUcontext current_context() {
+  static CtxGetCurrentFn fn = nullptr;
+  if (!fn) {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !f)
+      return nullptr;
+    fn = (CtxGetCurrentFn)f;
+  }
+  CUcontext cur = nullptr;
+  if (fn(&cur) != CUDA_SUCCESS) return nullptr;
+  return cur;
+}
+
+// set-up with device `dev` current: the lookup is repeated only when the
+// thread's current context differs from the one the cached addresses were
+// taken under (none bound yet on this thread, another context, a reset)
 static int noalloc_setup(int dev, NoAllocPtrs *out) {
   std::lock_guard<std::mutex> lock(g_na_mutex);
+  CUcontext cur = current_context();
   NoAllocPtrs &p = g_na_ptrs[dev];
-  if (!p.work) {
+  if (!p.work || !cur || p.ctx != cur) {
     void *w = nullptr, *t = nullptr;
+    // the runtime binds the device's primary context first if none is current
     cudaError_t e = cudaGetSymbolAddress(&w, g_noalloc_work);
     if (e != cudaSuccess) {
       set_error(std::string("cudaGetSymbolAddress(work): ") + cudaGetErrorString(e));
@@ -48,8 +78,10 @@ static int noalloc_setup(int dev, NoAllocPtrs *out) {
       set_error(std::string("cudaGetSymbolAddress(twiddles): ") + cudaGetErrorString(e));
       return OPAW_ERR_CUDA;
     }
+    cur = current_context();
     p.tw = (double2 *)t;
     p.work = (double2 *)w;
+    p.ctx = cur;
   }
   *out = p;
   return OPAW_OK;
@@ -58,6 +90,16 @@ static int noalloc_setup(int dev, NoAllocPtrs *out) {
 __global__ void k_na_real_to_complex(const double *__restrict__ g, double2 *__restrict__ a, int64_t n) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) a[i] = make_double2(g[i], 0.0);
+}
+
+// twiddle tables exp(-2 pi i t / n_k) of the three axes, axis k at k * 256
+__global__ void k_na_twiddles(double2 *__restrict__ tw, int n0, int n1, int n2) {
+  const int k = blockIdx.x, t = threadIdx.x;
+  const int n = k == 0 ? n0 : (k == 1 ? n1 : n2);
+  if (t >= n) return;
+  double s, c;
+  sincospi(2.0 * (double)t / (double)n, &s, &c);
+  tw[k * kNoAllocMaxExtent + t] = make_double2(c, -s);
 }
 
 static bool radix_ok(int n) {
@@ -100,7 +142,6 @@ extern "C" int opaw_rconv_noalloc(int n0, int n1, int n2, const double *gin, con
 
   opaw_ctx c;  // launch plumbing only: no tables, no buffers
   c.stream = (cudaStream_t)stream;
-  double2 tw[3][kNoAllocMaxExtent];
   for (int k = 0; k < 3; k++) {
     FFTAxis &a = c.fft.ax[k];
     a.n = ext[k];
@@ -111,19 +152,16 @@ extern "C" int opaw_rconv_noalloc(int n0, int n1, int n2, const double *gin, con
         a.radix[a.nstage++] = r;
         m /= r;
       }
-    for (int t = 0; t < ext[k]; t++) {
-      const double ang = 2.0 * M_PI * (double)t / (double)ext[k];
-      tw[k][t] = make_double2(cos(ang), -sin(ang));
-    }
     a.tw64 = p.tw + (size_t)k * kNoAllocMaxExtent;
     a.tw32 = nullptr;
     c.fft.n[k] = ext[k];
-    OPAW_CUDA(cudaMemcpyAsync(a.tw64, tw[k], sizeof(double2) * ext[k], cudaMemcpyHostToDevice, c.stream));
   }
+  k_na_twiddles<<<3, kNoAllocMaxExtent, 0, c.stream>>>(p.tw, n0, n1, n2);
+  OPAW_CUDA(cudaGetLastError());
   k_na_real_to_complex<<<grid1(n, 256), 256, 0, c.stream>>>(gin, p.work, n);
   OPAW_CUDA(cudaGetLastError());
   OPAW_CHECK(rconv_device(&c, p.work, bk, gout, n0, n1, n2));
-  // the twiddles came from this stack frame, and the scratch is shared with the next call
+  // every call shares the scratch: it is free again once this call's work ended
   OPAW_CUDA(cudaStreamSynchronize(c.stream));
   return OPAW_OK;
 }

@@ -277,6 +277,71 @@ static int need_psi(opaw_ctx *c, int set) {
   return OPAW_OK;
 }
 
+// Points the set-1 pointers of the context at kicked set k (the FP64 path
+// runs each kicked set through the set-1 routines); unbind restores them.
+struct KickBind {
+  double2 *psi;
+  double *vks, *dij, *rhoij, *dens, *nhat, *vh, *vxc;
+  float *vksf;
+};
+static KickBind bind_kick(opaw_ctx *c, int k) {
+  KickBind b{c->d_psi[1], c->d_vks[1], c->d_dij[1], c->d_rhoij[1], c->d_dens[1], c->d_nhat[1], c->d_vh[1],
+             c->d_vxc[1], c->d_vks_f[1]};
+  const size_t nn = (size_t)c->nn, nd = (size_t)c->nd;
+  c->d_psi[1] += (size_t)k * c->norb[1] * nn;
+  c->d_vks[1] += k * nn;
+  c->d_vks_f[1] += k * nn;
+  c->d_dij[1] += k * nd;
+  c->d_rhoij[1] += k * nd;
+  c->d_dens[1] += k * nn;
+  c->d_nhat[1] += k * nn;
+  c->d_vh[1] += k * nn;
+  c->d_vxc[1] += k * nn;
+  return b;
+}
+static void unbind_kick(opaw_ctx *c, const KickBind &b) {
+  c->d_psi[1] = b.psi;
+  c->d_vks[1] = b.vks;
+  c->d_vks_f[1] = b.vksf;
+  c->d_dij[1] = b.dij;
+  c->d_rhoij[1] = b.rhoij;
+  c->d_dens[1] = b.dens;
+  c->d_nhat[1] = b.nhat;
+  c->d_vh[1] = b.vh;
+  c->d_vxc[1] = b.vxc;
+}
+
+// nsteps steps of the unperturbed set and every kicked set; per step
+// 3 + 6 nkick doubles into dd (device): dip, then dip'_k, d_dip_k per kick.
+// tmp: 9 nkick device doubles of scratch (FP64 path).
+static int steps_dev(opaw_ctx *c, int nsteps, double dt, int prec, double *dd, double *tmp) {
+  const size_t per = 3 + 6 * (size_t)c->nkick;
+  if (prec == OPAW_PREC_MIXED) return mixed_steps(c, nsteps, dt, c->d_kgamma, dd);
+  for (int it = 0; it < nsteps; it++) {
+    // ncpaw_make_hamiltonian_tddft (tddft.f90:75) and propdt (:80), one set
+    // after the other: the sets never interact, so this equals the
+    // reference's order (both rebuilds, then both propagations)
+    OPAW_CHECK(rebuild_resident(c, 0, prec));
+    OPAW_CHECK(rk4_set64(c, 0, dt));
+    double *o = dd + per * (size_t)it;
+    for (int k = 0; k < c->nkick; k++) {
+      const KickBind b = bind_kick(c, k);
+      int st = rebuild_resident(c, 1, prec);
+      if (st == OPAW_OK) st = rk4_set64(c, 1, dt);
+      // plot_dip (tddft.f90:84): [dip, dip'_k, d_dip_k] of this kick
+      if (st == OPAW_OK) st = dipole_dev(c, c->h_kgamma[k], tmp + 9 * k);
+      unbind_kick(c, b);
+      OPAW_CHECK(st);
+    }
+    // dip (the same for every kick) once, then dip'_k, d_dip_k per kick
+    OPAW_CUDA(cudaMemcpyAsync(o, tmp, sizeof(double) * 3, cudaMemcpyDeviceToDevice, c->stream));
+    for (int k = 0; k < c->nkick; k++)
+      OPAW_CUDA(cudaMemcpyAsync(o + 3 + 6 * k, tmp + 9 * k + 3, sizeof(double) * 6, cudaMemcpyDeviceToDevice,
+                                c->stream));
+  }
+  return OPAW_OK;
+}
+
 int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, double *d_dip_out, double *dip_out,
                 double *dip_pert_out) {
   OPAW_CHECK(need_psi(c, 0));
@@ -284,21 +349,16 @@ int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, doub
   OPAW_ARG(c->norb[0] == c->norb[1], "both sets must hold the same number of orbitals");
   OPAW_ARG(prec == OPAW_PREC_FP64 || prec == OPAW_PREC_MIXED, "precision must be OPAW_PREC_FP64 or OPAW_PREC_MIXED");
   OPAW_ARG(nsteps >= 0, "nsteps must be >= 0");
-  OPAW_CHECK(ensure(c->work[11], sizeof(double) * (9 * (size_t)(nsteps > 0 ? nsteps : 1) + 16)));
+  if (c->nkick != 1) {
+    set_error("the context holds several kicked sets: use opaw_tddft_steps_kicks");
+    return OPAW_ERR_STATE;
+  }
+  c->h_kgamma.assign(1, gamma);
+  OPAW_CHECK(upload_kgamma(c));
+  const size_t nout = 9 * (size_t)(nsteps > 0 ? nsteps : 1);
+  OPAW_CHECK(ensure(c->work[11], sizeof(double) * (nout + 9 + 16)));
   double *dd = (double *)c->work[11].p;  // 9 values per step: dip, dip_pert, d_dip
-  if (prec == OPAW_PREC_MIXED) {
-    OPAW_CHECK(mixed_steps(c, nsteps, dt, gamma, dd));
-  }
-  for (int it = 0; it < nsteps && prec == OPAW_PREC_FP64; it++) {
-    // ncpaw_make_hamiltonian_tddft (tddft.f90:75) and propdt (:80), one set
-    // after the other: the two sets never interact, so this equals the
-    // reference's order (both rebuilds, then both propagations)
-    for (int set = 0; set < 2; set++) {
-      OPAW_CHECK(rebuild_resident(c, set, prec));
-      OPAW_CHECK(rk4_set64(c, set, dt));
-    }
-    OPAW_CHECK(dipole_dev(c, gamma, dd + 9 * (size_t)it));  // plot_dip (tddft.f90:84)
-  }
+  OPAW_CHECK(steps_dev(c, nsteps, dt, prec, dd, dd + nout));
   if ((d_dip_out || dip_out || dip_pert_out) && nsteps > 0) {
     std::vector<double> h(9 * (size_t)nsteps);
     OPAW_CUDA(cudaMemcpyAsync(h.data(), dd, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
@@ -310,6 +370,71 @@ int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, doub
         if (d_dip_out) d_dip_out[3 * it + k] = h[9 * (size_t)it + 6 + k];
       }
   }
+  return OPAW_OK;
+}
+
+// the same for every kicked set of the context: dip [nsteps][3],
+// dip_pert and d_dip [nsteps][nkick][3] (any may be NULL)
+static int tddft_steps_kicks(opaw_ctx *c, int nsteps, double dt, int prec, double *dip_out, double *dip_pert_out,
+                             double *d_dip_out) {
+  OPAW_CHECK(need_psi(c, 0));
+  OPAW_CHECK(need_psi(c, 1));
+  OPAW_ARG(c->norb[0] == c->norb[1], "every set must hold the same number of orbitals");
+  OPAW_ARG(prec == OPAW_PREC_FP64 || prec == OPAW_PREC_MIXED, "precision must be OPAW_PREC_FP64 or OPAW_PREC_MIXED");
+  OPAW_ARG(nsteps >= 0, "nsteps must be >= 0");
+  OPAW_ARG((int)c->h_kgamma.size() == c->nkick, "kick strengths missing: excite with opaw_excite_kicks");
+  OPAW_CHECK(upload_kgamma(c));
+  const size_t per = 3 + 6 * (size_t)c->nkick;
+  const size_t nout = per * (size_t)(nsteps > 0 ? nsteps : 1);
+  OPAW_CHECK(ensure(c->work[11], sizeof(double) * (nout + 9 * (size_t)c->nkick + 16)));
+  double *dd = (double *)c->work[11].p;
+  OPAW_CHECK(steps_dev(c, nsteps, dt, prec, dd, dd + nout));
+  if ((d_dip_out || dip_out || dip_pert_out) && nsteps > 0) {
+    std::vector<double> h(per * (size_t)nsteps);
+    OPAW_CUDA(cudaMemcpyAsync(h.data(), dd, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    OPAW_CUDA(cudaStreamSynchronize(c->stream));
+    const int K = c->nkick;
+    for (int it = 0; it < nsteps; it++) {
+      const double *q = h.data() + per * (size_t)it;
+      for (int j = 0; j < 3; j++) {
+        if (dip_out) dip_out[3 * it + j] = q[j];
+        for (int k = 0; k < K; k++) {
+          if (dip_pert_out) dip_pert_out[3 * ((size_t)it * K + k) + j] = q[3 + 6 * k + j];
+          if (d_dip_out) d_dip_out[3 * ((size_t)it * K + k) + j] = q[6 + 6 * k + j];
+        }
+      }
+    }
+  }
+  return OPAW_OK;
+}
+
+// excite_psi_bar_pert for nkick kicks at once (tddft_excite.f90:1-16):
+// kicked set k = set 0 * exp(-i gamma_k r_{ipol_k})
+static int excite_kicks(opaw_ctx *c, int nkick, const int *ipol, const double *gamma) {
+  OPAW_CHECK(need_psi(c, 0));
+  OPAW_ARG(nkick >= 1 && ipol && gamma, "nkick must be >= 1 with ipol and gamma arrays");
+  for (int k = 0; k < nkick; k++) {
+    OPAW_ARG(ipol[k] >= 1 && ipol[k] <= 3, "ipol must be 1, 2 or 3");
+    OPAW_ARG(std::isfinite(gamma[k]), "gamma must be finite");
+  }
+  const int norb = c->norb[0];
+  OPAW_CHECK(kick_capacity(c, nkick));
+  if (c->norb[1] != norb || c->nkick != nkick) {
+    OPAW_CUDA(cudaStreamSynchronize(c->stream));
+    cudaFree(c->d_psi[1]);
+    c->d_psi[1] = nullptr;
+    OPAW_CUDA(cudaMalloc(&c->d_psi[1], sizeof(double2) * (size_t)c->nn * norb * nkick));
+    c->norb[1] = norb;
+  }
+  c->nkick = nkick;
+  c->h_kgamma.assign(gamma, gamma + nkick);
+  for (int k = 0; k < nkick; k++) {
+    k_excite<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_psi[0], c->d_psi[1] + (size_t)k * norb * c->nn, c->nn,
+                                                      norb, c->nx, c->ny, c->nz, ipol[k], gamma[k], c->dx, c->dy,
+                                                      c->dz);
+    c->launches++;
+  }
+  OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
 }
 
@@ -463,18 +588,31 @@ int opaw_rconv(int n0, int n1, int n2, const double *gin, const double *bk, doub
 
 int opaw_excite(opaw_ctx *c, int ipol, double gamma) {
   OPAW_CHECK(check_cs(c, 0));
-  OPAW_CHECK(need_psi(c, 0));
-  OPAW_ARG(ipol >= 1 && ipol <= 3, "ipol must be 1, 2 or 3");
-  const int norb = c->norb[0];
-  if (c->norb[1] != norb) {
-    cudaFree(c->d_psi[1]);
-    c->d_psi[1] = nullptr;
-    OPAW_CUDA(cudaMalloc(&c->d_psi[1], sizeof(double2) * (size_t)c->nn * norb));
-    c->norb[1] = norb;
-  }
-  k_excite<<<grid1(c->nn, 256), 256, 0, c->stream>>>(c->d_psi[0], c->d_psi[1], c->nn, norb, c->nx, c->ny, c->nz, ipol,
-                                                    gamma, c->dx, c->dy, c->dz);
-  c->launches++;
+  OPAW_CHECK(excite_kicks(c, 1, &ipol, &gamma));
+  return finish(c);
+}
+
+int opaw_excite_kicks(opaw_ctx *c, int nkick, const int *ipol, const double *gamma) {
+  OPAW_CHECK(check_cs(c, 0));
+  OPAW_CHECK(excite_kicks(c, nkick, ipol, gamma));
+  return finish(c);
+}
+
+int opaw_kick_download(opaw_ctx *c, int kick, double *psi, int norb) {
+  OPAW_CHECK(check_cs(c, 0));
+  OPAW_CHECK(need_psi(c, 1));
+  OPAW_ARG(psi, "psi must be non-null");
+  OPAW_ARG(kick >= 0 && kick < c->nkick, "kick index out of range");
+  OPAW_ARG(norb == c->norb[1], "norb differs from the kicked sets' count");
+  OPAW_CUDA(cudaMemcpyAsync(psi, c->d_psi[1] + (size_t)kick * norb * c->nn, sizeof(double2) * (size_t)c->nn * norb,
+                            cudaMemcpyDeviceToHost, c->stream));
+  return finish(c);
+}
+
+int opaw_tddft_steps_kicks(opaw_ctx *c, int nsteps, double dt, int precision, double *dip_out, double *dip_pert_out,
+                           double *d_dip_out) {
+  OPAW_CHECK(check_cs(c, 0));
+  OPAW_CHECK(tddft_steps_kicks(c, nsteps, dt, precision, dip_out, dip_pert_out, d_dip_out));
   return finish(c);
 }
 

@@ -145,7 +145,8 @@ template <typename R> struct OpEmbed {
   const double *d0, *d1;
   C *wb;
   int64_t bs = 0;  // batch stride of wb
-  int pair = 0;    // 1: batch b transforms d0 (b = 0) or d1 (b = 1) alone; 0: d0 + i d1
+  int pair = 0;    // 1: batch b transforms d0 (b = 0) or d1 (b = 1) alone; 2: d0 + b ss alone; 0: d0 + i d1
+  int64_t ss = 0;  // source stride of pair mode 2
   static constexpr bool kMid = false;
   __device__ C load(int b, int64_t g) const {
     int64_t i;
@@ -154,7 +155,7 @@ template <typename R> struct OpEmbed {
     v.y = 0;
     if (!e.inner(g, i)) return v;
     if (pair) {
-      v.x = (R)(b ? d1 : d0)[i];
+      v.x = (R)(pair == 2 ? d0 + b * ss : (b ? d1 : d0))[i];
       return v;
     }
     v.x = (R)d0[i];
@@ -225,14 +226,15 @@ template <typename R> struct OpCrop {
   double *v0, *v1;
   double cn, nbd;
   int64_t bs = 0;  // batch stride of wb
-  int pair = 0;    // 1: batch b holds the potential of v0 (b = 0) or v1 (b = 1)
+  int pair = 0;    // 1: batch b holds the potential of v0 (b = 0) or v1 (b = 1); 2: of v0 + b ss
+  int64_t ss = 0;  // output stride of pair mode 2
   static constexpr bool kMid = false;
   __device__ C load(int b, int64_t g) const { return wb[b * bs + g]; }
   __device__ void store(int b, int64_t g, C v) const {
     int64_t i;
     if (!e.inner(g, i)) return;
     if (pair) {
-      (b ? v1 : v0)[i] = ((double)v.x * cn) * nbd;
+      (pair == 2 ? v0 + b * ss : (b ? v1 : v0))[i] = ((double)v.x * cn) * nbd;
       return;
     }
     v0[i] = ((double)v.x * cn) * nbd;  // rconv :29, get_vcon :20
@@ -301,6 +303,34 @@ int hartree_pair_t(opaw_ctx *c, const double *dens0, const double *dens1, double
   return OPAW_OK;
 }
 template int hartree_pair_t<float>(opaw_ctx *, const double *, const double *, double *, double *);
+
+// nsrc independent real sources (src + b nn) in one batch of complex
+// transforms, each with its own relative precision: vh + b nn
+template <typename R>
+int hartree_batch_t(opaw_ctx *c, const double *src, int nsrc, double *vh) {
+  typedef typename Tr<R>::C C;
+  if (nsrc <= 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->work[3], (size_t)nsrc * sizeof(C) * c->nnb));
+  C *wb = (C *)c->work[3].p;
+  Embed e{c->nx, c->ny, c->nz, c->nxb, c->nyb, c->nxb / 2 - c->nx / 2, c->nyb / 2 - c->ny / 2, c->nzb / 2 - c->nz / 2};
+  Dims3 d{c->nxb, c->nyb, c->nzb};
+  const double nbd = (double)c->nxb * (double)c->nyb * (double)c->nzb;
+  const int64_t bs = c->nnb;
+  const LineSub xlines{e.my, c->ny, e.mz, c->nz}, ylines{0, c->nyb, e.mz, c->nz};
+  OpEmbed<R> emb{e, src, nullptr, wb, bs, 2, c->nn};
+  OpMasked<C> yfwd{wb, (int64_t)c->nxb, c->nyb, e.my, e.my + c->ny, bs};
+  OpCopy<C> inplace{wb, wb, bs};
+  OpVk<R> vkop{wb, VkOf<R>::get(c), (int64_t)c->nxb * c->nyb, e.mz, e.mz + c->nz, bs};
+  OpCrop<R> crop{e, wb, vh, nullptr, 1.0 / nbd, nbd, bs, 2, c->nn};
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, nsrc, -1, emb, &xlines)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, nsrc, -1, yfwd, &ylines)));
+  OPAW_CHECK((launch_axis<C, 2>(c, c->fftb.ax[2], d, nsrc, 0, vkop)));
+  OPAW_CHECK((launch_axis<C, 1>(c, c->fftb.ax[1], d, nsrc, +1, inplace, &ylines)));
+  OPAW_CHECK((launch_axis<C, 0>(c, c->fftb.ax[0], d, nsrc, +1, crop, &xlines)));
+  return OPAW_OK;
+}
+template int hartree_batch_t<float>(opaw_ctx *, const double *, int, double *);
+template int hartree_batch_t<double>(opaw_ctx *, const double *, int, double *);
 template int hartree_pair_t<double>(opaw_ctx *, const double *, const double *, double *, double *);
 
 int hartree(opaw_ctx *c, const double *dens0, const double *dens1, double *vh0, double *vh1) {

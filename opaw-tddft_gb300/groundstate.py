@@ -42,16 +42,31 @@ def _shs(ctx, dtype, X, Y):
     ctx.sync()
 
 
-def _orthonormalise(ctx, dtype, X, scratch):
-    """X <- X G^-1/2 (canonical orthogonalisation, orthog_phi.f90)."""
+def _orthonormalise(ctx, dtype, X, scratch, refill=None):
+    """X <- X G^-1/2 (canonical orthogonalisation, orthog_phi.f90).  When the
+    block has (numerically) lost rank, the directions whose Gram eigenvalue is
+    below 1e-6 of the largest are dropped, as orthog_phi.f90 drops the small
+    eigenvalues of its Gram matrix, and `refill(n)` supplies that many fresh
+    vectors before the block is orthonormalised again."""
     norb = X.shape[0]
     G = ctx.gram_dev(dtype, X.data_ptr(), norb, X.data_ptr(), norb)
     G = 0.5 * (G + G.conj().T)
     w, V = np.linalg.eigh(G)
-    if w.min() <= 0:
+    keep = w > 1e-6 * w.max()
+    if keep.all():
+        ctx.rotate_dev(dtype, X.data_ptr(), norb, V / np.sqrt(w)[None, :], scratch.data_ptr())
+        X.copy_(scratch)
+        return
+    if refill is None or not keep.any():
         raise RuntimeError("subspace lost rank")
-    ctx.rotate_dev(dtype, X.data_ptr(), norb, V / np.sqrt(w)[None, :], scratch.data_ptr())
-    X.copy_(scratch)
+    nk = int(keep.sum())
+    # the kept directions first, largest Gram eigenvalue (least filtered away) first
+    order = np.argsort(-w[keep])
+    M = (V[:, keep] / np.sqrt(w[keep])[None, :])[:, order]
+    ctx.rotate_dev(dtype, X.data_ptr(), norb, M, scratch.data_ptr())
+    X[:nk].copy_(scratch[:nk])
+    X[nk:].copy_(refill(norb - nk))
+    _orthonormalise(ctx, dtype, X, scratch, None)
 
 
 def _rayleigh_ritz(ctx, dtype, X, HX, scratch):
@@ -181,7 +196,7 @@ def _lowest_states(ctx, psi0, n_iter, degree, tol, fp64_polish, nbuf, seed, verb
         X.copy_(Y1)
         if verbose:
             print(f"  filter a={a:.4f} b={b:.4f} m={m} lam_max={lam_max:.3f} |Y| max row {float(torch.sqrt((X.abs() ** 2).sum(dim=1)).max()):.3e}")
-        _orthonormalise(ctx, dt32, X, S)
+        _orthonormalise(ctx, dt32, X, S, refill=smooth_noise)
         _shs(ctx, dt32, X, HX)
         w = _rayleigh_ritz(ctx, dt32, X, HX, S)
     # FP64 polish of the wanted vectors

@@ -164,10 +164,14 @@ def build_system(
     coords=None,
     comp_rc=None,
     comp_sigma=0.45,
+    species=None,
 ):
     """Builds a synthetic system; `n` is (nx, ny, nz) and h the spacing (all
     axes).  ekcut None takes the reference's default cap (`reference_ekcut`);
-    0 leaves the kinetic energy uncapped."""
+    0 leaves the kinetic energy uncapped.  `species` (one entry per atom of
+    `coords`, keys of SPECIES) gives each atom its own cutoff and projector
+    channels; without it every atom has cutoff rc with one s and three p
+    channels per radial width in `alphas`."""
     rng = np.random.default_rng(seed)
     nx, ny, nz = n
     dx = dy = dz = float(h)
@@ -184,13 +188,22 @@ def build_system(
     coords = np.asarray(coords, dtype=np.float64)
     natom = len(coords)
 
-    ms_atom = 4 * len(alphas)  # one s and three p channels per radial width
+    if species is None:
+        kinds = [dict(rc=rc, s_alphas=tuple(alphas), p_alphas=tuple(alphas))] * natom
+    else:
+        kinds = [SPECIES[k] for k in species]
+    # one s channel per s width, three p channels per p width
+    ms_of = [len(k["s_alphas"]) + 3 * len(k["p_alphas"]) for k in kinds]
+    nr_of = [2 * (math.ceil((k["rc"] + rpad) / h) + 1) for k in kinds]
     ir_start = np.zeros((natom, 3), np.int32)
-    nrough = np.full((natom, 3), nr, np.int32)
-    ms = np.full(natom, ms_atom, np.int32)
+    nrough = np.array([[v, v, v] for v in nr_of], np.int32).reshape(natom, 3)
+    ms = np.array(ms_of, np.int32)
     dv = dx * dy * dz
     p3d, p3d1, s, sinv = [], [], [], []
     for a in range(natom):
+        nr = nr_of[a]
+        rc_a = kinds[a]["rc"]
+        ms_atom = ms_of[a]
         for k in range(3):
             ir_start[a, k] = math.ceil((coords[a, k] + xmax[k]) / h) - nr // 2 + 1
         # box coordinates (box x fastest -> arrays indexed [bz, by, bx])
@@ -207,11 +220,11 @@ def build_system(
             Y = Y - L[1] * np.round(Y / L[1])
             Z = Z - L[2] * np.round(Z / L[2])
         R2 = X * X + Y * Y + Z * Z
-        inside = (R2 < rc * rc).astype(np.float64)
+        inside = (R2 < rc_a * rc_a).astype(np.float64)
         chans = []
-        for al in alphas:
+        for al in kinds[a]["s_alphas"]:
             chans.append(Y00 * np.exp(-R2 / (2 * al * al)) * inside)
-        for al in alphas:
+        for al in kinds[a]["p_alphas"]:
             g = np.exp(-R2 / (2 * al * al)) * inside
             for comp in _ylm_p(X, Y, Z):
                 chans.append(comp * g)
@@ -228,8 +241,6 @@ def build_system(
         sinv.append(1.0 / (1.0 + sa) - 1.0)
 
     # compensation spheres, shape functions, Q_ij^LM
-    if comp_rc is None:
-        comp_rc = rc
     nlm = 9
     Zg, Yg, Xg = np.meshgrid(zs, ys, xs, indexing="ij")
     local_grid, g3d_all, ngrid, qijlm_all = [], [], [], []
@@ -242,7 +253,8 @@ def build_system(
             Y = Y - L[1] * np.round(Y / L[1])
             Z = Z - L[2] * np.round(Z / L[2])
         R2 = X * X + Y * Y + Z * Z
-        iz, iy, ix = np.nonzero(R2 < comp_rc * comp_rc)  # C order == reference's z,y,x loop order
+        crc = kinds[a]["rc"] if comp_rc is None else comp_rc
+        iz, iy, ix = np.nonzero(R2 < crc * crc)  # C order == reference's z,y,x loop order
         x, y, z = X[iz, iy, ix], Y[iz, iy, ix], Z[iz, iy, ix]
         r2 = x * x + y * y + z * z
         gauss = np.exp(-r2 / (2 * comp_sigma**2))
@@ -254,7 +266,7 @@ def build_system(
         g3d_all.append(G.reshape(-1))
         local_grid.append(np.stack([ix + 1, iy + 1, iz + 1], axis=1).astype(np.int32))
         ngrid.append(len(ix))
-        m = ms_atom
+        m = ms_of[a]
         Q = np.zeros((m, m, nlm))  # [j][i][lm] in C order == Fortran (lm, i, j)
         for lm in range(nlm):
             A = rng.standard_normal((m, m)) * (0.05 if lm == 0 else 0.02)
@@ -284,7 +296,7 @@ def build_system(
 
     dij0, eijkl, dinit = [], [], []
     for a in range(natom):
-        m = ms_atom
+        m = ms_of[a]
         Qh = _haar(rng, m)
         lam = rng.uniform(-1.0, 1.0, m)
         D = (Qh * lam) @ Qh.T
@@ -312,6 +324,72 @@ def build_system(
         vks0=vks.reshape(-1).copy(), dij_init=np.concatenate(dinit), coords=coords,
     )
     return sysobj
+
+
+# Projector channels of the two elements of the polyacenes, with the counts
+# and cutoffs of the JTH LDA datasets the reference ships (C: 2 s + 2x3 p
+# partial waves, r_c = 1.507 Bohr; H: 2 s + 1x3 p, r_c = 0.995 Bohr) and
+# Gaussian radial shapes standing in for the tabulated projectors.
+SPECIES = {
+    "C": dict(rc=1.507, s_alphas=(0.5, 0.8), p_alphas=(0.5, 0.8), valence=4),
+    "H": dict(rc=0.995, s_alphas=(0.4, 0.6), p_alphas=(0.5,), valence=1),
+}
+ANGSTROM = 1.8897261  # Bohr
+
+
+def polyacene_geometry(nring, cc=1.40, ch=1.09):
+    """Planar linear polyacene C(4n+2)H(2n+4) along x in the z = 0 plane:
+    regular hexagons of side cc (Angstrom) sharing their vertical edges, one
+    H per carbon with two carbon neighbours, at ch along the ring radius.
+    Returns (species list, coordinates in Bohr) centred on the origin."""
+    a = cc
+    sx = math.sqrt(3.0) * a  # ring-centre spacing
+    cpos = []
+    centres = [((i - (nring - 1) / 2.0) * sx, 0.0) for i in range(nring)]
+    for cxr, cyr in centres:
+        for k in range(6):
+            th = math.radians(30.0 + 60.0 * k)
+            p = (round(cxr + a * math.cos(th), 6), round(cyr + a * math.sin(th), 6))
+            if p not in cpos:
+                cpos.append(p)
+    cpos.sort(key=lambda q: (q[0], q[1]))
+    hpos = []
+    for (x, y) in cpos:
+        nb = sum(1 for (u, v) in cpos if 0.1 < math.hypot(u - x, v - y) < 1.1 * a)
+        if nb == 2:  # outer carbon: H along the radius of its own ring
+            cxr = min(centres, key=lambda c: math.hypot(c[0] - x, c[1] - y))
+            d = (x - cxr[0], y - cxr[1])
+            r = math.hypot(*d)
+            hpos.append((x + ch * d[0] / r, y + ch * d[1] / r))
+    species = ["C"] * len(cpos) + ["H"] * len(hpos)
+    xyz = np.array([[x, y, 0.0] for (x, y) in cpos + hpos]) * ANGSTROM
+    return species, xyz
+
+
+def polyacene(nring, n, h, seed=None, **kw):
+    """Synthetic OPAW system of the polyacene with `nring` rings on the grid
+    n = (nx, ny, nz) at spacing h: the generated geometry, C and H projector
+    channels (SPECIES), Gaussian wells of v_ks on every atom, and the
+    valence electron count (4 per C, 1 per H; norb = electrons / 2)."""
+    species, xyz = polyacene_geometry(nring)
+    nel = sum(SPECIES[k]["valence"] for k in species)
+    return build_system(n=n, h=h, coords=xyz, species=species, norb=nel // 2,
+                        seed=1000 + nring if seed is None else seed, **kw)
+
+
+# The molecules of the propagation benchmarks: rings, grid, spacing
+MOLECULES = {
+    "benzene": (1, (40, 40, 28), 0.5),
+    "naphthalene": (2, (48, 48, 32), 0.5),
+    "anthracene": (3, (64, 48, 32), 0.5),
+    "tetracene": (4, (96, 64, 48), 0.45),
+}
+
+
+def molecule(name, **kw):
+    """The named polyacene on its benchmark grid (MOLECULES)."""
+    nring, n, h = MOLECULES[name]
+    return polyacene(nring, n, h, **kw)
 
 
 def orbitals(sysobj: System, norb: int, seed: int = 11, sigma: float = 1.5, chunk: int = 16):

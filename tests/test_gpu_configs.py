@@ -2,8 +2,12 @@
 the naphthalene case (48 x 48 x 32 at h = 0.5 Bohr, 18 atoms) and the
 tetracene case (96 x 64 x 48 at h = 0.45 Bohr, 30 atoms), seeded synthetic
 systems with those shapes and atom counts (projector boxes of the carbon
-cutoff), a few orbitals each: one TDDFT step in FP64 and mixed precision
-against the oracle, and the mixed d_dip against FP64 over several steps."""
+cutoff), and the generated naphthalene geometry with its carbon and hydrogen
+projector sets, a few orbitals each: one TDDFT step in FP64 and mixed
+precision against the oracle, and the mixed d_dip against FP64 over several
+steps."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -23,9 +27,17 @@ def rel(a, b):
     return float(np.abs(a - b).max() / np.abs(b).max())
 
 
-@pytest.fixture(scope="module", params=sorted(SHAPES))
+def make_system(name):
+    if name in SHAPES:
+        return synthetic.build_system(norb=3, **SHAPES[name])
+    # a generated polyacene (C atoms: 8 projectors, H atoms: 5, two box sizes),
+    # three of its orbitals occupied
+    return dataclasses.replace(synthetic.molecule(name), rnel=6.0)
+
+
+@pytest.fixture(scope="module", params=sorted(SHAPES) + ["naphthalene"])
 def case(request):
-    s = synthetic.build_system(norb=3, **SHAPES[request.param])
+    s = make_system(request.param)
     psi = synthetic.orbitals(s, 3, seed=21).reshape(3, -1)
     o = orc.Oracle(s)
     c = pkg.Context(s)
