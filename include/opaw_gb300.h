@@ -152,6 +152,49 @@ int opaw_proj_dev(opaw_ctx *ctx, int which, int dtype, const void *pin, int norb
  * norb positive kinetic energies; asynchronous on the context's stream
  * (the host array is consumed before the call returns); out may equal pin */
 int opaw_precond_kinetic_dev(opaw_ctx *ctx, int dtype, const void *pin, const double *ekin, void *out, int norb);
+/* kinetic energies ekin[b] = <x_b|T|x_b> / <x_b|x_b> of norb device
+ * orbitals, T the kinetic operator of the Hamiltonian (ek.f90:1-51: |k|^2/2
+ * capped at ekcut); the preconditioners' energy scale; host output, waits
+ * for the stream */
+int opaw_kinetic_energy_dev(opaw_ctx *ctx, int dtype, const void *x, int norb, double *ekin);
+
+/* ---- learned preconditioner (no reference counterpart: the reference's
+ * ground state comes from a Chebyshev-filtered SCF without preconditioning,
+ * chebyr_m.f90:1-48).  A 3-layer 3D convolutional network (3^3 kernels, 16
+ * channels, BF16 weights and activations, FP32 accumulation on the tensor
+ * cores) maps the normalised residual r / |r| of an orbital and v_ks - eps
+ * to a correction added to the Teter-Payne-Allan preconditioner's output.
+ * Parameters: 3 layers of [27 taps][16 ci][16 co] weights then 16 biases
+ * (float, 3 * 6928 values); activation channels are stored as 16 BF16
+ * values per voxel ([batch][z][y][x][16], unused channels zero). ---- */
+typedef struct opaw_net opaw_net;
+int opaw_net_create(unsigned long long seed, opaw_net **out);
+int opaw_net_free(opaw_net *net);
+int opaw_net_params(opaw_net *net, float *params);
+int opaw_net_set_params(opaw_net *net, const float *params);
+int64_t opaw_net_launches(opaw_net *net);
+/* forward pass of a host batch x (BF16 bits, [batch][nz][ny][nx][16]) into
+ * out (float, [batch][nz][ny][nx][16]; channels 0, 1 are the correction) */
+int opaw_net_forward(opaw_net *net, int batch, int nz, int ny, int nx, const uint16_t *x, float *out);
+/* loss = sum over the interior voxels (margin voxels from each face) of
+ * |out - tgt|^2 / count, and its gradient with respect to the parameters
+ * (float, params layout), of a host batch of P^3 patches; tgt [batch][P^3][2] */
+int opaw_net_loss_grad(opaw_net *net, int batch, int P, int margin, const uint16_t *x, const float *tgt,
+                       double *loss, float *grad);
+/* training patches from device fields of a context's grid: r, t complex128
+ * [norb][nn] (residuals and targets), per orbital eps and scale (host),
+ * origins [npatch][4] = (orbital, z0, y0, x0), periodic wrap; stored in the
+ * net at patch indices first .. first + npatch - 1 */
+int opaw_net_add_patches(opaw_net *net, opaw_ctx *ctx, const void *r, const void *t, int norb, const double *eps,
+                         const double *scale, int npatch, const int *origins, int P, int first);
+/* nsteps Adam steps (learning rate lr) on minibatches of `batch` of the first
+ * npatch stored patches; losses[s] the loss of step s (may be NULL) */
+int opaw_net_train(opaw_net *net, int npatch, int P, int margin, int nsteps, int batch, double lr, double *losses);
+/* w = K r + |r| N(r / |r|, v_ks - eps) for norb device orbitals of the
+ * context (K: opaw_precond_kinetic_dev with ekin); eps, ekin host [norb] */
+int opaw_precond_learned_dev(opaw_ctx *ctx, opaw_net *net, int dtype, const void *r, const double *eps,
+                             const double *ekin, void *w, int norb);
+
 /* fft3d_forward / fft3d_backward (lib/library_fftw_v3.f90:56-83): in-place
  * unnormalised 3D DFT of norb device arrays, sign -1 forward, +1 backward */
 int opaw_fft3d_dev(opaw_ctx *ctx, int dtype, void *data, int norb, int sign);
@@ -167,6 +210,13 @@ int opaw_rotate_dev(opaw_ctx *ctx, int dtype, const void *A, int na, const doubl
  * resident orbitals of `set`, Psi <- Psi V diag(l)^-1/2 with G = V diag(l) V^H;
  * eig (may be NULL) receives the Gram eigenvalues l ascending */
 int opaw_orthog(opaw_ctx *ctx, int set, double *eig);
+/* FP64 orthonormalisation of the resident orbitals of `set` entirely on the
+ * device (the re-orthogonalisation of the orbital Gram matrix; orthog_phi.f90
+ * does it with a host eigensolve): method 0 Cholesky, Psi <- Psi L^-H with
+ * G = L L^H; method 1 Loewdin, Psi <- Psi G^-1/2 by Newton-Schulz iteration,
+ * for orbitals close to orthonormal (max |G - I| < 0.5, else OPAW_ERR_ARG).
+ * offdiag (may be NULL) receives max |G - I| before the step. */
+int opaw_orthonormalize_dev(opaw_ctx *ctx, int set, int method, double *offdiag);
 /* host-only complex Hermitian eigensolver (cyclic Jacobi) used by
  * opaw_orthog, replacing EISPACK ch (library_1_matrix_all.f90:351-401):
  * H (n x n complex128, column-major, overwritten), w ascending, V columns */

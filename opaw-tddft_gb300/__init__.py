@@ -107,6 +107,18 @@ SIGNATURES = {
     "opaw_kick_download": (ct.c_int, [_P, ct.c_int, _P, ct.c_int]),
     "opaw_tddft_steps_kicks": (ct.c_int, [_P, ct.c_int, ct.c_double, ct.c_int, _P, _P, _P]),
     "opaw_precond_kinetic_dev": (ct.c_int, [_P, ct.c_int, _P, _P, _P, ct.c_int]),
+    "opaw_kinetic_energy_dev": (ct.c_int, [_P, ct.c_int, _P, ct.c_int, _P]),
+    "opaw_net_create": (ct.c_int, [ct.c_ulonglong, ct.POINTER(ct.c_void_p)]),
+    "opaw_net_free": (ct.c_int, [_P]),
+    "opaw_net_params": (ct.c_int, [_P, _P]),
+    "opaw_net_set_params": (ct.c_int, [_P, _P]),
+    "opaw_net_launches": (ct.c_int64, [_P]),
+    "opaw_net_forward": (ct.c_int, [_P, ct.c_int, ct.c_int, ct.c_int, ct.c_int, _P, _P]),
+    "opaw_net_loss_grad": (ct.c_int, [_P, ct.c_int, ct.c_int, ct.c_int, _P, _P, _P, _P]),
+    "opaw_net_add_patches": (ct.c_int, [_P, _P, _P, _P, ct.c_int, _P, _P, ct.c_int, _P, ct.c_int, ct.c_int]),
+    "opaw_net_train": (ct.c_int, [_P, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_double, _P]),
+    "opaw_precond_learned_dev": (ct.c_int, [_P, _P, ct.c_int, _P, _P, _P, _P, ct.c_int]),
+    "opaw_orthonormalize_dev": (ct.c_int, [_P, ct.c_int, ct.c_int, _P]),
     "opaw_ensemble_steps": (ct.c_int, [_P, ct.c_int, ct.c_int, ct.c_double, _P, _P, _P]),
 }
 
@@ -291,6 +303,11 @@ class Context:
         _check(lib().opaw_precond_kinetic_dev(self.h, dtype, ct.c_void_p(pin_ptr), _ptr(e), ct.c_void_p(out_ptr),
                                               norb))
 
+    def kinetic_energy_dev(self, dtype, x_ptr, norb):
+        out = np.empty(norb)
+        _check(lib().opaw_kinetic_energy_dev(self.h, dtype, ct.c_void_p(x_ptr), norb, _ptr(out)))
+        return out
+
     def fft3d_dev(self, dtype, ptr, norb, sign):
         _check(lib().opaw_fft3d_dev(self.h, dtype, ct.c_void_p(ptr), norb, sign))
 
@@ -309,6 +326,13 @@ class Context:
         w = np.empty(self.system_norb(set_))
         _check(lib().opaw_orthog(self.h, set_, _ptr(w)))
         return w
+
+    def orthonormalize(self, set_=0, method=0):
+        """FP64 orthonormalisation on the device: 0 Cholesky, 1 Loewdin
+        (Newton-Schulz); returns max |G - I| before it."""
+        off = ct.c_double()
+        _check(lib().opaw_orthonormalize_dev(self.h, set_, method, ct.byref(off)))
+        return off.value
 
     def system_norb(self, set_):
         return self._norb[set_]

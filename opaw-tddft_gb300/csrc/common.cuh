@@ -321,6 +321,9 @@ int h_fftk(opaw_ctx *c, const R *v0, const R *v1, const typename Tr<R>::C *t0, c
 template <typename R>
 int precond_kinetic(opaw_ctx *c, const typename Tr<R>::C *pin, const double *inv_ekin, typename Tr<R>::C *out,
                     int norb);
+// kinetic energies <x_o|T|x_o> / <x_o|x_o> of norb device orbitals into a host array
+template <typename R>
+int kinetic_energy(opaw_ctx *c, const typename Tr<R>::C *x, int norb, double *ekin);
 // <p~|pin> and <p~1|pin> in one pass over the boxes
 template <typename R>
 int gather2(opaw_ctx *c, const typename Tr<R>::C *pin, int norb, double2 *c0, double2 *c1);
@@ -345,7 +348,8 @@ int nhat_raw_of(opaw_ctx *c, const double *rhoij, double *out);
 int sums2(opaw_ctx *c, const double *a, const double *b, double *part);
 constexpr int kRedBlocks = 1024;
 int vxc_of(opaw_ctx *c, const double *dens, const double *core, double *out);
-int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, double *out);
+// D_ij (get_dij.f90) from rho_ij and the potential v_ks - v_xc of Dhat (vxc may be null)
+int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vxc, double *out);
 // (mixed.cu) nsteps mixed-precision TDDFT steps of the unperturbed set and
 // the c->nkick kicked sets (strengths gamma_dev[k]); 3 + 6 nkick doubles per
 // step into dd_dev: dip, then dip'_k and d_dip_k of every kick

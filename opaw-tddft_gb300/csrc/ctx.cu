@@ -716,6 +716,15 @@ int opaw_precond_kinetic_dev(opaw_ctx *c, int dtype, const void *pin, const doub
   return OPAW_ERR_ARG;
 }
 
+int opaw_kinetic_energy_dev(opaw_ctx *c, int dtype, const void *x, int norb, double *ekin) {
+  OPAW_CHECK(check_ctx(c));
+  OPAW_ARG(x && ekin && norb >= 0, "bad buffers");
+  if (dtype == OPAW_C128) return kinetic_energy<double>(c, (const double2 *)x, norb, ekin);
+  if (dtype == OPAW_C64) return kinetic_energy<float>(c, (const float2 *)x, norb, ekin);
+  set_error("dtype must be OPAW_C128 or OPAW_C64");
+  return OPAW_ERR_ARG;
+}
+
 int opaw_sn_apply_dev(opaw_ctx *c, int dtype, double n, const void *pin, void *sp, int norb) {
   OPAW_CHECK(check_ctx(c));
   OPAW_ARG(pin && sp && norb >= 0, "bad buffers");

@@ -148,6 +148,99 @@ int rotate_t(opaw_ctx *c, const typename Tr<R>::C *A, int na, const double2 *Mde
   return OPAW_OK;
 }
 
+// ---- FP64 orthonormalisation on the device -------------------------------
+// Cholesky of the Hermitian positive definite Gram matrix G (n x n,
+// column-major) in one CTA, G = L L^H (right-looking, a column at a time),
+// then M = L^-H (columns of L^-1 by forward substitution, a thread per
+// column): Psi M is orthonormal since M^H G M = I.  info[0] = k + 1 when the
+// k-th pivot is not positive (M is then left unset), 0 otherwise.
+__global__ void __launch_bounds__(256) k_chol_inv(double2 *__restrict__ G, int n, double2 *__restrict__ M,
+                                                  int *__restrict__ info) {
+  __shared__ int bad;
+  __shared__ double piv;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < n; k++) {
+    if (threadIdx.x == 0) {
+      const double d = G[k + (int64_t)n * k].x;
+      if (!(d > 0.0)) bad = k + 1;
+      piv = d > 0.0 ? sqrt(d) : 1.0;
+      G[k + (int64_t)n * k] = make_double2(piv, 0.0);
+    }
+    __syncthreads();
+    if (bad) break;
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) {
+      double2 &g = G[i + (int64_t)n * k];
+      g.x /= piv;
+      g.y /= piv;
+    }
+    __syncthreads();
+    // trailing update of the lower triangle: G[i][j] -= L[i][k] conj(L[j][k])
+    const int m = n - k - 1;
+    for (int64_t e = threadIdx.x; e < (int64_t)m * m; e += blockDim.x) {
+      const int j = k + 1 + (int)(e / m), i = k + 1 + (int)(e % m);
+      if (i < j) continue;
+      const double2 a = G[i + (int64_t)n * k], b = G[j + (int64_t)n * k];
+      double2 &g = G[i + (int64_t)n * j];
+      g.x -= a.x * b.x + a.y * b.y;
+      g.y -= a.y * b.x - a.x * b.y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) info[0] = bad;
+  if (bad) return;
+  // column j of X = L^-1: X[i][j] = (delta_ij - sum_{j<=q<i} L[i][q] X[q][j]) / L[i][i]; M = X^H
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int i = 0; i < j; i++) M[j + (int64_t)n * i] = make_double2(0.0, 0.0);  // M[j][i] = conj(X[i][j]) = 0
+    for (int i = j; i < n; i++) {
+      double sx = (i == j) ? 1.0 : 0.0, sy = 0.0;
+      for (int q = j; q < i; q++) {
+        const double2 l = G[i + (int64_t)n * q];
+        const double2 x = M[j + (int64_t)n * q];  // conj(X[q][j]) stored at M[j][q]
+        // L[i][q] X[q][j] with X[q][j] = conj(x)
+        sx -= l.x * x.x + l.y * x.y;
+        sy -= l.y * x.x - l.x * x.y;
+      }
+      const double d = G[i + (int64_t)n * i].x;
+      M[j + (int64_t)n * i] = make_double2(sx / d, -sy / d);  // store conj(X[i][j])
+    }
+  }
+}
+
+// small dense complex products on the device: C = alpha A B + beta I
+// (n x n column-major; a thread per output entry)
+__global__ void k_small_gemm(const double2 *__restrict__ A, const double2 *__restrict__ B, int n, double alpha,
+                             double beta, double2 *__restrict__ Cm) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * n) return;
+  const int i = (int)(e % n), j = (int)(e / n);
+  double sx = 0, sy = 0;
+  for (int q = 0; q < n; q++) {
+    const double2 a = A[i + (int64_t)n * q], b = B[q + (int64_t)n * j];
+    sx += a.x * b.x - a.y * b.y;
+    sy += a.x * b.y + a.y * b.x;
+  }
+  Cm[e] = make_double2(alpha * sx + (i == j ? beta : 0.0), alpha * sy);
+}
+
+// max |G - I| (one CTA) into out[0]
+__global__ void k_offdiag(const double2 *__restrict__ G, int n, double *__restrict__ out) {
+  __shared__ double sh[256];
+  double m = 0;
+  for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += blockDim.x) {
+    const int i = (int)(e % n), j = (int)(e / n);
+    const double2 g = G[e];
+    m = fmax(m, hypot(g.x - (i == j ? 1.0 : 0.0), g.y));
+  }
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+
 // ---- host: cyclic Jacobi for a complex Hermitian matrix (column-major).
 // On return w holds the eigenvalues ascending and V the eigenvectors.
 void herm_eig(int n, std::vector<std::complex<double>> &H, std::vector<double> &w,
@@ -284,6 +377,82 @@ int opaw_orthog(opaw_ctx *c, int set, double *eig_out) {
     for (int j = 0; j < n; j++) eig_out[j] = w[j];
   OPAW_CHECK(ensure(c->work[7], sizeof(double2) * (size_t)c->nn * n));
   OPAW_CHECK(opaw_rotate_dev(c, OPAW_C128, c->d_psi[set], n, (const double *)V.data(), n, c->work[7].p));
+  OPAW_CUDA(cudaMemcpyAsync(c->d_psi[set], c->work[7].p, sizeof(double2) * (size_t)c->nn * n,
+                            cudaMemcpyDeviceToDevice, c->stream));
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  return OPAW_OK;
+}
+
+// FP64 orthonormalisation of the resident orbitals of `set` on the device
+// (no host eigensolve): method 0 Cholesky, Psi <- Psi L^-H with G = L L^H;
+// method 1 Loewdin, Psi <- Psi G^-1/2 by the coupled Newton-Schulz iteration
+// (Y <- Y T, Z <- T Z, T = (3 I - Z Y) / 2 from Y = G, Z = I), which
+// converges when the orbitals are close to orthonormal (max |G - I| < 0.5 is
+// required; further away use method 0).  offdiag (may be NULL) receives
+// max |G - I| before the orthonormalisation.
+int opaw_orthonormalize_dev(opaw_ctx *c, int set, int method, double *offdiag) {
+  if (!c || (set != 0 && set != 1) || (method != 0 && method != 1)) {
+    set_error("bad arguments");
+    return OPAW_ERR_ARG;
+  }
+  const int n = c->norb[set];
+  if (n == 0) {
+    set_error("no orbitals uploaded for this set");
+    return OPAW_ERR_STATE;
+  }
+  const size_t nm = (size_t)n * n;
+  OPAW_CHECK(ensure(c->gramout, sizeof(double2) * 5 * nm + 64));
+  double2 *G = (double2 *)c->gramout.p, *M = G + nm, *Y = M + nm, *Z = Y + nm, *T = Z + nm;
+  int *info = (int *)(T + nm);
+  double *off = (double *)(T + nm) + 2;
+  OPAW_CHECK(gram_t<double>(c, c->d_psi[set], n, c->d_psi[set], n, G));
+  k_offdiag<<<1, 256, 0, c->stream>>>(G, n, off);
+  c->launches++;
+  double hoff = 0.0;
+  OPAW_CUDA(cudaMemcpyAsync(&hoff, off, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  if (offdiag) *offdiag = hoff;
+  const int nb = grid1((int64_t)nm, 256);
+  if (method == 0) {
+    k_chol_inv<<<1, 256, 0, c->stream>>>(G, n, M, info);
+    c->launches++;
+    int hinfo = 0;
+    OPAW_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    OPAW_CUDA(cudaStreamSynchronize(c->stream));
+    if (hinfo) {
+      set_error("orbitals are linearly dependent (Cholesky pivot " + std::to_string(hinfo) + " not positive)");
+      return OPAW_ERR_NONFINITE;
+    }
+  } else {
+    if (!(hoff < 0.5)) {
+      set_error("Loewdin by Newton-Schulz needs max |G - I| < 0.5: use the Cholesky method");
+      return OPAW_ERR_ARG;
+    }
+    OPAW_CUDA(cudaMemcpyAsync(Y, G, sizeof(double2) * nm, cudaMemcpyDeviceToDevice, c->stream));
+    // Z = I: 0 A B + 1 I
+    k_small_gemm<<<nb, 256, 0, c->stream>>>(G, G, n, 0.0, 1.0, Z);
+    c->launches++;
+    for (int it = 0; it < 30; it++) {
+      k_small_gemm<<<nb, 256, 0, c->stream>>>(Z, Y, n, -0.5, 1.5, T);  // T = (3 I - Z Y) / 2
+      k_small_gemm<<<nb, 256, 0, c->stream>>>(Y, T, n, 1.0, 0.0, M);   // Y T
+      OPAW_CUDA(cudaMemcpyAsync(Y, M, sizeof(double2) * nm, cudaMemcpyDeviceToDevice, c->stream));
+      k_small_gemm<<<nb, 256, 0, c->stream>>>(T, Z, n, 1.0, 0.0, M);   // T Z
+      OPAW_CUDA(cudaMemcpyAsync(Z, M, sizeof(double2) * nm, cudaMemcpyDeviceToDevice, c->stream));
+      c->launches += 3;
+      if (it % 4 == 3) {  // converged when Y (-> G^1/2 G^-1/2 ... ) Z -> I: check |T - I|
+        k_offdiag<<<1, 256, 0, c->stream>>>(T, n, off);
+        c->launches++;
+        double d = 1.0;
+        OPAW_CUDA(cudaMemcpyAsync(&d, off, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        OPAW_CUDA(cudaStreamSynchronize(c->stream));
+        if (d < 1e-15) break;
+      }
+    }
+    OPAW_CUDA(cudaMemcpyAsync(M, Z, sizeof(double2) * nm, cudaMemcpyDeviceToDevice, c->stream));  // G^-1/2
+  }
+  OPAW_CUDA(cudaGetLastError());
+  OPAW_CHECK(ensure(c->work[7], sizeof(double2) * (size_t)c->nn * n));
+  OPAW_CHECK(rotate_t<double>(c, c->d_psi[set], n, M, n, (double2 *)c->work[7].p));
   OPAW_CUDA(cudaMemcpyAsync(c->d_psi[set], c->work[7].p, sizeof(double2) * (size_t)c->nn * n,
                             cudaMemcpyDeviceToDevice, c->stream));
   OPAW_CUDA(cudaStreamSynchronize(c->stream));

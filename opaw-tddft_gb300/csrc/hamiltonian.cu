@@ -9,6 +9,8 @@
 // so FP64 results are bit-reproducible run to run.
 #include <algorithm>
 
+#include <vector>
+
 #include "fft.cuh"
 
 namespace opaw {
@@ -880,6 +882,73 @@ int precond_kinetic(opaw_ctx *c, const typename Tr<R>::C *pin, const double *inv
 }
 template int precond_kinetic<float>(opaw_ctx *, const float2 *, const double *, float2 *, int);
 template int precond_kinetic<double>(opaw_ctx *, const double2 *, const double *, double2 *, int);
+
+// per orbital sum over k of min(|k|^2 / 2, ekcut) |F x|^2 and of |F x|^2 (one
+// block per orbital); their ratio is the kinetic energy <x|T|x> / <x|x> of
+// the Hamiltonian's kinetic operator (ek.f90)
+template <typename C, typename R>
+__global__ void k_ekin_sums(const C *__restrict__ fx, int nx, int ny, int nz, const R *__restrict__ k2x,
+                            const R *__restrict__ k2y, const R *__restrict__ k2z, double ekcut,
+                            double *__restrict__ out) {
+  __shared__ double sh[2][8];
+  const int o = blockIdx.x;
+  const int64_t nn = (int64_t)nx * ny * nz;
+  double a = 0, b = 0;
+  for (int64_t g = threadIdx.x; g < nn; g += blockDim.x) {
+    const int x = (int)(g % nx), y = (int)((g / nx) % ny), z = (int)(g / ((int64_t)nx * ny));
+    double e = 0.5 * ((double)k2x[x] + (double)k2y[y] + (double)k2z[z]);
+    if (ekcut > 0.0 && e > ekcut) e = ekcut;
+    const C v = fx[(int64_t)o * nn + g];
+    const double m = (double)v.x * v.x + (double)v.y * v.y;
+    a += e * m;
+    b += m;
+  }
+#pragma unroll
+  for (int q = 16; q > 0; q >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, q);
+    b += __shfl_down_sync(0xffffffffu, b, q);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = a;
+    sh[1][w] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sa = 0, sb = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+      sa += sh[0][i];
+      sb += sh[1][i];
+    }
+    out[2 * o] = sa;
+    out[2 * o + 1] = sb;
+  }
+}
+
+// kinetic energies <x_o|T|x_o> / <x_o|x_o> of norb device orbitals (host out)
+template <typename R>
+int kinetic_energy(opaw_ctx *c, const typename Tr<R>::C *x, int norb, double *ekin) {
+  typedef typename Tr<R>::C C;
+  if (norb <= 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->work[0], sizeof(C) * (size_t)c->nn * norb));
+  OPAW_CHECK(ensure(c->pre, sizeof(double) * 2 * (size_t)norb));
+  C *w = (C *)c->work[0].p;
+  OPAW_CUDA(cudaMemcpyAsync(w, x, sizeof(C) * (size_t)c->nn * norb, cudaMemcpyDeviceToDevice, c->stream));
+  OPAW_CHECK(fft3d<R>(c, c->fft, w, norb, -1));
+  const R *k2[3];
+  for (int k = 0; k < 3; k++) k2[k] = sizeof(R) == 8 ? (const R *)c->d_k2[k] : (const R *)c->d_k2f[k];
+  k_ekin_sums<C, R><<<norb, 256, 0, c->stream>>>(w, c->nx, c->ny, c->nz, k2[0], k2[1], k2[2], c->ekcut,
+                                                 (double *)c->pre.p);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  std::vector<double> h(2 * (size_t)norb);
+  OPAW_CUDA(cudaMemcpyAsync(h.data(), c->pre.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  for (int o = 0; o < norb; o++) ekin[o] = h[2 * o + 1] > 0.0 ? h[2 * o] / h[2 * o + 1] : 0.0;
+  return OPAW_OK;
+}
+template int kinetic_energy<float>(opaw_ctx *, const float2 *, int, double *);
+template int kinetic_energy<double>(opaw_ctx *, const double2 *, int, double *);
 
 // sigma table for sn_phi's exponent n: cached for n = -1, -1/2, 1/2, 1
 static int sigma_table(opaw_ctx *c, double n, const double **out) {

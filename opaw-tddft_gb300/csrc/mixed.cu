@@ -1307,10 +1307,10 @@ static int mix_potentials(opaw_ctx *c, Mix &m) {
   MIX_LAUNCHED();
   OPAW_CUDA(cudaMemcpyAsync(c->d_vh[0], m.vh, sizeof(double) * c->nn, cudaMemcpyDeviceToDevice, c->stream));
   // D_ij of every set (FP64) and the kicks' differences
-  OPAW_CHECK(dij_of(c, c->d_rhoij[0], c->d_vks[0], c->d_dij[0]));
+  OPAW_CHECK(dij_of(c, c->d_rhoij[0], c->d_vks[0], c->d_vxc[0], c->d_dij[0]));
   for (int k = 0; k < K; k++)
     OPAW_CHECK(dij_of(c, c->d_rhoij[1] + (size_t)k * c->nd, c->d_vks[1] + (size_t)k * c->nn,
-                      c->d_dij[1] + (size_t)k * c->nd));
+                      c->d_vxc[1] + (size_t)k * c->nn, c->d_dij[1] + (size_t)k * c->nd));
   if (c->nd > 0) {
     k_mix_ddij<<<dim3(grid1(c->nd, 128), K), 128, 0, c->stream>>>(c->d_dij[0], c->d_dij[1], m.ddij, c->nd);
     MIX_LAUNCHED();

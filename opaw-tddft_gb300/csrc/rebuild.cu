@@ -542,8 +542,11 @@ __global__ void k_scale2(double *__restrict__ a, double *__restrict__ b, int64_t
 }
 
 // --------------------------------------------------- D_ij (A16) --
-// prod[a][lm] = dv sum_g v_ks(r_g) g_lm(r_g)
-__global__ void k_dhat_prod(const double *__restrict__ vks, const int *__restrict__ gpt,
+// prod[a][lm] = dv sum_g (v_ks - v_xc)(r_g) g_lm(r_g): the potential of
+// Dhat_ij without the XC part, as pawdij builds it when the compensation
+// charge is not in the XC density (usexcnhat = 0, the value libpaw_mod.f90
+// sets: libpaw/4_m_pawdij.F90:375-385 takes vtrial - vxc); vxc may be null
+__global__ void k_dhat_prod(const double *__restrict__ vks, const double *__restrict__ vxc, const int *__restrict__ gpt,
                             const int64_t *__restrict__ goff, const int *__restrict__ ngrid,
                             const int *__restrict__ nlm, const int64_t *__restrict__ g3off,
                             const double *__restrict__ g3d, int nlmmax, double dv, double *__restrict__ prod) {
@@ -555,7 +558,10 @@ __global__ void k_dhat_prod(const double *__restrict__ vks, const int *__restric
   for (int l = 0; l < nlmmax; l++) {
     double acc = 0;
     if (l < L)
-      for (int ig = threadIdx.x; ig < ng; ig += blockDim.x) acc += vks[pts[ig]] * G[ig + (int64_t)ng * l];
+      for (int ig = threadIdx.x; ig < ng; ig += blockDim.x) {
+        const int gp = pts[ig];
+        acc += (vxc ? vks[gp] - vxc[gp] : vks[gp]) * G[ig + (int64_t)ng * l];
+      }
     acc = block_sum(acc, sh);
     if (threadIdx.x == 0) prod[a * nlmmax + l] = acc * dv;
   }
@@ -671,8 +677,8 @@ int dij_step(opaw_ctx *c, int set) {
   OPAW_CHECK(ensure(c->red, sizeof(double) * (2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1) * 2)));
   double *prod = red_scratch(c) + 2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1);
   const int L = c->nlmmax > 0 ? c->nlmmax : 1;
-  k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(c->d_vks[set], c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off,
-                                                c->d_g3d, L, c->dv, prod);
+  k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(c->d_vks[set], c->d_vxc[set], c->d_gpt, c->d_goff, c->d_ngrid,
+                                                c->d_nlm, c->d_g3off, c->d_g3d, L, c->dv, prod);
   k_dij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(prod, L, c->d_rhoij[set], c->d_qijlm, c->d_dij0, c->d_eijkl,
                                                   c->d_ms, c->d_nlm, c->d_doff, c->d_qoff, c->d_eoff,
                                                   c->d_dslot_atom, c->nd, c->dij_max, c->d_dij[set]);
@@ -736,12 +742,12 @@ int vxc_of(opaw_ctx *c, const double *dens, const double *core, double *out) {
   return OPAW_OK;
 }
 
-int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, double *out) {
+int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vxc, double *out) {
   if (c->natom == 0) return OPAW_OK;
   OPAW_CHECK(ensure(c->red, sizeof(double) * (2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1) * 2)));
   double *prod = red_scratch(c) + 2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1);
   const int L = c->nlmmax > 0 ? c->nlmmax : 1;
-  k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(vks, c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off, c->d_g3d, L,
+  k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(vks, vxc, c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off, c->d_g3d, L,
                                                 c->dv, prod);
   k_dij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(prod, L, rhoij, c->d_qijlm, c->d_dij0, c->d_eijkl, c->d_ms, c->d_nlm,
                                                   c->d_doff, c->d_qoff, c->d_eoff, c->d_dslot_atom, c->nd, c->dij_max,

@@ -614,8 +614,11 @@ void orc_vks(orc_ctx *c, int set) {
 
 /* ------------------------------------------------------------------------ */
 /* A16 get_dij: get_dij.f90:13-31,100-155 with the on-site model              */
-/*   D = D0 + D_H(rho) + Dhat[v_ks];  D_H_ij = sum_kl E_ijkl rho_kl ;          */
-/*   Dhat_ij = dv sum_g v_ks(r_g) sum_lm q_ij^lm g_lm(r_g);                    */
+/*   D = D0 + D_H(rho) + Dhat[v_ks - v_xc];  D_H_ij = sum_kl E_ijkl rho_kl ;   */
+/*   Dhat_ij = dv sum_g (v_ks - v_xc)(r_g) sum_lm q_ij^lm g_lm(r_g): get_dij   */
+/*   passes vks and vxc to pawdij, which builds Dhat on vtrial - vxc when the  */
+/*   compensation charge is not in the XC density (usexcnhat = 0,            */
+/*   1_libpaw_mod.f90:49; libpaw/4_m_pawdij.F90:375-385)                      */
 /*   lower triangle mirrored and clamped at dij_max (:140-150)                 */
 /* ------------------------------------------------------------------------ */
 void orc_dij(orc_ctx *c, int set) {
@@ -632,7 +635,7 @@ void orc_dij(orc_ctx *c, int set) {
       double acc = 0;
       for (int ig = 0; ig < ng; ig++) {
         size_t gi = (lg[3 * ig] - 1) + (size_t)c->nx * ((lg[3 * ig + 1] - 1) + (size_t)c->ny * (lg[3 * ig + 2] - 1));
-        acc += c->vks[set][gi] * G[ig + (size_t)ng * l];
+        acc += (c->vks[set][gi] - c->vxc[set][gi]) * G[ig + (size_t)ng * l];
       }
       prod[l] = acc * c->dv;
     }

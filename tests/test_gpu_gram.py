@@ -149,3 +149,34 @@ def test_lowest_states_against_oracle():
     assert np.abs(ev - np.sort(w)).max() < 1e-6, (ev, w)
     r = np.sqrt((np.abs(HX - w[:, None] * X) ** 2).sum(axis=1) * s.dv)
     assert r.max() < 1e-4, r
+
+
+def test_orthonormalize_on_device(spec):
+    """FP64 Cholesky and Loewdin orthonormalisation without a host eigensolve
+    (opaw_orthonormalize_dev): Cholesky gives Psi L^-H, Loewdin Psi G^-1/2,
+    both with an identity Gram matrix; Loewdin refuses orbitals far from
+    orthonormal."""
+    s, c = spec
+    rng = np.random.default_rng(4)
+    Q = synthetic.orbitals(s, 6, seed=9).reshape(6, -1)
+    A = Q + 0.02 * (rng.standard_normal(Q.shape) + 1j * rng.standard_normal(Q.shape)) * np.abs(Q).max()
+    G = A.conj() @ A.T * s.dv
+    w, V = np.linalg.eigh(G)
+    lo = (A.T @ (V @ np.diag(w ** -0.5) @ V.conj().T)).T   # Psi G^-1/2
+    L = np.linalg.cholesky(G)
+    ch = (A.T @ np.linalg.inv(L).conj().T).T                # Psi L^-H
+    for method, ref in ((0, ch), (1, lo)):
+        c.upload(0, A)
+        off = c.orthonormalize(0, method)
+        assert abs(off - np.abs(G - np.eye(6)).max()) < 1e-12
+        X = c.download(0, 6).reshape(6, -1)
+        assert np.abs(X.conj() @ X.T * s.dv - np.eye(6)).max() < 1e-12, method
+        assert rel(X, ref) < 1e-11, method
+    B = rng.standard_normal((6, s.nn)) + 1j * rng.standard_normal((6, s.nn))
+    c.upload(0, B)
+    with pytest.raises(pkg.OpawError) as e:
+        c.orthonormalize(0, 1)
+    assert e.value.status == 1
+    c.orthonormalize(0, 0)
+    X = c.download(0, 6).reshape(6, -1)
+    assert np.abs(X.conj() @ X.T * s.dv - np.eye(6)).max() < 1e-11
