@@ -80,6 +80,21 @@ typedef struct opaw_system {
   const double *dij0;      /* per atom [ms*ms] frozen on-site term D0 */
   const double *eijkl;     /* per atom [ms^4] on-site Hartree tensor: D_H_ij = sum_kl E[i,j,k,l] rho_kl */
   double dij_max;          /* |D_ij| clamp (param_dij_max, 0_parameter.f90:17) */
+  /* On-site exchange-correlation term of D_ij, D_xc = dE_xc/drho_ij of the
+   * one-centre densities (libpaw pawdenpot + pawdij with the first-order
+   * moment development pawxcdev = 1, LDA, nspden = 1: m_paw_denpot.F90:136,
+   * 2_m_pawxc.F90 pawxcm, 4_m_pawdij.F90 pawdijxcm).  rad_n == NULL leaves
+   * the term out.  Per atom, concatenated in atom order: */
+  const int *rad_n;        /* [natom] radial mesh points of the PAW sphere (pawrad%mesh_size) */
+  const double *rad_r;     /* per atom [rad_n] radii r_k > 0 (pawrad%rad) */
+  const double *rad_w;     /* per atom [rad_n] weights: int_0^rpaw f dr = sum_k w_k f(r_k) (simp_gen) */
+  const int *nphi;         /* [natom] radial partial waves (pawtab%basis_size) */
+  const double *phi;       /* per atom [nphi][rad_n] all-electron u(r) = r phi(r) (pawtab%phi) */
+  const double *tphi;      /* per atom [nphi][rad_n] pseudo u~(r) = r phi~(r) (pawtab%tphi) */
+  const double *coredens;  /* per atom [rad_n] core density n_c(r) (pawtab%coredens) */
+  const double *tcoredens; /* per atom [rad_n] pseudo core density (pawtab%tcoredens) */
+  const int *proj_lmn;     /* [3 * sum ms] per projector: l, m (-l..l, real Y_lm of ylm.f90), partial
+                            * wave index (pawtab%indlmn) */
 } opaw_system;
 
 typedef struct opaw_ctx opaw_ctx;
@@ -203,6 +218,10 @@ int opaw_fft3d_dev(opaw_ctx *ctx, int dtype, void *data, int norb, int sign);
  * of orthog_phi.f90:76-111 and the subspace matrices of diag.f90:49-97),
  * complex128 host output, column-major G[i + na*j] */
 int opaw_gram_dev(opaw_ctx *ctx, int dtype, const void *A, int na, const void *B, int nb, double *G);
+/* the same for a result known to be Hermitian (A^H A, or A^H H A with H
+ * Hermitian; n x n): only the tiles on and above the diagonal are summed, the
+ * others are their conjugate mirror images */
+int opaw_gram_herm_dev(opaw_ctx *ctx, int dtype, const void *A, const void *B, int n, double *G);
 /* subspace rotation out_j = sum_i A_i M[i + na*j] (orthog_phi.f90:148-156,
  * diag.f90:118); M complex128 host, column-major; out must differ from A */
 int opaw_rotate_dev(opaw_ctx *ctx, int dtype, const void *A, int na, const double *M, int nb, void *out);

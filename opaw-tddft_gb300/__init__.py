@@ -51,7 +51,47 @@ class OpawSystem(ct.Structure):
         ("ngrid", _I), ("local_grid", _I), ("nlm", _I),
         ("g3d", _D), ("qijlm", _D), ("vloc", _D), ("ncoret", _D),
         ("dij0", _D), ("eijkl", _D), ("dij_max", ct.c_double),
+        ("rad_n", _I), ("rad_r", _D), ("rad_w", _D), ("nphi", _I), ("phi", _D), ("tphi", _D),
+        ("coredens", _D), ("tcoredens", _D), ("proj_lmn", _I),
     ]
+
+
+def system_struct(s):
+    """The opaw_system of a host System and the arrays it points to (keep
+    them alive as long as the struct is used).  Systems without the radial
+    tables of the on-site XC term pass NULL for them."""
+    keep = {}
+
+    def I(name, v):
+        a = _arr(v, np.int32).reshape(-1)
+        keep[name] = a
+        return a.ctypes.data_as(_I)
+
+    def D(name, v):
+        a = _arr(v, np.float64).reshape(-1)
+        keep[name] = a
+        return a.ctypes.data_as(_D)
+
+    st = OpawSystem(
+        s.nx, s.ny, s.nz, s.dx, s.dy, s.dz, s.ekcut, s.scale_vh, s.periodic, s.rnel, s.natom,
+        I("ir_start", s.ir_start), I("nrough", s.nrough), I("ms", s.ms),
+        D("p3d", s.p3d), D("p3d1", s.p3d1), D("s", s.s), D("sinv", s.sinv),
+        I("ngrid", s.ngrid), I("local_grid", s.local_grid), I("nlm", s.nlm),
+        D("g3d", s.g3d), D("qijlm", s.qijlm), D("vloc", s.vloc), D("ncoret", s.ncoret),
+        D("dij0", s.dij0), D("eijkl", s.eijkl), s.dij_max,
+    )
+    rad = getattr(s, "radial", None)
+    if rad is not None:
+        st.rad_n = I("rad_n", rad["rad_n"])
+        st.rad_r = D("rad_r", rad["rad_r"])
+        st.rad_w = D("rad_w", rad["rad_w"])
+        st.nphi = I("nphi", rad["nphi"])
+        st.phi = D("phi", rad["phi"])
+        st.tphi = D("tphi", rad["tphi"])
+        st.coredens = D("coredens", rad["coredens"])
+        st.tcoredens = D("tcoredens", rad["tcoredens"])
+        st.proj_lmn = I("proj_lmn", rad["proj_lmn"])
+    return st, keep
 
 
 # every exported symbol of include/opaw_gb300.h with its ctypes signature
@@ -119,6 +159,7 @@ SIGNATURES = {
     "opaw_net_train": (ct.c_int, [_P, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_double, _P]),
     "opaw_precond_learned_dev": (ct.c_int, [_P, _P, ct.c_int, _P, _P, _P, _P, ct.c_int]),
     "opaw_orthonormalize_dev": (ct.c_int, [_P, ct.c_int, ct.c_int, _P]),
+    "opaw_gram_herm_dev": (ct.c_int, [_P, ct.c_int, _P, _P, ct.c_int, _P]),
     "opaw_ensemble_steps": (ct.c_int, [_P, ct.c_int, ct.c_int, ct.c_double, _P, _P, _P]),
 }
 
@@ -159,26 +200,7 @@ class Context:
     def __init__(self, system):
         self.system = system
         s = system
-        self._keep = {}
-
-        def I(name, v):
-            a = _arr(v, np.int32).reshape(-1)
-            self._keep[name] = a
-            return a.ctypes.data_as(_I)
-
-        def D(name, v):
-            a = _arr(v, np.float64).reshape(-1)
-            self._keep[name] = a
-            return a.ctypes.data_as(_D)
-
-        st = OpawSystem(
-            s.nx, s.ny, s.nz, s.dx, s.dy, s.dz, s.ekcut, s.scale_vh, s.periodic, s.rnel, s.natom,
-            I("ir_start", s.ir_start), I("nrough", s.nrough), I("ms", s.ms),
-            D("p3d", s.p3d), D("p3d1", s.p3d1), D("s", s.s), D("sinv", s.sinv),
-            I("ngrid", s.ngrid), I("local_grid", s.local_grid), I("nlm", s.nlm),
-            D("g3d", s.g3d), D("qijlm", s.qijlm), D("vloc", s.vloc), D("ncoret", s.ncoret),
-            D("dij0", s.dij0), D("eijkl", s.eijkl), s.dij_max,
-        )
+        st, self._keep = system_struct(s)
         self._sys = st
         self._norb = [0, 0]
         self.nkick = 1
@@ -314,6 +336,12 @@ class Context:
     def gram_dev(self, dtype, a_ptr, na, b_ptr, nb):
         out = np.empty((nb, na), np.complex128)  # C order [j][i] == column-major G[i + na j]
         _check(lib().opaw_gram_dev(self.h, dtype, ct.c_void_p(a_ptr), na, ct.c_void_p(b_ptr), nb, _ptr(out)))
+        return out.T
+
+    def gram_herm_dev(self, dtype, a_ptr, b_ptr, n):
+        """dv A^H B for a result known to be Hermitian (upper tiles summed)."""
+        out = np.empty((n, n), np.complex128)
+        _check(lib().opaw_gram_herm_dev(self.h, dtype, ct.c_void_p(a_ptr), ct.c_void_p(b_ptr), n, _ptr(out)))
         return out.T
 
     def rotate_dev(self, dtype, a_ptr, na, M, out_ptr):

@@ -224,6 +224,16 @@ struct opaw_ctx {
   int ncunion = 0;
   int *d_cpt = nullptr, *d_cstart = nullptr, *d_catom = nullptr, *d_cig = nullptr;
 
+  // on-site XC term of D_ij (onsite_xc.cu): radial tables per atom, the
+  // Gaunt coefficients per atom [9][ms][ms], scratch [2][9][radial points]
+  // and the result [nd]
+  int oxc_on = 0;
+  int *oxc_rad_n = nullptr, *oxc_pwave = nullptr;
+  int64_t *oxc_roff = nullptr, *oxc_phioff = nullptr;
+  double *oxc_r = nullptr, *oxc_w = nullptr, *oxc_core = nullptr, *oxc_tcore = nullptr;
+  double *oxc_phi = nullptr, *oxc_tphi = nullptr, *oxc_gaunt = nullptr, *oxc_scratch = nullptr;
+  double *oxc_dxc = nullptr;
+
   // kinetic separable tables: k^2 per axis (double, exact copies of the
   // reference's kx*kx) and float twins
   double *d_k2[3] = {nullptr, nullptr, nullptr};
@@ -348,6 +358,11 @@ int nhat_raw_of(opaw_ctx *c, const double *rhoij, double *out);
 int sums2(opaw_ctx *c, const double *a, const double *b, double *part);
 constexpr int kRedBlocks = 1024;
 int vxc_of(opaw_ctx *c, const double *dens, const double *core, double *out);
+// (onsite_xc.cu) the on-site XC term of D_ij: set-up from the system's
+// radial tables (none given: the term is off), release, and D_xc of rho_ij
+int onsite_init(opaw_ctx *c, const opaw_system *s);
+void onsite_free(opaw_ctx *c);
+int onsite_xc_of(opaw_ctx *c, const double *rhoij, double *dxc);
 // D_ij (get_dij.f90) from rho_ij and the potential v_ks - v_xc of Dhat (vxc may be null)
 int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vxc, double *out);
 // (mixed.cu) nsteps mixed-precision TDDFT steps of the unperturbed set and

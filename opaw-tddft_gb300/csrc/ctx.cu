@@ -347,6 +347,8 @@ static int build(opaw_ctx *c, const opaw_system *s) {
     OPAW_CHECK(upload<double>(&c->d_vh[st], nullptr, c->nn));
     OPAW_CHECK(upload<double>(&c->d_vxc[st], nullptr, c->nn));
   }
+  OPAW_CHECK(onsite_init(c, s));
+  OPAW_CHECK(upload<double>(&c->oxc_dxc, nullptr, c->nd));
   OPAW_CHECK(fft3_init(c->fft, c->nx, c->ny, c->nz));
   OPAW_CHECK(fft3_init(c->fftb, c->nxb, c->nyb, c->nzb));
   OPAW_CUDA(cudaMallocHost(&c->h_red, 4096 * sizeof(double)));
@@ -376,6 +378,8 @@ static void destroy(opaw_ctx *c) {
     for (void *p : sp) cudaFree(p);
   }
   cudaFree(c->d_kgamma);
+  onsite_free(c);
+  cudaFree(c->oxc_dxc);
   for (auto &b : c->work) cudaFree(b.p);
   for (auto &b : c->coef) cudaFree(b.p);
   cudaFree(c->coefr.p);

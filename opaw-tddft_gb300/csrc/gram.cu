@@ -23,12 +23,13 @@ constexpr int kGramSplit = 152; // K splits (one wave of CTAs per output tile ro
 template <typename R>
 __global__ void __launch_bounds__(256) k_gram(const typename Tr<R>::C *__restrict__ A, int na,
                                               const typename Tr<R>::C *__restrict__ B, int nb, int64_t nn,
-                                              double2 *__restrict__ part) {
+                                              double2 *__restrict__ part, int herm) {
   typedef typename Tr<R>::C C;
   __shared__ C sa[kGramTile][kGramK + 1];
   __shared__ C sb[kGramTile][kGramK + 1];
   const int ti = threadIdx.x / kGramTile, tj = threadIdx.x % kGramTile;
   const int i0 = blockIdx.x * kGramTile, j0 = blockIdx.y * kGramTile;
+  if (herm && i0 > j0) return;  // Hermitian result: the tiles below the diagonal are mirrored
   const int z = blockIdx.z, nz = gridDim.z;
   const int64_t k0 = nn * z / nz, k1 = nn * (z + 1) / nz;
   double accx = 0, accy = 0;
@@ -61,19 +62,28 @@ __global__ void __launch_bounds__(256) k_gram(const typename Tr<R>::C *__restric
   if (i < na && j < nb) part[((int64_t)z * na + i) * nb + j] = make_double2(accx, accy);
 }
 
-// G[i + na j] = dv sum_z part[z][i][j] (fixed order)
+// G[i + na j] = dv sum_z part[z][i][j] (fixed order); herm: the entries of
+// tiles below the diagonal are the conjugates of their mirror images
 __global__ void k_gram_reduce(const double2 *__restrict__ part, int nz, int na, int nb, double dv,
-                              double2 *__restrict__ G) {
+                              double2 *__restrict__ G, int herm) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= na * nb) return;
-  const int i = t / nb, j = t % nb;
+  int i = t / nb, j = t % nb;
+  bool cj = false;
+  if (herm && (i / kGramTile) > (j / kGramTile)) {
+    const int q = i;
+    i = j;
+    j = q;
+    cj = true;
+  }
   double sx = 0, sy = 0;
   for (int z = 0; z < nz; z++) {
     const double2 v = part[((int64_t)z * na + i) * nb + j];
     sx += v.x;
     sy += v.y;
   }
-  G[i + (int64_t)na * j] = make_double2(sx * dv, sy * dv);
+  if (cj) G[j + (int64_t)na * i] = make_double2(sx * dv, -sy * dv);
+  else G[i + (int64_t)na * j] = make_double2(sx * dv, sy * dv);
 }
 
 // out_j = sum_i A_i M[i + na j]: 256 grid points x 16 output orbitals per CTA
@@ -128,12 +138,13 @@ __global__ void __launch_bounds__(256) k_rotate(const typename Tr<R>::C *__restr
 }
 
 template <typename R>
-int gram_t(opaw_ctx *c, const typename Tr<R>::C *A, int na, const typename Tr<R>::C *B, int nb, double2 *Gdev) {
+int gram_t(opaw_ctx *c, const typename Tr<R>::C *A, int na, const typename Tr<R>::C *B, int nb, double2 *Gdev,
+           int herm = 0) {
   OPAW_CHECK(ensure(c->gram, sizeof(double2) * (size_t)kGramSplit * na * nb + 16));
   double2 *part = (double2 *)c->gram.p;
   dim3 grid((na + kGramTile - 1) / kGramTile, (nb + kGramTile - 1) / kGramTile, kGramSplit);
-  k_gram<R><<<grid, 256, 0, c->stream>>>(A, na, B, nb, c->nn, part);
-  k_gram_reduce<<<grid1((int64_t)na * nb, 128), 128, 0, c->stream>>>(part, kGramSplit, na, nb, c->dv, Gdev);
+  k_gram<R><<<grid, 256, 0, c->stream>>>(A, na, B, nb, c->nn, part, herm);
+  k_gram_reduce<<<grid1((int64_t)na * nb, 128), 128, 0, c->stream>>>(part, kGramSplit, na, nb, c->dv, Gdev, herm);
   c->launches += 2;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
@@ -323,6 +334,24 @@ int opaw_gram_dev(opaw_ctx *c, int dtype, const void *A, int na, const void *B, 
     return OPAW_ERR_ARG;
   }
   OPAW_CUDA(cudaMemcpyAsync(G, Gd, sizeof(double2) * (size_t)na * nb, cudaMemcpyDeviceToHost, c->stream));
+  OPAW_CUDA(cudaStreamSynchronize(c->stream));
+  return OPAW_OK;
+}
+
+int opaw_gram_herm_dev(opaw_ctx *c, int dtype, const void *A, const void *B, int n, double *G) {
+  if (!c || !A || !B || !G || n <= 0) {
+    set_error("bad arguments");
+    return OPAW_ERR_ARG;
+  }
+  OPAW_CHECK(ensure(c->gramout, sizeof(double2) * (size_t)n * n));
+  double2 *Gd = (double2 *)c->gramout.p;
+  if (dtype == OPAW_C128) OPAW_CHECK(gram_t<double>(c, (const double2 *)A, n, (const double2 *)B, n, Gd, 1));
+  else if (dtype == OPAW_C64) OPAW_CHECK(gram_t<float>(c, (const float2 *)A, n, (const float2 *)B, n, Gd, 1));
+  else {
+    set_error("dtype must be OPAW_C128 or OPAW_C64");
+    return OPAW_ERR_ARG;
+  }
+  OPAW_CUDA(cudaMemcpyAsync(G, Gd, sizeof(double2) * (size_t)n * n, cudaMemcpyDeviceToHost, c->stream));
   OPAW_CUDA(cudaStreamSynchronize(c->stream));
   return OPAW_OK;
 }

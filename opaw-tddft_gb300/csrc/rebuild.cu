@@ -571,7 +571,8 @@ __global__ void k_dij(const double *__restrict__ prod, int nlmmax, const double 
                       const double *__restrict__ q, const double *__restrict__ d0, const double *__restrict__ E,
                       const int *__restrict__ ms, const int *__restrict__ nlm, const int64_t *__restrict__ doff,
                       const int64_t *__restrict__ qoff, const int64_t *__restrict__ eoff,
-                      const int *__restrict__ dslot, int nd, double dmax, double *__restrict__ dij) {
+                      const int *__restrict__ dslot, int nd, double dmax, const double *__restrict__ dxc,
+                      double *__restrict__ dij) {
   const int t = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);  // warp per entry
   const int lane = threadIdx.x & 31;
   if (t >= nd) return;
@@ -590,6 +591,7 @@ __global__ void k_dij(const double *__restrict__ prod, int nlmmax, const double 
   d = warp_allsum(d);
   if (lane != 0) return;
   d += d0[doff[a] + i + m * j];
+  if (dxc) d += dxc[doff[a] + i + m * j];  // on-site XC (pawdijxcm)
   if (dmax > 0 && fabs(d) > dmax) d = d / fabs(d) * dmax;  // get_dij.f90:144
   dij[doff[a] + i + m * j] = d;
   dij[doff[a] + j + m * i] = d;
@@ -679,9 +681,11 @@ int dij_step(opaw_ctx *c, int set) {
   const int L = c->nlmmax > 0 ? c->nlmmax : 1;
   k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(c->d_vks[set], c->d_vxc[set], c->d_gpt, c->d_goff, c->d_ngrid,
                                                 c->d_nlm, c->d_g3off, c->d_g3d, L, c->dv, prod);
+  OPAW_CHECK(onsite_xc_of(c, c->d_rhoij[set], c->oxc_dxc));
   k_dij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(prod, L, c->d_rhoij[set], c->d_qijlm, c->d_dij0, c->d_eijkl,
                                                   c->d_ms, c->d_nlm, c->d_doff, c->d_qoff, c->d_eoff,
-                                                  c->d_dslot_atom, c->nd, c->dij_max, c->d_dij[set]);
+                                                  c->d_dslot_atom, c->nd, c->dij_max,
+                                                  c->oxc_on ? c->oxc_dxc : nullptr, c->d_dij[set]);
   c->launches += 2;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
@@ -749,9 +753,10 @@ int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vx
   const int L = c->nlmmax > 0 ? c->nlmmax : 1;
   k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(vks, vxc, c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off, c->d_g3d, L,
                                                 c->dv, prod);
+  OPAW_CHECK(onsite_xc_of(c, rhoij, c->oxc_dxc));
   k_dij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(prod, L, rhoij, c->d_qijlm, c->d_dij0, c->d_eijkl, c->d_ms, c->d_nlm,
                                                   c->d_doff, c->d_qoff, c->d_eoff, c->d_dslot_atom, c->nd, c->dij_max,
-                                                  out);
+                                                  c->oxc_on ? c->oxc_dxc : nullptr, out);
   c->launches += 2;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;

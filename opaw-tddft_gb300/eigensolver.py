@@ -10,11 +10,13 @@ preconditioned residuals, previous directions), with
 
 * the Teter-Payne-Allan kinetic preconditioner (opaw_precond_kinetic_dev),
   the plain method, or
-* that preconditioner corrected by the learned 3D-conv network
-  (opaw_precond_learned_dev, `learned.Net`).
+* in the complex128 phase, that preconditioner's direction K r together
+  with the one corrected by the learned 3D-conv network, K r + |r| N
+  (opaw_precond_learned_dev, `learned.Net`): both join the basis, so the
+  Rayleigh-Ritz step uses the network's direction as far as it helps.
 
 Every operator runs in libopaw_gb300.so: S^-1/2 H S^-1/2 (opaw_shs_apply_dev),
-the Gram matrices of the Rayleigh-Ritz step (opaw_gram_dev), the subspace
+the Gram matrices of the Rayleigh-Ritz step (opaw_gram_herm_dev), the subspace
 rotations (opaw_rotate_dev), the preconditioners and the kinetic energies
 they scale with; the small dense eigenproblems (3m x 3m) run on the host in
 FP64.  The iteration runs in complex64 until the largest residual is below
@@ -53,10 +55,8 @@ def _rr(ctx, dt, S, HS, m, drop=1e-12):
     matrix (small eigenvalues dropped), the m lowest Ritz pairs.  Returns
     (theta[m], Y [ns, m]) with the Ritz vectors S^T Y."""
     ns = S.shape[0]
-    G = ctx.gram_dev(dt, S.data_ptr(), ns, S.data_ptr(), ns)
-    Hs = ctx.gram_dev(dt, S.data_ptr(), ns, HS.data_ptr(), ns)
-    G = 0.5 * (G + G.conj().T)
-    Hs = 0.5 * (Hs + Hs.conj().T)
+    G = ctx.gram_herm_dev(dt, S.data_ptr(), S.data_ptr(), ns)
+    Hs = ctx.gram_herm_dev(dt, S.data_ptr(), HS.data_ptr(), ns)
     lg, Vg = np.linalg.eigh(G)
     keep = lg > drop * lg.max()
     B = Vg[:, keep] / np.sqrt(lg[keep])[None, :]
@@ -139,15 +139,19 @@ def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbo
                 record.append((X.clone(), R.clone(), np.array(w, np.float64)))
             ekin = ctx.kinetic_energy_dev(dt, X.data_ptr(), m)
             W = torch.empty_like(R)
-            if net is None:
-                ctx.precond_kinetic_dev(dt, R.data_ptr(), ekin, W.data_ptr(), m)
-            else:
-                net.apply(ctx, dt, R.data_ptr(), np.asarray(w, np.float64), ekin, W.data_ptr(), m)
+            ctx.precond_kinetic_dev(dt, R.data_ptr(), ekin, W.data_ptr(), m)
+            if net is not None and dt == pkg.OPAW_C128:
+                # the learned direction joins the kinetic one in the basis
+                # (span[X, K r, K r + |r| N, P]): the Rayleigh-Ritz step takes
+                # what helps, so a poor network cannot stall the iteration
+                WL = torch.empty_like(R)
+                net.apply(ctx, dt, R.data_ptr(), np.asarray(w, np.float64), ekin, WL.data_ptr(), m)
+                W = torch.cat([W, WL])
             # unit columns: the residual directions shrink with convergence
             # and would otherwise fall under the Gram matrix's drop threshold
             W /= torch.sqrt((W.abs() ** 2).sum(dim=1, keepdim=True) * dv).clamp_min(1e-300).to(W.real.dtype)
             HW = torch.empty_like(W)
-            ctx.shs_apply_dev(0, dt, W.data_ptr(), HW.data_ptr(), m)
+            ctx.shs_apply_dev(0, dt, W.data_ptr(), HW.data_ptr(), W.shape[0])
             if P is not None:
                 pn = torch.sqrt((P.abs() ** 2).sum(dim=1, keepdim=True) * dv).clamp_min(1e-300).to(P.real.dtype)
                 P /= pn

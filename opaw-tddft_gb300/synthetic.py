@@ -69,6 +69,9 @@ class System:
     dij_init: np.ndarray | None = None  # [sum ms^2]
     coords: np.ndarray | None = None  # [natom,3] Bohr
     extra: dict = field(default_factory=dict)
+    # radial tables of the on-site XC term (keys of the rad_* / phi / core
+    # fields of opaw_system); None leaves D_xc out
+    radial: dict | None = None
 
     @property
     def nn(self) -> int:
@@ -165,13 +168,15 @@ def build_system(
     comp_rc=None,
     comp_sigma=0.45,
     species=None,
+    onsite_xc=True,
 ):
     """Builds a synthetic system; `n` is (nx, ny, nz) and h the spacing (all
     axes).  ekcut None takes the reference's default cap (`reference_ekcut`);
     0 leaves the kinetic energy uncapped.  `species` (one entry per atom of
     `coords`, keys of SPECIES) gives each atom its own cutoff and projector
     channels; without it every atom has cutoff rc with one s and three p
-    channels per radial width in `alphas`."""
+    channels per radial width in `alphas`.  onsite_xc adds the radial tables
+    of the on-site XC term of D_ij (`radial_tables`)."""
     rng = np.random.default_rng(seed)
     nx, ny, nz = n
     dx = dy = dz = float(h)
@@ -308,6 +313,7 @@ def build_system(
         # Fortran order (i fastest): element (i,j,k,l) at i + m*(j + m*(k + m*l))
         eijkl.append(E.transpose(3, 2, 1, 0).reshape(-1))
 
+    radial = radial_tables(kinds, ms_of, seed + 17) if onsite_xc else None
     sysobj = System(
         nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz, ekcut=float(ekcut),
         scale_vh=int(scale_vh if scale_vh is not None else (1 if periodic else 2)),
@@ -321,9 +327,63 @@ def build_system(
         g3d=np.concatenate(g3d_all), qijlm=np.concatenate(qijlm_all),
         vloc=vks.reshape(-1).copy(), ncoret=ncoret.reshape(-1),
         dij0=np.concatenate(dij0), eijkl=np.concatenate(eijkl),
-        vks0=vks.reshape(-1).copy(), dij_init=np.concatenate(dinit), coords=coords,
+        vks0=vks.reshape(-1).copy(), dij_init=np.concatenate(dinit), coords=coords, radial=radial,
     )
     return sysobj
+
+
+def radial_mesh(rc, n=241, b=5.0):
+    """Log-type mesh of the PAW sphere, r_k = rc (e^{b (k+1)/n} - 1) / (e^b - 1),
+    k = 0..n-1, and Simpson weights in k times dr/dk (n odd)."""
+    k = np.arange(n, dtype=np.float64)
+    e = np.exp(b * (k + 1) / n)
+    r = rc * (e - 1.0) / (np.exp(b) - 1.0)
+    drdk = rc * (b / n) * e / (np.exp(b) - 1.0)
+    w = np.ones(n)
+    w[1:-1:2] = 4.0
+    w[2:-1:2] = 2.0
+    w /= 3.0
+    return r, w * drdk
+
+
+def radial_tables(kinds, ms_of, seed):
+    """Synthetic one-centre data of every atom with the layout of libpaw's
+    pawtab / pawrad: a log mesh of the sphere (radius rc), partial waves per
+    channel width (all-electron u(r) = r^(l+1) e^(-r^2/2a^2) (1 + 0.3
+    e^(-r^2/2(0.3a)^2)), pseudo u~ without the inner bump, both scaled so
+    that int u~^2 dr = 1), a 1s-like core of 2 electrons for carbon-like
+    atoms (none for hydrogen-like ones, whose core is zero) and a smooth
+    pseudo core, and per projector (l, m, partial-wave index) in the order
+    of the projector channels (s channels, then p channels with m = -1, 0, 1
+    for y, z, x)."""
+    rad_n, rad_r, rad_w, nphi, phi, tphi, core, tcore, lmn = [], [], [], [], [], [], [], [], []
+    for kd, m in zip(kinds, ms_of):
+        r, w = radial_mesh(kd["rc"])
+        waves = [(0, a) for a in kd["s_alphas"]] + [(1, a) for a in kd["p_alphas"]]
+        for (l, a) in waves:
+            tu = r ** (l + 1) * np.exp(-r * r / (2 * a * a))
+            u = tu * (1.0 + 0.3 * np.exp(-r * r / (2 * (0.3 * a) ** 2)))
+            nrm = np.sqrt(np.sum(w * tu * tu))
+            phi.append(u / nrm)
+            tphi.append(tu / nrm)
+        ns_ = len(kd["s_alphas"])
+        ch = [(0, 0, i) for i in range(ns_)]
+        for j in range(len(kd["p_alphas"])):
+            ch += [(1, mm, ns_ + j) for mm in (-1, 0, 1)]
+        assert len(ch) == m
+        lmn.extend(ch)
+        rad_n.append(r.size)
+        rad_r.append(r)
+        rad_w.append(w)
+        nphi.append(len(waves))
+        nc = 2.0 if kd.get("valence", 4) >= 4 else 0.0
+        beta = 20.0
+        core.append(nc * (beta / np.pi) ** 1.5 * np.exp(-beta * r * r))
+        tcore.append(0.05 * np.exp(-r * r / (2 * 0.4 ** 2)) * (1.0 if nc > 0 else 0.0))
+    return {"rad_n": np.array(rad_n, np.int32), "rad_r": np.concatenate(rad_r), "rad_w": np.concatenate(rad_w),
+            "nphi": np.array(nphi, np.int32), "phi": np.concatenate(phi), "tphi": np.concatenate(tphi),
+            "coredens": np.concatenate(core), "tcoredens": np.concatenate(tcore),
+            "proj_lmn": np.array(lmn, np.int32).reshape(-1)}
 
 
 # Projector channels of the two elements of the polyacenes, with the counts

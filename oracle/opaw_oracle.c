@@ -164,6 +164,11 @@ typedef struct orc_ctx {
   double *vk;     /* [nb] MT kernel with 1/Nb folded in */
   /* per-set state */
   double *vks[2], *dij[2], *rhoij[2], *dens[2], *nhat[2], *vh[2], *vxc[2];
+  /* on-site XC tables (oxc = 0: the term is off) */
+  int oxc;
+  int *rad_n, *nphi, *proj_lmn;
+  size_t *roff, *phioff;
+  double *rad_r, *rad_w, *phi, *tphi, *core, *tcore;
 } orc_ctx;
 
 static void *dupa(const void *src, size_t bytes) {
@@ -232,6 +237,24 @@ orc_ctx *orc_create(const opaw_system *sys) {
     c->dij[s] = (double *)calloc(c->nd ? c->nd : 1, sizeof(double));
     c->rhoij[s] = (double *)calloc(c->nd ? c->nd : 1, sizeof(double));
   }
+  if (sys->rad_n) {
+    c->oxc = 1;
+    c->rad_n = (int *)dupa(sys->rad_n, sizeof(int) * na);
+    c->nphi = (int *)dupa(sys->nphi, sizeof(int) * na);
+    c->proj_lmn = (int *)dupa(sys->proj_lmn, sizeof(int) * 3 * c->ns);
+    c->roff = (size_t *)calloc(na + 1, sizeof(size_t));
+    c->phioff = (size_t *)calloc(na + 1, sizeof(size_t));
+    for (int a = 0; a < na; a++) {
+      c->roff[a + 1] = c->roff[a] + c->rad_n[a];
+      c->phioff[a + 1] = c->phioff[a] + (size_t)c->nphi[a] * c->rad_n[a];
+    }
+    c->rad_r = (double *)dupa(sys->rad_r, sizeof(double) * c->roff[na]);
+    c->rad_w = (double *)dupa(sys->rad_w, sizeof(double) * c->roff[na]);
+    c->core = (double *)dupa(sys->coredens, sizeof(double) * c->roff[na]);
+    c->tcore = (double *)dupa(sys->tcoredens, sizeof(double) * c->roff[na]);
+    c->phi = (double *)dupa(sys->phi, sizeof(double) * c->phioff[na]);
+    c->tphi = (double *)dupa(sys->tphi, sizeof(double) * c->phioff[na]);
+  }
   orc_ek_prep(c);
   orc_vk_prep(c);
   return c;
@@ -243,6 +266,9 @@ void orc_free(orc_ctx *c) {
                 c->goff, c->g3off, c->qoff, c->eoff, c->local_grid, c->p3d, c->p3d1, c->s,
                 c->sinv, c->g3d, c->qijlm, c->vloc, c->ncoret, c->dij0, c->eijkl, c->ek, c->vk};
   for (size_t i = 0; i < sizeof(ps) / sizeof(ps[0]); i++) free(ps[i]);
+  void *po[] = {c->rad_n, c->nphi, c->proj_lmn, c->roff, c->phioff, c->rad_r, c->rad_w, c->core, c->tcore,
+                c->phi, c->tphi};
+  for (size_t i = 0; i < sizeof(po) / sizeof(po[0]); i++) free(po[i]);
   for (int s = 0; s < 2; s++) {
     free(c->vks[s]); free(c->dens[s]); free(c->nhat[s]); free(c->vh[s]);
     free(c->vxc[s]); free(c->dij[s]); free(c->rhoij[s]);
@@ -613,8 +639,159 @@ void orc_vks(orc_ctx *c, int set) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* A16 get_dij: get_dij.f90:13-31,100-155 with the on-site model              */
-/*   D = D0 + D_H(rho) + Dhat[v_ks - v_xc];  D_H_ij = sum_kl E_ijkl rho_kl ;   */
+/* A16 on-site XC term of libpaw's D_ij (pawdenpot + pawdij with pawxcdev = 1, */
+/* LDA, nspden = 1, usexcnhat = 0; 2_m_pawxc.F90 pawxcm, 4_m_pawdij.F90       */
+/* pawdijxcm): one-centre densities in moments of the real Y_lm               */
+/*   n_L(r) = sum_ij rho_ij u_i u_j / r^2 G^L_ij (+ sqrt(4 pi) n_c, L = 0)      */
+/* potential moments of the first-order development around n_s = n_0/sqrt4pi */
+/*   V_0 = sqrt(4pi) v(n_s) + v''(n_s) sum_{L>0} n_L^2 / (2 sqrt(4pi)),        */
+/*   V_L = v'(n_s) n_L,  v', v'' central differences, relative step 1e-4,     */
+/* and D_xc_ij = sum_L G^L_ij int (V_L u_i u_j - V~_L u~_i u~_j) dr.           */
+/* ------------------------------------------------------------------------ */
+static void orc_ylm2(double x, double y, double z, double *Y) {
+  /* real spherical harmonics, l <= 2, index l^2 + l + m (ylm.f90 order) */
+  const double pi = acos(-1.0);
+  Y[0] = sqrt(1.0 / (4.0 * pi));
+  Y[1] = sqrt(3.0 / (4.0 * pi)) * y;
+  Y[2] = sqrt(3.0 / (4.0 * pi)) * z;
+  Y[3] = sqrt(3.0 / (4.0 * pi)) * x;
+  Y[4] = sqrt(15.0 / (4.0 * pi)) * x * y;
+  Y[5] = sqrt(15.0 / (4.0 * pi)) * y * z;
+  Y[6] = sqrt(5.0 / (16.0 * pi)) * (3.0 * z * z - 1.0);
+  Y[7] = sqrt(15.0 / (4.0 * pi)) * x * z;
+  Y[8] = sqrt(15.0 / (16.0 * pi)) * (x * x - y * y);
+}
+
+/* G[L][a][b] = int Y_L Y_a Y_b dOmega, L < 9, a, b < 4: Gauss-Legendre in
+ * cos(theta) (16 nodes, Newton on P_16) times 32 uniform points in phi,
+ * exact for these polynomial degrees */
+static void orc_gaunt(double *G) {
+  const int nt = 16, np = 32;
+  const double pi = acos(-1.0);
+  for (int e = 0; e < 9 * 16; e++) G[e] = 0.0;
+  for (int i = 0; i < nt; i++) {
+    double t = cos(pi * (i + 0.75) / (nt + 0.5)), d = 1.0, p0 = 1.0, p1 = t;
+    for (int it = 0; it < 100; it++) {
+      p0 = 1.0;
+      p1 = t;
+      for (int k = 2; k <= nt; k++) {
+        double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      d = nt * (t * p1 - p0) / (t * t - 1.0);
+      double dt = p1 / d;
+      t -= dt;
+      if (fabs(dt) < 1e-16) break;
+    }
+    double wt = 2.0 / ((1.0 - t * t) * d * d), st = sqrt(1.0 - t * t);
+    for (int j = 0; j < np; j++) {
+      double ph = 2.0 * pi * j / np, Y[9];
+      orc_ylm2(st * cos(ph), st * sin(ph), t, Y);
+      for (int L = 0; L < 9; L++)
+        for (int a = 0; a < 4; a++)
+          for (int b = 0; b < 4; b++) G[(L * 4 + a) * 4 + b] += wt * (2.0 * pi / np) * Y[L] * Y[a] * Y[b];
+    }
+  }
+}
+
+/* v(n0 + dn) - v(n0) by divided differences of every factor of the LDA
+ * formula (no cancellation of two nearly equal potentials) */
+static void orc_parts(double n, double *u, double *rs, double *s, double *Q, double *dQ, double *lg) {
+  const double A = 0.031091, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382, b4 = 0.49294;
+  *u = cbrt(n);
+  *rs = cbrt(3.0 / (4.0 * acos(-1.0))) / *u;
+  *s = sqrt(*rs);
+  *Q = 2.0 * A * (b1 * *s + b2 * *rs + b3 * *rs * *s + b4 * *rs * *rs);
+  *dQ = 2.0 * A * (0.5 * b1 / *s + b2 + 1.5 * b3 * *s + 2.0 * b4 * *rs);
+  *lg = log1p(1.0 / *Q);
+}
+static double orc_vdiff(double n0, double dn) {
+  const double A = 0.031091, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382, b4 = 0.49294;
+  double n1 = n0 + dn;
+  if (!(n0 > 1e-15) || !(n1 > 1e-15)) return orc_vxc_point(n1) - orc_vxc_point(n0);
+  double u0, r0, s0, Q0, dQ0, l0, u1, r1, s1, Q1, dQ1, l1;
+  orc_parts(n0, &u0, &r0, &s0, &Q0, &dQ0, &l0);
+  orc_parts(n1, &u1, &r1, &s1, &Q1, &dQ1, &l1);
+  double du = dn / (u1 * u1 + u1 * u0 + u0 * u0);
+  double dvx = -cbrt(3.0 / acos(-1.0)) * du;
+  double drs = -cbrt(3.0 / (4.0 * acos(-1.0))) * du / (u1 * u0);
+  double ds = drs / (s1 + s0);
+  double drss = drs * s1 + r0 * ds, drs2 = drs * (r1 + r0);
+  double dQ = 2.0 * A * (b1 * ds + b2 * drs + b3 * drss + b4 * drs2);
+  double ddQ = 2.0 * A * (-0.5 * b1 * ds / (s1 * s0) + 1.5 * b3 * ds + 2.0 * b4 * drs);
+  double dlg = log1p(-dQ / (Q1 * (Q0 + 1.0)));
+  double dec = -2.0 * A * (a1 * drs * l1 + (1.0 + a1 * r0) * dlg);
+  double G0 = Q0 * (Q0 + 1.0), G1 = Q1 * (Q1 + 1.0);
+  double F1 = dQ1 / G1;
+  double dF = (ddQ * G0 - dQ0 * dQ * (Q1 + Q0 + 1.0)) / (G1 * G0);
+  double ddec = -2.0 * A * a1 * dlg + 2.0 * A * (a1 * drs * F1 + (1.0 + a1 * r0) * dF);
+  double dec1 = -2.0 * A * a1 * l1 + 2.0 * A * (1.0 + a1 * r1) * dQ1 / (Q1 * (Q1 + 1.0));
+  return dvx + dec - (drs * dec1 + r0 * ddec) / 3.0;
+}
+
+void orc_onsite_xc(orc_ctx *c, const double *rho, double *dxc) {
+  double gl[9 * 16];
+  orc_gaunt(gl);
+  const double sq4pi = sqrt(4.0 * acos(-1.0)), delta = 1e-4;
+  for (int a = 0; a < c->natom; a++) {
+    int m = c->ms[a], nr = c->rad_n[a];
+    const double *R = rho + c->doff[a], *r = c->rad_r + c->roff[a], *w = c->rad_w + c->roff[a];
+    const int *lmn = c->proj_lmn + 3 * c->soff[a];
+    double *V = (double *)calloc((size_t)2 * 9 * nr, sizeof(double));
+    for (int sdx = 0; sdx < 2; sdx++) {
+      const double *U = (sdx ? c->tphi : c->phi) + c->phioff[a];
+      const double *core = (sdx ? c->tcore : c->core) + c->roff[a];
+      for (int k = 0; k < nr; k++) {
+        double n[9] = {0};
+        for (int i = 0; i < m; i++)
+          for (int j = 0; j < m; j++) {
+            int ai = lmn[3 * i] * lmn[3 * i] + lmn[3 * i] + lmn[3 * i + 1];
+            int aj = lmn[3 * j] * lmn[3 * j] + lmn[3 * j] + lmn[3 * j + 1];
+            double f = R[i + (size_t)m * j] * U[(size_t)lmn[3 * i + 2] * nr + k] * U[(size_t)lmn[3 * j + 2] * nr + k] /
+                       (r[k] * r[k]);
+            for (int L = 0; L < 9; L++) n[L] += f * gl[(L * 4 + ai) * 4 + aj];
+          }
+        n[0] += sq4pi * core[k];
+        double up = 0.5 * n[0] / sq4pi; /* spin density, kept >= xc_denpos */
+        if (up < 1e-14) up = 1e-14;
+        double ns = 2.0 * up, v0 = orc_vxc_point(ns), h = (ns + delta * ns) - ns, d1 = 0.0, d2 = 0.0; /* ns +- h exact */
+        if (up > 1e-14) { /* (v+ - v-) / 2h, (v+ + v- - 2 v0) / h^2 from dp = v+ - v0, dm = v0 - v- */
+          double dp = orc_vdiff(ns, h), dm = -orc_vdiff(ns, -h);
+          d1 = (dp + dm) / (2.0 * h);
+          d2 = (dp - dm) / (h * h);
+        }
+        double v1 = 0.0;
+        for (int L = 1; L < 9; L++) v1 += n[L] * n[L];
+        double *Vs = V + (size_t)sdx * 9 * nr;
+        Vs[k] = v0 * sq4pi + v1 * d2 / (2.0 * sq4pi);
+        for (int L = 1; L < 9; L++) Vs[(size_t)L * nr + k] = d1 * n[L];
+      }
+    }
+    const double *U0 = c->phi + c->phioff[a], *U1 = c->tphi + c->phioff[a];
+    for (int j = 0; j < m; j++)
+      for (int i = 0; i <= j; i++) {
+        int ai = lmn[3 * i] * lmn[3 * i] + lmn[3 * i] + lmn[3 * i + 1];
+        int aj = lmn[3 * j] * lmn[3 * j] + lmn[3 * j] + lmn[3 * j + 1];
+        double acc = 0.0;
+        for (int k = 0; k < nr; k++) {
+          double pp = U0[(size_t)lmn[3 * i + 2] * nr + k] * U0[(size_t)lmn[3 * j + 2] * nr + k];
+          double tt = U1[(size_t)lmn[3 * i + 2] * nr + k] * U1[(size_t)lmn[3 * j + 2] * nr + k];
+          double sm = 0.0;
+          for (int L = 0; L < 9; L++)
+            sm += gl[(L * 4 + ai) * 4 + aj] * (V[(size_t)L * nr + k] * pp - V[(size_t)(9 + L) * nr + k] * tt);
+          acc += w[k] * sm;
+        }
+        dxc[c->doff[a] + i + (size_t)m * j] = acc;
+        dxc[c->doff[a] + j + (size_t)m * i] = acc;
+      }
+    free(V);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* A16 get_dij: get_dij.f90:13-31,100-155                                     */
+/*   D = D0 + D_H(rho) + D_xc(rho) + Dhat[v_ks - v_xc];  D_H_ij = sum_kl E_ijkl rho_kl ;   */
 /*   Dhat_ij = dv sum_g (v_ks - v_xc)(r_g) sum_lm q_ij^lm g_lm(r_g): get_dij   */
 /*   passes vks and vxc to pawdij, which builds Dhat on vtrial - vxc when the  */
 /*   compensation charge is not in the XC density (usexcnhat = 0,            */
@@ -622,6 +799,11 @@ void orc_vks(orc_ctx *c, int set) {
 /*   lower triangle mirrored and clamped at dij_max (:140-150)                 */
 /* ------------------------------------------------------------------------ */
 void orc_dij(orc_ctx *c, int set) {
+  double *dxc = NULL;
+  if (c->oxc) {
+    dxc = (double *)calloc(c->nd ? c->nd : 1, sizeof(double));
+    orc_onsite_xc(c, c->rhoij[set], dxc);
+  }
   for (int a = 0; a < c->natom; a++) {
     int m = c->ms[a], L = c->nlm[a], ng = c->ngrid[a];
     const double *R = c->rhoij[set] + c->doff[a];
@@ -647,12 +829,14 @@ void orc_dij(orc_ctx *c, int set) {
           for (int k = 0; k < m; k++)
             d += E[i + (size_t)m * (j + (size_t)m * (k + (size_t)m * l2))] * R[k + (size_t)m * l2];
         for (int l = 0; l < L; l++) d += prod[l] * Q[l + (size_t)L * (i + (size_t)m * j)];
+        if (dxc) d += dxc[c->doff[a] + i + (size_t)m * j];
         double mx = c->sys.dij_max;
         if (mx > 0 && fabs(d) > mx) d = d / fabs(d) * mx; /* :144 */
         D[i + (size_t)m * j] = d;
         D[j + (size_t)m * i] = d;
       }
   }
+  free(dxc);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -56,6 +56,7 @@ def lib():
             "orc_rk4_prop_shs": (None, [_P, _P, _P, ct.c_int, ct.c_double]),
             "orc_tddft_steps": (None, [_P, _P, _P, ct.c_int, ct.c_int, ct.c_double, ct.c_double, _P]),
             "orc_nthreads": (ct.c_int, []),
+            "orc_onsite_xc": (None, [_P, _P, _P]),
         }
         for n, (r, a) in sig.items():
             f = getattr(L, n)
@@ -108,26 +109,7 @@ class Oracle:
 
         self.system = system
         s = system
-        keep = {}
-
-        def I(n, v):
-            a = _c(v, np.int32).reshape(-1)
-            keep[n] = a
-            return a.ctypes.data_as(ct.POINTER(ct.c_int))
-
-        def D(n, v):
-            a = _c(v, np.float64).reshape(-1)
-            keep[n] = a
-            return a.ctypes.data_as(ct.POINTER(ct.c_double))
-
-        st = pkg.OpawSystem(
-            s.nx, s.ny, s.nz, s.dx, s.dy, s.dz, s.ekcut, s.scale_vh, s.periodic, s.rnel, s.natom,
-            I("ir_start", s.ir_start), I("nrough", s.nrough), I("ms", s.ms),
-            D("p3d", s.p3d), D("p3d1", s.p3d1), D("s", s.s), D("sinv", s.sinv),
-            I("ngrid", s.ngrid), I("local_grid", s.local_grid), I("nlm", s.nlm),
-            D("g3d", s.g3d), D("qijlm", s.qijlm), D("vloc", s.vloc), D("ncoret", s.ncoret),
-            D("dij0", s.dij0), D("eijkl", s.eijkl), s.dij_max,
-        )
+        st, keep = pkg.system_struct(s)
         self._keep = keep
         self._st = st
         self.h = lib().orc_create(ct.byref(st))
@@ -231,6 +213,13 @@ class Oracle:
 
     def dij(self, set_=0):
         lib().orc_dij(self.h, set_)
+
+    def onsite_xc(self, rhoij):
+        """The on-site XC term D_xc of the given rho_ij [sum ms^2]."""
+        r = _c(rhoij, np.float64)
+        out = np.zeros_like(r)
+        lib().orc_onsite_xc(self.h, _p(r), _p(out))
+        return out
 
     def rebuild(self, psibar, set_=0):
         a = _c(psibar, np.complex128)

@@ -180,3 +180,23 @@ def test_orthonormalize_on_device(spec):
     c.orthonormalize(0, 0)
     X = c.download(0, 6).reshape(6, -1)
     assert np.abs(X.conj() @ X.T * s.dv - np.eye(6)).max() < 1e-11
+
+
+def test_gram_hermitian_form(spec):
+    """opaw_gram_herm_dev sums only the tiles on and above the diagonal and
+    mirrors the rest: it equals the full Gram of A^H A, and the Hermitian
+    part of A^H (H A), 40 orbitals (three tiles per side)."""
+    torch = pytest.importorskip("torch")
+    s, c = spec
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((40, s.nn)) + 1j * rng.standard_normal((40, s.nn))
+    a = torch.from_numpy(A).cuda()
+    ha = torch.empty_like(a)
+    c.shs_apply_dev(0, pkg.OPAW_C128, a.data_ptr(), ha.data_ptr(), 40)
+    c.sync()
+    G = c.gram_dev(pkg.OPAW_C128, a.data_ptr(), 40, a.data_ptr(), 40)
+    Gh = c.gram_herm_dev(pkg.OPAW_C128, a.data_ptr(), a.data_ptr(), 40)
+    assert rel(Gh, G) < 1e-13 and np.abs(Gh - Gh.conj().T).max() < 1e-13 * np.abs(G).max()
+    H = c.gram_dev(pkg.OPAW_C128, a.data_ptr(), 40, ha.data_ptr(), 40)
+    Hh = c.gram_herm_dev(pkg.OPAW_C128, a.data_ptr(), ha.data_ptr(), 40)
+    assert rel(Hh, 0.5 * (H + H.conj().T)) < 1e-11
