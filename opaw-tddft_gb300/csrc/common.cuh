@@ -228,7 +228,8 @@ struct opaw_ctx {
   // Gaunt coefficients per atom [9][ms][ms], scratch [2][9][radial points]
   // and the result [nd]
   int oxc_on = 0;
-  int *oxc_rad_n = nullptr, *oxc_pwave = nullptr;
+  int *oxc_rad_n = nullptr, *oxc_pwave = nullptr, *oxc_nphi = nullptr;
+  int oxc_nchunk = 1;
   int64_t *oxc_roff = nullptr, *oxc_phioff = nullptr;
   double *oxc_r = nullptr, *oxc_w = nullptr, *oxc_core = nullptr, *oxc_tcore = nullptr;
   double *oxc_phi = nullptr, *oxc_tphi = nullptr, *oxc_gaunt = nullptr, *oxc_scratch = nullptr;
@@ -369,6 +370,7 @@ int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vx
 // the c->nkick kicked sets (strengths gamma_dev[k]); 3 + 6 nkick doubles per
 // step into dd_dev: dip, then dip'_k and d_dip_k of every kick
 int mixed_steps(opaw_ctx *c, int nsteps, double dt, const double *gamma_dev, double *dd_dev);
+int ensemble_steps(opaw_ctx *const *cs, int n, int nsteps, double dt, double *const *dd, double *const *fixed);
 // LDA potential of n points (device arrays)
 int vxc_points(opaw_ctx *c, const double *dens, double *vxc, int64_t n);
 // gout = 1/N ifft(bk fft(a)) on the context's main FFT plan; a is overwritten

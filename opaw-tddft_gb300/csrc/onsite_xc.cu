@@ -17,13 +17,14 @@
 //   V_0 = sqrt(4 pi) v(n_s) + (1/2) v''(n_s) sum_{L>0} n_L^2 / sqrt(4 pi),
 //   V_L = v'(n_s) n_L   (L > 0),
 //
-// v the LDA potential (Slater + PW92), v' and v'' central finite differences
-// with the relative step 1e-4 as pawxcm takes them (formed from
-// cancellation-free potential differences, oxc_vdiff); the pseudo part V~ is
-// the same with u~ and the pseudo core (the compensation charge is not in the
+// v the LDA potential (Slater + PW92), v' and v'' pawxcm's central finite
+// differences with the relative step 1e-4 (evaluated from the potential's
+// power series around n_s, oxc_vxc_series); the pseudo part V~ is the same
+// with u~ and the pseudo core (the compensation charge is not in the
 // XC density, usexcnhat = 0).  G^L_ij = int Y_L Y_i Y_j dOmega, real Y_lm in
 // the ylm.f90 order.  Projectors with l <= 1 (s and p partial waves, those of
 // the reference's datasets) are supported: L <= 2, 9 moments.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -101,69 +102,123 @@ static void gaunt_l1(double *G) {
     if (std::fabs(G[e]) < 1e-14) G[e] = 0.0;
 }
 
-// LDA v_xc of the total density (Slater + PW92, the formula of vxc_point in
-// rebuild.cu)
-__device__ __forceinline__ double oxc_vxc(double n) {
-  if (!(n > 1e-15)) return 0.0;
-  const double pi = 3.14159265358979323846;
-  const double vx = -cbrt(3.0 * n / pi);
-  const double A = 0.031091, a1 = 0.21370, b1 = 7.5957, b2 = 3.5876, b3 = 1.6382, b4 = 0.49294;
-  const double rs = cbrt(3.0 / (4.0 * pi * n));
-  const double srs = sqrt(rs);
-  const double Q = 2.0 * A * (b1 * srs + b2 * rs + b3 * rs * srs + b4 * rs * rs);
-  const double dQ = 2.0 * A * (0.5 * b1 / srs + b2 + 1.5 * b3 * srs + 2.0 * b4 * rs);
-  const double lg = log(1.0 + 1.0 / Q);
-  const double ec = -2.0 * A * (1.0 + a1 * rs) * lg;
-  const double dec = -2.0 * A * a1 * lg + 2.0 * A * (1.0 + a1 * rs) * dQ / (Q * Q + Q);
-  return vx + (ec - rs / 3.0 * dec);
+constexpr double kPwA = 0.031091, kPwA1 = 0.21370, kPwB1 = 7.5957, kPwB2 = 3.5876, kPwB3 = 1.6382, kPwB4 = 0.49294;
+
+// The same LDA potential as a truncated power series in the relative density
+// change x = dn / n0, v(n0 (1 + x)) = sum_{k <= 4} v_k x^k (Taylor-mode
+// arithmetic: rs, sqrt(rs) and n^(1/3) are binomial series of (1 + x)^p, Q a
+// combination of them, log1p(1/Q) and the quotients by the recurrences of
+// series division and logarithm).  pawxcm's central differences with the step
+// h = t n0 are then, exactly up to the truncated order x^5 (t^4 = 1e-16),
+//   (v(n0 + h) - v(n0 - h)) / 2h        = (v_1 + v_3 t^2) / n0,
+//   (v(n0 + h) + v(n0 - h) - 2 v0) / h^2 = 2 (v_2 + v_4 t^2) / n0^2,
+// from one cube root, one square root and one log1p per point instead of
+// three evaluations of the potential, and without the rounding the
+// differences amplify.
+constexpr int kTs = 5;
+struct Ts {
+  double c[kTs];
+};
+__device__ __forceinline__ Ts ts_pow1p(double scale, double p) {  // scale (1 + x)^p
+  Ts r;
+  double b = scale;
+#pragma unroll
+  for (int k = 0; k < kTs; k++) {
+    r.c[k] = b;
+    b *= (p - k) / (k + 1);
+  }
+  return r;
+}
+__device__ __forceinline__ Ts ts_mul(const Ts &a, const Ts &b) {
+  Ts r;
+#pragma unroll
+  for (int k = 0; k < kTs; k++) {
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j <= k; j++) acc += a.c[j] * b.c[k - j];
+    r.c[k] = acc;
+  }
+  return r;
+}
+__device__ __forceinline__ Ts ts_recip(const Ts &a) {
+  Ts r;
+  const double i0 = 1.0 / a.c[0];
+  r.c[0] = i0;
+#pragma unroll
+  for (int k = 1; k < kTs; k++) {
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 1; j <= k; j++) acc += a.c[j] * r.c[k - j];
+    r.c[k] = -acc * i0;
+  }
+  return r;
+}
+// log(g) with log(g_0) given
+__device__ __forceinline__ Ts ts_log(const Ts &g, double f0) {
+  Ts f;
+  f.c[0] = f0;
+  const double i0 = 1.0 / g.c[0];
+#pragma unroll
+  for (int k = 1; k < kTs; k++) {
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 1; j < k; j++) acc += j * f.c[j] * g.c[k - j];
+    f.c[k] = (g.c[k] - acc / k) * i0;
+  }
+  return f;
+}
+__device__ __forceinline__ Ts ts_axpy(double a, const Ts &x, const Ts &y) {  // a x + y
+  Ts r;
+#pragma unroll
+  for (int k = 0; k < kTs; k++) r.c[k] = fma(a, x.c[k], y.c[k]);
+  return r;
 }
 
-// v(n + dn) - v(n) of the same LDA without the cancellation of two nearly
-// equal potentials: divided differences of every factor of the formula (the
-// FP64 form of vxc_pair_f in mixed.cu).  The finite-difference derivatives of
-// pawxcm are formed from these differences, so their cancellation costs a
-// factor 1/step instead of 1/step^2 of the rounding.
-struct OxcParts {
-  double u, rs, s, Q, dQ, lg;
-};
-constexpr double kPwA = 0.031091, kPwA1 = 0.21370, kPwB1 = 7.5957, kPwB2 = 3.5876, kPwB3 = 1.6382, kPwB4 = 0.49294;
-__device__ __forceinline__ OxcParts oxc_parts(double n) {
-  OxcParts p;
-  p.u = cbrt(n);
-  p.rs = 0.62035049089940001 / p.u;  // (3/(4 pi))^(1/3) / n^(1/3)
-  p.s = sqrt(p.rs);
-  p.Q = 2.0 * kPwA * (kPwB1 * p.s + kPwB2 * p.rs + kPwB3 * p.rs * p.s + kPwB4 * p.rs * p.rs);
-  p.dQ = 2.0 * kPwA * (0.5 * kPwB1 / p.s + kPwB2 + 1.5 * kPwB3 * p.s + 2.0 * kPwB4 * p.rs);
-  p.lg = log1p(1.0 / p.Q);
-  return p;
+// v_0 .. v_4 of the LDA potential around n0 in x = dn / n0
+__device__ __forceinline__ Ts oxc_vxc_series(double n0) {
+  const double u0 = cbrt(n0);
+  const double rs0 = 0.62035049089940001 / u0;  // (3/(4 pi))^(1/3) / n^(1/3)
+  const double s0 = sqrt(rs0);
+  const Ts u = ts_pow1p(u0, 1.0 / 3.0);
+  const Ts rs = ts_pow1p(rs0, -1.0 / 3.0);
+  const Ts sr = ts_pow1p(s0, -1.0 / 6.0);           // sqrt(rs)
+  const Ts rss = ts_pow1p(rs0 * s0, -0.5);          // rs^(3/2)
+  const Ts rs2 = ts_pow1p(rs0 * rs0, -2.0 / 3.0);   // rs^2
+  const Ts isr = ts_pow1p(1.0 / s0, 1.0 / 6.0);     // rs^(-1/2)
+  Ts Q, dQ;
+#pragma unroll
+  for (int k = 0; k < kTs; k++) {
+    Q.c[k] = 2.0 * kPwA * (kPwB1 * sr.c[k] + kPwB2 * rs.c[k] + kPwB3 * rss.c[k] + kPwB4 * rs2.c[k]);
+    dQ.c[k] = 2.0 * kPwA * (0.5 * kPwB1 * isr.c[k] + 1.5 * kPwB3 * sr.c[k] + 2.0 * kPwB4 * rs.c[k]);
+  }
+  dQ.c[0] += 2.0 * kPwA * kPwB2;
+  // lg = log1p(1/Q) = log(1 + 1/Q)
+  Ts T = ts_recip(Q);
+  T.c[0] += 1.0;
+  const Ts lg = ts_log(T, log1p(1.0 / Q.c[0]));
+  Ts onea = rs;  // 1 + a1 rs
+#pragma unroll
+  for (int k = 0; k < kTs; k++) onea.c[k] *= kPwA1;
+  onea.c[0] += 1.0;
+  const Ts QQ = ts_mul(Q, ts_axpy(1.0, Q, Ts{{1.0, 0.0, 0.0, 0.0, 0.0}}));  // Q (Q + 1)
+  const Ts F = ts_mul(dQ, ts_recip(QQ));
+  const Ts ec = ts_mul(onea, lg);               // / (-2A)
+  const Ts dec2 = ts_mul(onea, F);              // dec = -2A a1 lg + 2A dec2
+  const Ts rsdec = ts_mul(rs, ts_axpy(-kPwA1, lg, dec2));  // rs dec / 2A
+  Ts v;
+#pragma unroll
+  for (int k = 0; k < kTs; k++)
+    v.c[k] = -0.98474502184269641 * u.c[k] - 2.0 * kPwA * ec.c[k] - 2.0 * kPwA * rsdec.c[k] / 3.0;
+  return v;
 }
-__device__ __forceinline__ double oxc_dec(const OxcParts &p) {  // d eps_c / d rs
-  return -2.0 * kPwA * kPwA1 * p.lg + 2.0 * kPwA * (1.0 + kPwA1 * p.rs) * p.dQ / (p.Q * (p.Q + 1.0));
-}
-__device__ double oxc_vdiff(double n0, double dn) {
-  const double n1 = n0 + dn;
-  if (!(n0 > 1e-15) || !(n1 > 1e-15)) return oxc_vxc(n1) - oxc_vxc(n0);
-  const OxcParts p0 = oxc_parts(n0), p1 = oxc_parts(n1);
-  const double du = dn / (p1.u * p1.u + p1.u * p0.u + p0.u * p0.u);
-  const double dvx = -0.98474502184269641 * du;  // (3/pi)^(1/3)
-  const double drs = -0.62035049089940001 * du / (p1.u * p0.u);
-  const double ds = drs / (p1.s + p0.s);
-  const double drss = drs * p1.s + p0.rs * ds;
-  const double drs2 = drs * (p1.rs + p0.rs);
-  const double dQ = 2.0 * kPwA * (kPwB1 * ds + kPwB2 * drs + kPwB3 * drss + kPwB4 * drs2);
-  const double ddQ = 2.0 * kPwA * (-0.5 * kPwB1 * ds / (p1.s * p0.s) + 1.5 * kPwB3 * ds + 2.0 * kPwB4 * drs);
-  const double dlg = log1p(-dQ / (p1.Q * (p0.Q + 1.0)));
-  const double dec = -2.0 * kPwA * (kPwA1 * drs * p1.lg + (1.0 + kPwA1 * p0.rs) * dlg);
-  const double G0 = p0.Q * (p0.Q + 1.0), G1 = p1.Q * (p1.Q + 1.0);
-  const double F1 = p1.dQ / G1;
-  const double dF = (ddQ * G0 - p0.dQ * dQ * (p1.Q + p0.Q + 1.0)) / (G1 * G0);
-  const double ddec = -2.0 * kPwA * kPwA1 * dlg + 2.0 * kPwA * (kPwA1 * drs * F1 + (1.0 + kPwA1 * p0.rs) * dF);
-  return dvx + dec - (drs * oxc_dec(p1) + p0.rs * ddec) / 3.0;
-}
+
+constexpr int kOxcMaxW = 6;                          // partial waves per atom
+constexpr int kOxcMaxP = kOxcMaxW * (kOxcMaxW + 1) / 2;  // unordered wave pairs
+constexpr int kOxcChunk = 64;                        // radial points per CTA
 
 struct OxcTabs {
-  const int *rad_n;
-  const int64_t *roff;     // per atom offset into r, w, core, tcore, and of the scratch (x 2 kOxcL)
+  const int *rad_n, *nphi;
+  const int64_t *roff;     // per atom offset into r, w, core, tcore
   const double *r, *w, *core, *tcore;
   const int64_t *phioff;   // per atom offset into phi, tphi
   const double *phi, *tphi;
@@ -171,91 +226,137 @@ struct OxcTabs {
   const double *gaunt;     // per atom [kOxcL][ms][ms]
   const int *ms;
   const int64_t *doff, *soff;
+  const int *dslot;        // atom of every D_ij entry
+  int nchunk;              // radial chunks of the longest mesh
 };
 
-__device__ __forceinline__ double oxc_warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+// index of the unordered wave pair (a, b) among the nw (nw + 1) / 2
+__device__ __forceinline__ int oxc_pair(int a, int b, int nw) {
+  if (a > b) {
+    const int t = a;
+    a = b;
+    b = t;
+  }
+  return a * nw - a * (a - 1) / 2 + (b - a);
 }
 
-// One CTA per atom.  Phase 1: the potential moments V_L(r_k) of the
-// all-electron and pseudo one-centre densities into the scratch [2][L][k];
-// phase 2: D_xc_ij, a warp per (i <= j), in a fixed order.
-__global__ void __launch_bounds__(256) k_onsite_xc(OxcTabs T, const double *__restrict__ rho,
-                                                   double *__restrict__ scratch, double *__restrict__ dxc) {
-  const int a = blockIdx.x;
-  const int m = T.ms[a], nr = T.rad_n[a];
+// Partial integrals of the potential moments over one radial chunk of one
+// part (all-electron s = 0, pseudo s = 1) of one atom, in wave pairs:
+//
+//   I^L_ab = sum_{k in chunk} w_k V_L(r_k) u_a(r_k) u_b(r_k),
+//
+// with n_L(r) = sum_ab C^L_ab u_a u_b / r^2 (+ sqrt(4 pi) n_c),
+// C^L_ab = sum_{ij: {pw_i, pw_j} = {a, b}} rho_ij G^L_ij: the moments and the
+// integrals run over wave pairs (at most 21) instead of projector pairs
+// (64 for 8 projectors), the FP64 work is spread over (atom, part, chunk)
+// CTAs, and every sum runs in a fixed order.
+__global__ void __launch_bounds__(kOxcChunk) k_oxc_radial(OxcTabs T, const double *__restrict__ rho,
+                                                          double *__restrict__ part) {
+  const int a = blockIdx.x, s = blockIdx.y, ch = blockIdx.z, t = threadIdx.x;
+  const int m = T.ms[a], nr = T.rad_n[a], nw = T.nphi[a], np = nw * (nw + 1) / 2;
+  if (ch * kOxcChunk >= nr) return;
+  __shared__ double C[kOxcL][kOxcMaxP];
+  __shared__ double Vw[kOxcL][kOxcChunk];
+  __shared__ double Us[kOxcMaxW][kOxcChunk];
   const double *R = rho + T.doff[a];
   const double *G = T.gaunt + (int64_t)kOxcL * T.doff[a];
-  const double *r = T.r + T.roff[a], *w = T.w + T.roff[a];
   const int *pw = T.pwave + T.soff[a];
-  double *V = scratch + 2 * kOxcL * T.roff[a];
-  const double sq4pi = 3.5449077018110318;  // sqrt(4 pi)
-  for (int k = threadIdx.x; k < nr; k += blockDim.x) {
-    for (int s = 0; s < 2; s++) {
-      const double *U = (s ? T.tphi : T.phi) + T.phioff[a];
-      double n[kOxcL];
-#pragma unroll
-      for (int L = 0; L < kOxcL; L++) n[L] = 0.0;
-      const double inv_r2 = 1.0 / (r[k] * r[k]);
-      for (int j = 0; j < m; j++) {
-        const double uj = U[(int64_t)pw[j] * nr + k];
-        for (int i = 0; i < m; i++) {
-          const double f = R[i + m * j] * U[(int64_t)pw[i] * nr + k] * uj * inv_r2;
-#pragma unroll
-          for (int L = 0; L < kOxcL; L++) n[L] += f * G[(L * m + i) * m + j];
-        }
-      }
-      n[0] += sq4pi * (s ? T.tcore : T.core)[T.roff[a] + k];
-      double up = 0.5 * n[0] / sq4pi;  // spin density of the spherical part
-      if (up < kOxcDenPos) up = kOxcDenPos;
-      const double ns = 2.0 * up;
-      // the step is taken as the difference of two doubles, so that
-      // ns + h and ns - h are exact and the divided differences see the
-      // steps they divide by
-      const double v0 = oxc_vxc(ns), h = (ns + kOxcDelta * ns) - ns;
-      double d1 = 0.0, d2 = 0.0;
-      if (up > kOxcRhoMin) {
-        // (v+ - v-) / 2h and (v+ + v- - 2 v0) / h^2 of pawxcm from the
-        // differences dp = v+ - v0, dm = v0 - v-
-        const double dp = oxc_vdiff(ns, h), dm = -oxc_vdiff(ns, -h);
-        d1 = (dp + dm) / (2.0 * h);
-        d2 = (dp - dm) / (h * h);
-      }
-      double v1sum = 0.0;
-#pragma unroll
-      for (int L = 1; L < kOxcL; L++) v1sum += n[L] * n[L];
-      double *Vs = V + (int64_t)s * kOxcL * nr;
-      Vs[k] = v0 * sq4pi + v1sum * d2 / (2.0 * sq4pi);
-#pragma unroll
-      for (int L = 1; L < kOxcL; L++) Vs[(int64_t)L * nr + k] = d1 * n[L];
-    }
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const double *U0 = T.phi + T.phioff[a], *U1 = T.tphi + T.phioff[a];
-  for (int e = warp; e < m * m; e += nw) {
-    const int i = e % m, j = e / m;
-    if (i > j) continue;
+  for (int e = t; e < kOxcL * np; e += blockDim.x) {
+    const int L = e / np, p = e % np;
     double acc = 0.0;
-    for (int k = lane; k < nr; k += 32) {
-      const double pp = U0[(int64_t)pw[i] * nr + k] * U0[(int64_t)pw[j] * nr + k];
-      const double tt = U1[(int64_t)pw[i] * nr + k] * U1[(int64_t)pw[j] * nr + k];
-      double s = 0.0;
-#pragma unroll
-      for (int L = 0; L < kOxcL; L++) {
-        const double g = G[(L * m + i) * m + j];
-        s += g * (V[(int64_t)L * nr + k] * pp - V[(int64_t)(kOxcL + L) * nr + k] * tt);
-      }
-      acc += w[k] * s;
-    }
-    acc = oxc_warp_sum(acc);
-    if (lane == 0) {
-      dxc[T.doff[a] + i + m * j] = acc;
-      dxc[T.doff[a] + j + m * i] = acc;
-    }
+    for (int j = 0; j < m; j++)
+      for (int i = 0; i < m; i++)
+        if (oxc_pair(pw[i], pw[j], nw) == p) acc += R[i + m * j] * G[(L * m + i) * m + j];
+    C[L][p] = acc;
   }
+  const int k = ch * kOxcChunk + t;
+  const bool valid = k < nr;
+  const double *U = (s ? T.tphi : T.phi) + T.phioff[a];
+  for (int wv = 0; wv < nw; wv++) Us[wv][t] = valid ? U[(int64_t)wv * nr + k] : 0.0;
+  __syncthreads();
+  double V[kOxcL];
+#pragma unroll
+  for (int L = 0; L < kOxcL; L++) V[L] = 0.0;
+  if (valid) {
+    const double sq4pi = 3.5449077018110318;  // sqrt(4 pi)
+    const double rk = T.r[T.roff[a] + k];
+    const double inv_r2 = 1.0 / (rk * rk);
+    double n[kOxcL];
+#pragma unroll
+    for (int L = 0; L < kOxcL; L++) n[L] = 0.0;
+    for (int wa = 0; wa < nw; wa++)
+      for (int wb = wa; wb < nw; wb++) {
+        const double uu = Us[wa][t] * Us[wb][t] * inv_r2;
+        const int p = oxc_pair(wa, wb, nw);
+#pragma unroll
+        for (int L = 0; L < kOxcL; L++) n[L] += C[L][p] * uu;
+      }
+    n[0] += sq4pi * (s ? T.tcore : T.core)[T.roff[a] + k];
+    double up = 0.5 * n[0] / sq4pi;  // spin density of the spherical part
+    if (up < kOxcDenPos) up = kOxcDenPos;
+    const double ns = 2.0 * up;
+    // the step is taken as the difference of two doubles, so that ns + h and
+    // ns - h are exact and the divided differences see the steps they divide by
+    const double h = (ns + kOxcDelta * ns) - ns;
+    const Ts vs = oxc_vxc_series(ns);
+    const double v0 = vs.c[0];
+    double d1 = 0.0, d2 = 0.0;
+    if (up > kOxcRhoMin) {  // pawxcm's central differences at the step h (series above)
+      const double t = h / ns, t2 = t * t;
+      d1 = fma(vs.c[3], t2, vs.c[1]) / ns;
+      d2 = 2.0 * fma(vs.c[4], t2, vs.c[2]) / (ns * ns);
+    }
+    double v1sum = 0.0;
+#pragma unroll
+    for (int L = 1; L < kOxcL; L++) v1sum += n[L] * n[L];
+    const double wk = T.w[T.roff[a] + k];
+    V[0] = wk * (v0 * sq4pi + v1sum * d2 / (2.0 * sq4pi));
+#pragma unroll
+    for (int L = 1; L < kOxcL; L++) V[L] = wk * d1 * n[L];
+  }
+#pragma unroll
+  for (int L = 0; L < kOxcL; L++) Vw[L][t] = V[L];
+  __syncthreads();
+  double *out = part + (((int64_t)a * 2 + s) * T.nchunk + ch) * (kOxcL * kOxcMaxP);
+  for (int e = t; e < kOxcL * np; e += blockDim.x) {
+    const int L = e / np, p = e % np;
+    int wa = 0, q = p;
+    while (q >= nw - wa) {
+      q -= nw - wa;
+      wa++;
+    }
+    const int wb = wa + q;
+    double acc = 0.0;
+    for (int i = 0; i < kOxcChunk; i++) acc += Vw[L][i] * Us[wa][i] * Us[wb][i];
+    out[L * kOxcMaxP + p] = acc;
+  }
+}
+
+// D_xc_ij = sum_L G^L_ij sum_chunks (I^L_{pw_i pw_j} - I~^L_{pw_i pw_j}): a
+// warp per entry, lanes over (L, chunk) in a fixed order (the same arithmetic
+// for ij and ji, so every block is exactly symmetric)
+__global__ void __launch_bounds__(256) k_oxc_assemble(OxcTabs T, const double *__restrict__ part, int nd,
+                                                      double *__restrict__ dxc) {
+  const int e = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (e >= nd) return;
+  const int a = T.dslot[e];
+  const int m = T.ms[a], nr = T.rad_n[a], nw = T.nphi[a];
+  const int loc = e - (int)T.doff[a], i = loc % m, j = loc / m;
+  const int nch = (nr + kOxcChunk - 1) / kOxcChunk;
+  const double *G = T.gaunt + (int64_t)kOxcL * T.doff[a];
+  const int *pw = T.pwave + T.soff[a];
+  const int p = oxc_pair(pw[i], pw[j], nw);
+  const double *ae = part + ((int64_t)a * 2) * T.nchunk * (kOxcL * kOxcMaxP);
+  const double *ps = ae + (int64_t)T.nchunk * (kOxcL * kOxcMaxP);
+  double acc = 0.0;
+  for (int q = lane; q < kOxcL * nch; q += 32) {
+    const int L = q / nch, c = q % nch;
+    const int64_t o = (int64_t)c * (kOxcL * kOxcMaxP) + L * kOxcMaxP + p;
+    acc += G[(L * m + i) * m + j] * (ae[o] - ps[o]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) dxc[e] = acc;
 }
 
 // ---- set-up: validate and upload the radial tables (ctx.cu calls this)
@@ -265,12 +366,15 @@ int onsite_init(opaw_ctx *c, const opaw_system *s) {
            "on-site XC: every radial table is needed when rad_n is given");
   const int na = c->natom;
   std::vector<int64_t> roff(na + 1, 0), phioff(na + 1, 0);
+  int nchunk = 1;
   std::vector<int> pwave(c->ns > 0 ? c->ns : 1);
   std::vector<double> gl(kOxcL * 16);
   gaunt_l1(gl.data());
   std::vector<double> gaunt((size_t)kOxcL * (c->nd > 0 ? c->nd : 1), 0.0);
   for (int a = 0; a < na; a++) {
     OPAW_ARG(s->rad_n[a] >= 3 && s->nphi[a] >= 1, "on-site XC: radial mesh or partial waves missing");
+    OPAW_ARG(s->nphi[a] <= kOxcMaxW, "on-site XC: at most 6 partial waves per atom");
+    nchunk = std::max(nchunk, (s->rad_n[a] + kOxcChunk - 1) / kOxcChunk);
     roff[a + 1] = roff[a] + s->rad_n[a];
     phioff[a + 1] = phioff[a] + (int64_t)s->nphi[a] * s->rad_n[a];
     const int m = c->h_ms[a];
@@ -310,14 +414,16 @@ int onsite_init(opaw_ctx *c, const opaw_system *s) {
   OPAW_CHECK(up((void **)&c->oxc_tphi, s->tphi, sizeof(double) * phioff[na]));
   OPAW_CHECK(up((void **)&c->oxc_pwave, pwave.data(), sizeof(int) * pwave.size()));
   OPAW_CHECK(up((void **)&c->oxc_gaunt, gaunt.data(), sizeof(double) * gaunt.size()));
-  OPAW_CHECK(up((void **)&c->oxc_scratch, nullptr, sizeof(double) * 2 * kOxcL * roff[na]));
+  OPAW_CHECK(up((void **)&c->oxc_nphi, s->nphi, sizeof(int) * na));
+  OPAW_CHECK(up((void **)&c->oxc_scratch, nullptr, sizeof(double) * (size_t)na * 2 * nchunk * kOxcL * kOxcMaxP));
+  c->oxc_nchunk = nchunk;
   c->oxc_on = 1;
   return OPAW_OK;
 }
 
 void onsite_free(opaw_ctx *c) {
   void *p[] = {c->oxc_rad_n, c->oxc_roff, c->oxc_r, c->oxc_w, c->oxc_core, c->oxc_tcore, c->oxc_phioff,
-               c->oxc_phi, c->oxc_tphi, c->oxc_pwave, c->oxc_gaunt, c->oxc_scratch};
+               c->oxc_phi, c->oxc_tphi, c->oxc_pwave, c->oxc_gaunt, c->oxc_scratch, c->oxc_nphi};
   for (void *q : p) cudaFree(q);
 }
 
@@ -326,6 +432,8 @@ int onsite_xc_of(opaw_ctx *c, const double *rhoij, double *dxc) {
   if (!c->oxc_on || c->natom == 0) return OPAW_OK;
   OxcTabs T;
   T.rad_n = c->oxc_rad_n;
+  T.nphi = c->oxc_nphi;
+  T.nchunk = c->oxc_nchunk;
   T.roff = c->oxc_roff;
   T.r = c->oxc_r;
   T.w = c->oxc_w;
@@ -339,8 +447,10 @@ int onsite_xc_of(opaw_ctx *c, const double *rhoij, double *dxc) {
   T.ms = c->d_ms;
   T.doff = c->d_doff;
   T.soff = c->d_soff;
-  k_onsite_xc<<<c->natom, 256, 0, c->stream>>>(T, rhoij, c->oxc_scratch, dxc);
-  c->launches++;
+  T.dslot = c->d_dslot_atom;
+  k_oxc_radial<<<dim3(c->natom, 2, c->oxc_nchunk), kOxcChunk, 0, c->stream>>>(T, rhoij, c->oxc_scratch);
+  k_oxc_assemble<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(T, c->oxc_scratch, c->nd, dxc);
+  c->launches += 2;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
 }

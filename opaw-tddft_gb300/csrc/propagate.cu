@@ -314,9 +314,24 @@ static void unbind_kick(opaw_ctx *c, const KickBind &b) {
 // nsteps steps of the unperturbed set and every kicked set; per step
 // 3 + 6 nkick doubles into dd (device): dip, then dip'_k, d_dip_k per kick.
 // tmp: 9 nkick device doubles of scratch (FP64 path).
+// the fewest steps of a call that replay a captured graph (instantiating it
+// costs about as much as a few steps of plain launches)
+constexpr int kGraphMinSteps = 8;
+
+// tmp: max(9 nkick, 2 (3 + 6 nkick)) device doubles of scratch
 static int steps_dev(opaw_ctx *c, int nsteps, double dt, int prec, double *dd, double *tmp) {
   const size_t per = 3 + 6 * (size_t)c->nkick;
-  if (prec == OPAW_PREC_MIXED) return mixed_steps(c, nsteps, dt, c->d_kgamma, dd);
+  if (prec == OPAW_PREC_MIXED) {
+    // a block of steps replays a captured two-step graph (one context of the
+    // ensemble path); with per-launch kernel timing on, or for a few steps,
+    // the launches are issued one by one
+    if (!c->ktime_on && nsteps >= kGraphMinSteps) {
+      opaw_ctx *cs[1] = {c};
+      double *ddv[1] = {dd}, *fx[1] = {tmp};
+      return ensemble_steps(cs, 1, nsteps, dt, ddv, fx);
+    }
+    return mixed_steps(c, nsteps, dt, c->d_kgamma, dd);
+  }
   for (int it = 0; it < nsteps; it++) {
     // ncpaw_make_hamiltonian_tddft (tddft.f90:75) and propdt (:80), one set
     // after the other: the sets never interact, so this equals the
@@ -356,7 +371,7 @@ int tddft_steps(opaw_ctx *c, int nsteps, double dt, double gamma, int prec, doub
   c->h_kgamma.assign(1, gamma);
   OPAW_CHECK(upload_kgamma(c));
   const size_t nout = 9 * (size_t)(nsteps > 0 ? nsteps : 1);
-  OPAW_CHECK(ensure(c->work[11], sizeof(double) * (nout + 9 + 16)));
+  OPAW_CHECK(ensure(c->work[11], sizeof(double) * (nout + 18 + 16)));
   double *dd = (double *)c->work[11].p;  // 9 values per step: dip, dip_pert, d_dip
   OPAW_CHECK(steps_dev(c, nsteps, dt, prec, dd, dd + nout));
   if ((d_dip_out || dip_out || dip_pert_out) && nsteps > 0) {
@@ -386,7 +401,7 @@ static int tddft_steps_kicks(opaw_ctx *c, int nsteps, double dt, int prec, doubl
   OPAW_CHECK(upload_kgamma(c));
   const size_t per = 3 + 6 * (size_t)c->nkick;
   const size_t nout = per * (size_t)(nsteps > 0 ? nsteps : 1);
-  OPAW_CHECK(ensure(c->work[11], sizeof(double) * (nout + 9 * (size_t)c->nkick + 16)));
+  OPAW_CHECK(ensure(c->work[11], sizeof(double) * (nout + 12 * (size_t)c->nkick + 6 + 16)));
   double *dd = (double *)c->work[11].p;
   OPAW_CHECK(steps_dev(c, nsteps, dt, prec, dd, dd + nout));
   if ((d_dip_out || dip_out || dip_pert_out) && nsteps > 0) {
