@@ -327,7 +327,10 @@ int opaw_ensemble_steps(opaw_ctx *const *ctx, int nctx, int nsteps, double dt, d
                         double *const *dip_pert_out, double *const *d_dip_out);
 /* nsteps iterations of the opaw_tddft loop body (tddft.f90:67-91):
  * rebuild both sets, rk4_prop_shs (rk4.f90:1-103), plot_dip.  d_dip_out
- * receives 3*nsteps values (may be NULL). */
+ * receives 3*nsteps values (may be NULL).  In mixed precision a call of 8 or
+ * more steps replays a captured two-step CUDA graph (the launches of
+ * opaw_ensemble_steps for one context); fewer steps, or kernel timing on
+ * (opaw_ktime_begin), issue the launches one by one, with the same results. */
 int opaw_tddft_steps(opaw_ctx *ctx, int nsteps, double dt, double gamma, int precision,
                      double *d_dip_out);
 /* the same with everything plot_dip writes per step (tddft_plot.f90:101-104):
