@@ -757,6 +757,10 @@ def main():
                "api": "opaw_tddft_steps_host (psi, psi_pert host arrays in/out each step)", "steps": nh,
                "call_ms": [round(x, 2) for x in calls]}
 
+    # the launch shapes the autotuner picked during the warm-up steps
+    tune = [{"site": t["site"], "chosen": t["candidates"][t["chosen"]] if t["chosen"] >= 0 else None,
+             "ms": dict(zip(t["candidates"], [round(x, 4) for x in t["ms"]]))} for t in ctx.tune_report()]
+
     series = None
     if rank == 0 and args.series != "none":
         full = args.series == "full"
@@ -793,6 +797,7 @@ def main():
             "fp64_gpu_over_fp64_cpu": (fp64["orbital_steps_per_s"] / cpu["value"]) if (fp64 and cpu) else None,
             "e2e": e2e,
             "gpu_launches": launches,
+            "autotune": tune,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)

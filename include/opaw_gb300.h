@@ -123,6 +123,19 @@ int64_t opaw_kernel_launches(opaw_ctx *ctx);
  * with no counterpart in the reference. */
 int opaw_ktime_begin(opaw_ctx *ctx);
 int opaw_ktime_end(opaw_ctx *ctx, double *ms, int *launches, double *bytes);
+
+/* Launch-shape autotuner (no reference counterpart).  Some launch shapes
+ * have candidates that compute bit-identical results with different speed
+ * (L2 prefetch distance of the copy plane pass, lines per CTA of the z pass,
+ * orbitals per CTA of the box terms, block size of the dense stage pass);
+ * the context times each candidate twice on the launches it makes anyway and
+ * keeps the fastest per launch shape.  On by default; off: the defaults. */
+int opaw_tune_enable(opaw_ctx *ctx, int on);
+/* the tuner's state as JSON, [{"site", "candidates", "ms", "chosen"}, ...]
+ * (chosen -1: still timing); writes at most len bytes with the terminating
+ * NUL, *needed = the full length + 1 */
+int opaw_tune_report(opaw_ctx *ctx, char *buf, int64_t len, int64_t *needed);
+
 /* waits for all work issued on the context's stream (the *_dev entry points
  * below are asynchronous on that stream) */
 int opaw_sync(opaw_ctx *ctx);

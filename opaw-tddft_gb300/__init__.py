@@ -104,6 +104,8 @@ SIGNATURES = {
     "opaw_kernel_launches": (ct.c_int64, [_P]),
     "opaw_ktime_begin": (ct.c_int, [_P]),
     "opaw_ktime_end": (ct.c_int, [_P, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int), ct.POINTER(ct.c_double)]),
+    "opaw_tune_enable": (ct.c_int, [_P, ct.c_int]),
+    "opaw_tune_report": (ct.c_int, [_P, ct.c_char_p, ct.c_int64, ct.POINTER(ct.c_int64)]),
     "opaw_sync": (ct.c_int, [_P]),
     "opaw_psi_upload": (ct.c_int, [_P, ct.c_int, _P, ct.c_int]),
     "opaw_psi_download": (ct.c_int, [_P, ct.c_int, _P, ct.c_int]),
@@ -233,6 +235,20 @@ class Context:
 
     def sync(self):
         _check(lib().opaw_sync(self.h))
+
+    def tune_enable(self, on=True):
+        """Switches the launch-shape autotuner on (the default) or off."""
+        _check(lib().opaw_tune_enable(self.h, 1 if on else 0))
+
+    def tune_report(self):
+        """The autotuner's sites: [{"site", "candidates", "ms", "chosen"}]."""
+        import json
+
+        need = ct.c_int64(0)
+        _check(lib().opaw_tune_report(self.h, None, 0, ct.byref(need)))
+        buf = ct.create_string_buffer(int(need.value))
+        _check(lib().opaw_tune_report(self.h, buf, need.value, ct.byref(need)))
+        return json.loads(buf.value.decode())
 
     def ktime_begin(self):
         """Start live event timing of the fused dense pass (opaw_ktime_begin)."""

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <deque>
 #include <string>
 #include <vector>
 
@@ -149,6 +150,18 @@ struct DeviceBuf {
   size_t bytes = 0;
 };
 
+// One launch site of the autotuner (autotune.cu): its candidates are timed
+// with CUDA events on the launches the computation makes anyway (every
+// candidate computes bit-identical results), kTuneRounds times each in turn;
+// then the fastest is kept for the context's lifetime.
+struct TuneSite {
+  std::vector<std::string> labels;
+  std::vector<cudaEvent_t> ev;  // [round][candidate][start, stop]
+  std::vector<float> ms;        // best time per candidate
+  int next = 0;                 // timed launches so far
+  int chosen = -1;
+};
+
 }  // namespace opaw
 
 struct opaw_ctx {
@@ -160,6 +173,9 @@ struct opaw_ctx {
   int nsm = 0;  // multiprocessors of the context's device
   // live timing of the fused dense pass (opaw_ktime_begin / _end)
   bool ktime_on = false;
+  // autotuner state: launch site key -> site (autotune.cu)
+  bool tune_on = true;
+  std::deque<std::pair<std::string, opaw::TuneSite>> tune;
   std::vector<cudaEvent_t> kev;  // start/stop pairs, reused
   int kev_used = 0;
   double kbytes = 0.0;
@@ -371,6 +387,13 @@ int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vx
 // step into dd_dev: dip, then dip'_k and d_dip_k of every kick
 int mixed_steps(opaw_ctx *c, int nsteps, double dt, const double *gamma_dev, double *dd_dev);
 int ensemble_steps(opaw_ctx *const *cs, int n, int nsteps, double dt, double *const *dd, double *const *fixed);
+// autotuner: the candidate to launch at site `key` (labels: one per
+// candidate; dflt when tuning is off, finished or the stream is capturing);
+// *timed != nullptr: the launch is being timed, close it with tune_end
+int tune_begin(opaw_ctx *c, const std::string &key, const std::vector<std::string> &labels, int dflt,
+               TuneSite **timed);
+int tune_end(opaw_ctx *c, TuneSite *timed);
+void tune_free(opaw_ctx *c);
 // LDA potential of n points (device arrays)
 int vxc_points(opaw_ctx *c, const double *dens, double *vxc, int64_t n);
 // gout = 1/N ifft(bk fft(a)) on the context's main FFT plan; a is overwritten

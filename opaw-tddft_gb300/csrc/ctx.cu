@@ -380,6 +380,7 @@ static void destroy(opaw_ctx *c) {
   cudaFree(c->d_kgamma);
   onsite_free(c);
   cudaFree(c->oxc_dxc);
+  tune_free(c);
   for (auto &b : c->work) cudaFree(b.p);
   for (auto &b : c->coef) cudaFree(b.p);
   cudaFree(c->coefr.p);

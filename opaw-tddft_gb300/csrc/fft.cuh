@@ -10,7 +10,9 @@
 #pragma once
 
 #include <algorithm>
+#include <string>
 #include <type_traits>
+#include <typeinfo>
 #include <utility>
 
 #include "common.cuh"
@@ -366,7 +368,17 @@ __device__ __forceinline__ void l2_prefetch_bulk(const void *gmem, unsigned byte
 }
 
 
+// a readable name of an operation functor for the autotuner's keys: its
+// kName when it has one, else the type's name
+template <class Op, class = void> struct OpNameOf {
+  static std::string get() { return typeid(Op).name(); }
+};
+template <class Op> struct OpNameOf<Op, std::void_t<decltype(Op::kName)>> {
+  static std::string get() { return Op::kName; }
+};
+
 template <typename C> struct OpCopy {
+  static constexpr const char *kName = "copy";
   const C *src;
   C *dst;
   int64_t bstride;
@@ -664,9 +676,8 @@ template <typename C, int N> constexpr int ct_tile() {
   return budget / N >= 32 ? 32 : (budget / N >= 16 ? 16 : (budget / N >= 8 ? 8 : 4));
 }
 
-template <typename C, int N, int AXIS, class Op>
-int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op, const LineSub *lsub) {
-  constexpr int TL = ct_tile<C, N>();
+template <typename C, int N, int TL, int AXIS, class Op>
+int launch_ct_tl(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op, const LineSub *lsub) {
   const LineSub sub = lsub ? *lsub : LineSub::full(d);
   int64_t tiles;
   if (AXIS == 0) tiles = (int64_t)((sub.na + TL - 1) / TL) * sub.nb;
@@ -691,6 +702,29 @@ int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const
     return OPAW_ERR_CUDA;
   }
   return OPAW_OK;
+}
+
+// z pass: the tile width (lines per CTA) is tuned between the default and
+// half of it (the lines are transformed the same way in either); the other
+// axes take the default
+template <typename C, int N, int AXIS, class Op>
+int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op, const LineSub *lsub) {
+  constexpr int TL = ct_tile<C, N>();
+  if constexpr (AXIS == 2 && TL >= 16) {
+    static const std::vector<std::string> labels = {std::to_string(TL) + " lines per CTA",
+                                                    std::to_string(TL / 2) + " lines per CTA"};
+    const std::string key = std::string("z pass ") + (sizeof(C) == 8 ? "c64" : "c128") + " n " + std::to_string(N) +
+                            " lines " + std::to_string((int64_t)d.n0 * d.n1) + " batch " + std::to_string(batch) +
+                            " op " + OpNameOf<Op>::get();
+    TuneSite *ts = nullptr;
+    const int cand = tune_begin(c, key, labels, 0, &ts);
+    const int st = cand == 1 ? launch_ct_tl<C, N, TL / 2, AXIS>(c, a, d, batch, sign, op, lsub)
+                             : launch_ct_tl<C, N, TL, AXIS>(c, a, d, batch, sign, op, lsub);
+    OPAW_CHECK(st);
+    return tune_end(c, ts);
+  } else {
+    return launch_ct_tl<C, N, TL, AXIS>(c, a, d, batch, sign, op, lsub);
+  }
 }
 
 // ------------------------------------------------------------------------
@@ -878,14 +912,25 @@ int launch_xy(opaw_ctx *c, const FFTAxis &ax, const FFTAxis &ay, int nz, int bat
     }
   }
   dim3 grid((unsigned)nz, (unsigned)batch);
-  kern<<<grid, 384, smem, c->stream>>>(sign, axis_tw<C>(ax), axis_tw<C>(ay), op, 2 * c->nsm);
+  // L2 prefetch distance of the plain copy pass, in resident waves (tuned)
+  int ahead = 2 * c->nsm;
+  TuneSite *ts = nullptr;
+  if constexpr (HasRaw<Op>::value && !HasPre<Op>::value) {
+    static const std::vector<std::string> labels = {"no prefetch", "prefetch 1 wave ahead", "prefetch 2 waves ahead",
+                                                    "prefetch 4 waves ahead"};
+    const int waves[4] = {0, 1, 2, 4};
+    const std::string key = "xy copy " + std::to_string(NX) + "x" + std::to_string(NY) + " nz " +
+                            std::to_string(nz) + " batch " + std::to_string(batch);
+    ahead = waves[tune_begin(c, key, labels, 2, &ts)] * c->nsm;
+  }
+  kern<<<grid, 384, smem, c->stream>>>(sign, axis_tw<C>(ax), axis_tw<C>(ay), op, ahead);
   c->launches++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error(std::string("xy launch: ") + cudaGetErrorString(e));
     return OPAW_ERR_CUDA;
   }
-  return OPAW_OK;
+  return tune_end(c, ts);
 }
 
 // both x and y transforms of every z-plane in one pass when the plane has a

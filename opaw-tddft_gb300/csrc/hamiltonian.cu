@@ -507,6 +507,7 @@ __global__ void k_coef_scale(const double2 *__restrict__ cin, double2 *__restric
 // kinetic hook on z-lines: v *= min((kx^2 + ky^2 + kz^2)/2, ekcut) / N   (ek.f90:40-50)
 template <typename R> struct OpKin;
 template <> struct OpKin<double> {
+  static constexpr const char *kName = "kinetic";
   double2 *buf;
   int64_t bstride;
   const double *k2x, *k2y, *k2z;
@@ -529,6 +530,7 @@ template <> struct OpKin<double> {
   }
 };
 template <> struct OpKin<float> {
+  static constexpr const char *kName = "kinetic";
   float2 *buf;
   int64_t bstride;
   const float *k2x, *k2y, *k2z;
@@ -556,6 +558,7 @@ template <> struct OpKin<float> {
 //   K(x) = (27 + 18 x + 12 x^2 + 8 x^3) / (27 + 18 x + 12 x^2 + 8 x^3 + 16 x^4),
 // applied with the 1/N of the unnormalised inverse transform folded in
 template <typename R> struct OpTPA {
+  static constexpr const char *kName = "kinetic preconditioner";
   typedef typename Tr<R>::C C;
   C *buf;
   int64_t bstride;

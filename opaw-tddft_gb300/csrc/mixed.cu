@@ -28,6 +28,8 @@
 // the reference's own form for comparison.
 #include <cmath>
 
+#include <type_traits>
+
 #include "fft.cuh"
 
 namespace opaw {
@@ -1141,15 +1143,30 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
   f.stage = stage;
   f.first = first;
   f.write_t = write_t;
-  constexpr int OG = 4, MS = 8;
-  const size_t bsmem = sizeof(float4) * 3 * OG * MS * (size_t)c->uamax;
+  constexpr int MS = 8;
+  const size_t bsmem = sizeof(float4) * 3 * 4 * MS * (size_t)c->uamax;  // at the larger orbital group
   if (c->nunion > 0 && c->ns > 0 && c->d_uent && c->msmax <= MS && bsmem <= 48 * 1024 && (stage || write_t)) {
-    const dim3 nb((c->nunion + kUTile - 1) / kUTile, (m.norb + OG - 1) / OG, (m.nset + 1) / 2);
     const int mode = (stage ? 1 : 0) | (write_t ? 2 : 0);
-    auto kern = mode == 1 ? k_mix_boxcoef_t<1, MS, OG> : mode == 2 ? k_mix_boxcoef_t<2, MS, OG> : k_mix_boxcoef_t<3, MS, OG>;
-    kern<<<nb, kUTile, bsmem, c->stream>>>(c->nunion, m.norb, c->ns, c->uamax, m.nset, c->d_ustart, c->d_uent,
+    // orbitals per CTA (tuned): every (union point, orbital) term is the same sum either way
+    auto launch = [&](auto og) {
+      constexpr int OG = decltype(og)::value;
+      const dim3 nb((c->nunion + kUTile - 1) / kUTile, (m.norb + OG - 1) / OG, (m.nset + 1) / 2);
+      const size_t sm = sizeof(float4) * 3 * OG * MS * (size_t)c->uamax;
+      auto kern = mode == 1 ? k_mix_boxcoef_t<1, MS, OG>
+                            : mode == 2 ? k_mix_boxcoef_t<2, MS, OG> : k_mix_boxcoef_t<3, MS, OG>;
+      kern<<<nb, kUTile, sm, c->stream>>>(c->nunion, m.norb, c->ns, c->uamax, m.nset, c->d_ustart, c->d_uent,
                                           c->d_utile, c->d_utile_na, c->d_p3d_f, c->d_p3d1_f, m.cab, m.cg, m.bg);
+    };
+    static const std::vector<std::string> labels = {"4 orbitals per CTA", "2 orbitals per CTA"};
+    TuneSite *ts = nullptr;
+    const int cand = tune_begin(c, "box terms mode " + std::to_string(mode) + " union " +
+                                       std::to_string(c->nunion) + " orbitals " + std::to_string(m.norb) +
+                                       " sets " + std::to_string(m.nset),
+                                labels, 0, &ts);
+    if (cand == 1) launch(std::integral_constant<int, 2>());
+    else launch(std::integral_constant<int, 4>());
     MIX_LAUNCHED();
+    OPAW_CHECK(tune_end(c, ts));
   } else if (c->nunion > 0 && c->ns > 0) {
     const dim3 nb(grid1(c->nunion, 128), m.norb, m.nset);
     k_mix_boxcoef<<<nb, 128, 0, c->stream>>>(c->nunion, m.norb, c->ns, c->d_ustart, c->d_uatom, c->d_ubox,
@@ -1170,8 +1187,17 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
     c->kev_used += 2;
     OPAW_CUDA(cudaEventRecord(ev0, c->stream));
   }
-  k_mix_dense<<<grid1(c->nn, 256) * m.nkick, 256, 0, c->stream>>>(f, c->d_uidx, m.bg, c->ns > 0 ? c->nunion : 0);
+  // block size (tuned): a thread per grid point either way
+  static const std::vector<std::string> dlabels = {"256 threads per CTA", "128 threads per CTA"};
+  TuneSite *dts_site = nullptr;
+  const int dcand = tune_begin(c, "dense pass points " + std::to_string(c->nn) + " orbitals " +
+                                     std::to_string(m.norb) + " kicks " + std::to_string(m.nkick),
+                              dlabels, 0, &dts_site);
+  const int dthreads = dcand == 1 ? 128 : 256;
+  k_mix_dense<<<grid1(c->nn, dthreads) * m.nkick, dthreads, 0, c->stream>>>(f, c->d_uidx, m.bg,
+                                                                             c->ns > 0 ? c->nunion : 0);
   MIX_LAUNCHED();
+  OPAW_CHECK(tune_end(c, dts_site));
   if (ev1) {
     OPAW_CUDA(cudaEventRecord(ev1, c->stream));
     // algorithmic bytes: the union index of every point; per point and

@@ -192,6 +192,7 @@ template <typename C> struct OpMasked {
 };
 
 template <typename R> struct OpVk {
+  static constexpr const char *kName = "hartree kernel";
   typedef typename Tr<R>::C C;
   C *wb;
   const R *vk;
