@@ -299,13 +299,31 @@ def roofline(ctx, pkg, torch, stream, s, psi0, norb):
     r1.record(stream)
     torch.cuda.synchronize()
     nl = ctx.launches - l1
-    per_launch_s = r0.elapsed_time(r1) / 1e3 / nl
+    ours_ms = r0.elapsed_time(r1) / reps
+    per_launch_s = ours_ms / 1e3 / (nl / reps)
     alg_bytes = 2.0 * norb * s.nn * 8  # read + write the complex64 batch once per axis pass
     achieved = alg_bytes / per_launch_s / 1e9
+    # comparison only: the same batch of 3D transforms through cuFFT (torch.fft,
+    # out of place) on the same stream
+    cufft_ms = None
+    with torch.cuda.stream(stream):
+        v = batch.view(norb, s.nz, s.ny, s.nx)
+        for _ in range(2):
+            w = torch.fft.fftn(v, dim=(1, 2, 3))
+        del w
+        r0.record(stream)
+        for _ in range(reps):
+            w = torch.fft.fftn(v, dim=(1, 2, 3))
+        r1.record(stream)
+        torch.cuda.synchronize()
+        cufft_ms = r0.elapsed_time(r1) / reps
+        del w, v
     del batch
     return {"kernel": f"k_fft_xy + k_fft_ct (forward 3D FFT: xy-plane pass and z pass, {norb} x 96^3 complex64)",
             "achieved": achieved, "unit": "GB/s", "frac": achieved / peak, "alg_bytes_per_launch": alg_bytes,
-            "avg_launch_ms": per_launch_s * 1e3}
+            "avg_launch_ms": per_launch_s * 1e3, "ms_per_3d_fft": ours_ms,
+            "cufft_ms_per_3d_fft": cufft_ms, "cufft_note": "the same batch through cuFFT (torch.fft.fftn, out of "
+                                                           "place), a comparison only: the step never calls it"}
 
 
 def ground_state(pkg, s, norb, seed=2025):
@@ -476,9 +494,11 @@ POLYACENE_GRIDS = {2: (64, 48, 48), 3: (80, 48, 48), 4: (96, 64, 48), 5: (112, 6
 
 def precond_leg(pkg, torch, full):
     """Ground-state eigensolve of synthetic polyacenes C(4n+2)H(2n+4) at h =
-    0.4 Bohr (grids up to 128x64x48): LOBPCG to the unpreconditioned
-    eigen-residual 1e-8 with the plain Teter-Payne-Allan kinetic
-    preconditioner and with the learned 3D-conv correction.  The network is
+    0.4 Bohr (grids up to 128x64x48): LOBPCG (soft locking) to the
+    unpreconditioned eigen-residual 1e-8 with the plain Teter-Payne-Allan
+    kinetic preconditioner, with the learned 3D-conv correction beside it in
+    the basis (augment), and with the learned direction alone (replace, the
+    kinetic one its fallback).  The network is
     trained on the device on residual -> correction patches from the plain
     solves of n = 2, 3, 4 and evaluated on the held-out n = 5, 6, where both
     solvers start from the same orbitals; their eigenvalues are compared with
@@ -521,6 +541,7 @@ def precond_leg(pkg, torch, full):
         eigensolver.lobpcg(c, X0[:, :], tol=1e-3)  # warm-up: grows the device buffers
         plain = eigensolver.lobpcg(c, X0, tol=1e-8)
         lrn = eigensolver.lobpcg(c, X0, net=net, tol=1e-8)
+        rep = eigensolver.lobpcg(c, X0, net=net, tol=1e-8, learned_mode="replace")
         e = {"grid": list(POLYACENE_GRIDS[n]), "orbitals": norb,
              "plain": {"iterations": plain.iterations, "iterations_fp32": plain.iterations_fp32,
                        "seconds": plain.seconds, "max_residual": float(plain.residuals.max()),
@@ -528,7 +549,12 @@ def precond_leg(pkg, torch, full):
              "learned": {"iterations": lrn.iterations, "iterations_fp32": lrn.iterations_fp32,
                          "seconds": lrn.seconds, "max_residual": float(lrn.residuals.max()),
                          "converged": lrn.converged},
+             "learned_replace": {"iterations": rep.iterations, "iterations_fp32": rep.iterations_fp32,
+                                 "seconds": rep.seconds, "max_residual": float(rep.residuals.max()),
+                                 "converged": rep.converged, "fallback_iteration": rep.fallback_iteration},
              "speedup_learned_over_plain": plain.seconds / lrn.seconds,
+             "speedup_learned_replace_over_plain": plain.seconds / rep.seconds,
+             "eig_max_diff_learned_replace_vs_plain_ha": float(np.abs(rep.eigenvalues - plain.eigenvalues).max()),
              "eig_max_diff_learned_vs_plain_ha": float(np.abs(lrn.eigenvalues - plain.eigenvalues).max())}
         if n == 5:
             w_ch, _, res_ch = groundstate.lowest_states(c, X0, n_iter=200, tol=1e-6, fp64_polish=6)

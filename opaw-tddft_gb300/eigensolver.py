@@ -48,6 +48,7 @@ class Result:
         self.seconds = 0.0
         self.history = []  # (iteration, max residual, seconds)
         self.converged = False
+        self.fallback_iteration = None  # learned_mode "replace": where K r took over
 
 
 def _rr(ctx, dt, S, HS, m, drop=1e-12):
@@ -67,21 +68,28 @@ def _rr(ctx, dt, S, HS, m, drop=1e-12):
 
 
 def lobpcg(ctx, X0, net=None, tol=1e-8, switch_tol=1e-3, max_iter=400, record=None, record_every=4,
-           verbose=False):
+           verbose=False, learned_mode="augment", lock=True):
     """Lowest len(X0) eigenpairs of S^-1/2 H S^-1/2 (set 0's v_ks and D_ij)
     from the starting orbitals X0 [m, nn].  net: a trained `learned.Net`
-    (None: the plain kinetic preconditioner).  record: a list that receives
-    (X, R, eps) of every `record_every`-th complex128 iteration (device
-    tensors) for training.  Every torch operation runs on the library's
-    stream.  Returns a `Result`."""
+    (None: the plain kinetic preconditioner).  learned_mode: "augment" puts
+    both K r and the learned K r + |r| N in the basis; "replace" uses the
+    learned direction alone, falling back to K r for the rest of the solve
+    when the largest residual has not fallen by 10% over 6 iterations.
+    lock: columns whose residual is below tol contribute no W or P
+    directions (soft locking; they stay in X and in the Rayleigh-Ritz step).
+    record: a list that receives (X, R, eps) of every `record_every`-th
+    complex128 iteration (device tensors) for training.  Every torch
+    operation runs on the library's stream.  Returns a `Result`."""
+    if learned_mode not in ("augment", "replace"):
+        raise ValueError("learned_mode must be 'augment' or 'replace'")
     torch = _torch()
     with torch.cuda.stream(torch.cuda.ExternalStream(ctx.stream)):
-        out = _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbose)
+        out = _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbose, learned_mode, lock)
         torch.cuda.current_stream().synchronize()
     return out
 
 
-def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbose):
+def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbose, learned_mode, lock):
     torch = _torch()
     res = Result()
     dv = ctx.system.dv
@@ -105,6 +113,9 @@ def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbo
         ctx.rotate_dev(dt, HX.data_ptr(), m, Y, HXn.data_ptr())
         X, HX, w = Xn, HXn, th
         P = HP = None
+        pvalid = None
+        hist64 = []
+        fallback = False
         fresh = True  # HX is H X itself, not the rotated recurrence
         since = 0
         best = np.inf
@@ -137,44 +148,68 @@ def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbo
                 continue
             if record is not None and dt == pkg.OPAW_C128 and it % record_every == 0:
                 record.append((X.clone(), R.clone(), np.array(w, np.float64)))
-            ekin = ctx.kinetic_energy_dev(dt, X.data_ptr(), m)
-            W = torch.empty_like(R)
-            ctx.precond_kinetic_dev(dt, R.data_ptr(), ekin, W.data_ptr(), m)
-            if net is not None and dt == pkg.OPAW_C128:
-                # the learned direction joins the kinetic one in the basis
-                # (span[X, K r, K r + |r| N, P]): the Rayleigh-Ritz step takes
-                # what helps, so a poor network cannot stall the iteration
-                WL = torch.empty_like(R)
-                net.apply(ctx, dt, R.data_ptr(), np.asarray(w, np.float64), ekin, WL.data_ptr(), m)
-                W = torch.cat([W, WL])
+            if dt == pkg.OPAW_C128:
+                hist64.append(float(rn.max()))
+                if (net is not None and learned_mode == "replace" and not fallback and len(hist64) > 6
+                        and hist64[-1] > 0.9 * hist64[-7]):
+                    fallback = True  # the learned direction stalls: the kinetic one takes over
+                    res.fallback_iteration = it
+            # soft locking: converged columns add no directions
+            ia = np.nonzero(rn >= ptol)[0] if lock else np.arange(m)
+            ia_t = torch.as_tensor(ia, device="cuda")
+            Ra = R if len(ia) == m else R[ia_t].contiguous()
+            Xa = X if len(ia) == m else X[ia_t].contiguous()
+            wa = np.asarray(w, np.float64)[ia]
+            ekin = ctx.kinetic_energy_dev(dt, Xa.data_ptr(), len(ia))
+            W = torch.empty_like(Ra)
+            ctx.precond_kinetic_dev(dt, Ra.data_ptr(), ekin, W.data_ptr(), len(ia))
+            if net is not None and dt == pkg.OPAW_C128 and not fallback:
+                # augment: the learned direction joins the kinetic one
+                # (span[X, K r, K r + |r| N, P]), so the Rayleigh-Ritz step
+                # takes what helps; replace: the learned direction alone
+                WL = torch.empty_like(Ra)
+                net.apply(ctx, dt, Ra.data_ptr(), wa, ekin, WL.data_ptr(), len(ia))
+                W = torch.cat([W, WL]) if learned_mode == "augment" else WL
             # unit columns: the residual directions shrink with convergence
             # and would otherwise fall under the Gram matrix's drop threshold
             W /= torch.sqrt((W.abs() ** 2).sum(dim=1, keepdim=True) * dv).clamp_min(1e-300).to(W.real.dtype)
             HW = torch.empty_like(W)
             ctx.shs_apply_dev(0, dt, W.data_ptr(), HW.data_ptr(), W.shape[0])
+            blocks, hblocks = [X, W], [HX, HW]
             if P is not None:
-                pn = torch.sqrt((P.abs() ** 2).sum(dim=1, keepdim=True) * dv).clamp_min(1e-300).to(P.real.dtype)
-                P /= pn
-                HP /= pn
-            if P is None:
-                S = torch.cat([X, W])
-                HS = torch.cat([HX, HW])
-            else:
-                S = torch.cat([X, W, P])
-                HS = torch.cat([HX, HW, HP])
+                ip = ia[pvalid[ia]]
+                if len(ip):
+                    ip_t = torch.as_tensor(ip, device="cuda")
+                    Pa, HPa = P[ip_t], HP[ip_t]
+                    pn = torch.sqrt((Pa.abs() ** 2).sum(dim=1, keepdim=True) * dv).clamp_min(1e-300).to(Pa.real.dtype)
+                    blocks.append(Pa / pn)
+                    hblocks.append(HPa / pn)
+            S = torch.cat(blocks)
+            HS = torch.cat(hblocks)
             th, Y = _rr(ctx, dt, S, HS, m, drop)
             ns = S.shape[0]
             Xn = torch.empty_like(X)
             HXn = torch.empty_like(X)
             ctx.rotate_dev(dt, S.data_ptr(), ns, Y, Xn.data_ptr())
             ctx.rotate_dev(dt, HS.data_ptr(), ns, Y, HXn.data_ptr())
-            # the new directions: the part of the Ritz vectors outside span(X)
-            Pn = torch.empty_like(X)
-            HPn = torch.empty_like(X)
+            # the new directions of the active columns: the part of their Ritz
+            # vectors outside span(X)
+            Ya = np.ascontiguousarray(Y[m:][:, ia])
             St, HSt = S[m:].contiguous(), HS[m:].contiguous()
-            ctx.rotate_dev(dt, St.data_ptr(), ns - m, np.ascontiguousarray(Y[m:]), Pn.data_ptr())
-            ctx.rotate_dev(dt, HSt.data_ptr(), ns - m, np.ascontiguousarray(Y[m:]), HPn.data_ptr())
-            X, HX, P, HP, w = Xn, HXn, Pn, HPn, th
+            Pn_a = torch.empty_like(Ra)
+            HPn_a = torch.empty_like(Ra)
+            ctx.rotate_dev(dt, St.data_ptr(), ns - m, Ya, Pn_a.data_ptr())
+            ctx.rotate_dev(dt, HSt.data_ptr(), ns - m, Ya, HPn_a.data_ptr())
+            if len(ia) == m:
+                P, HP = Pn_a, HPn_a
+            else:
+                P = torch.zeros_like(X)
+                HP = torch.zeros_like(X)
+                P[ia_t] = Pn_a
+                HP[ia_t] = HPn_a
+            pvalid = np.zeros(m, bool)
+            pvalid[ia] = True
+            X, HX, w = Xn, HXn, th
             fresh = False
             since += 1
             it += 1

@@ -193,4 +193,10 @@ def test_lobpcg_learned_reaches_1e8(ground):
     assert r.converged and r.residuals.max() < 1e-8
     assert np.abs(r.eigenvalues - plain.eigenvalues).max() < 1e-6
     assert np.abs(r.eigenvalues - w_ch).max() < 1e-6
+    # the learned direction alone (with the kinetic fallback), and without
+    # soft locking: the same eigenpairs
+    for kw in ({"learned_mode": "replace"}, {"lock": False}):
+        r = eigensolver.lobpcg(c, X0, net=net, tol=1e-8, **kw)
+        assert r.converged and r.residuals.max() < 1e-8, kw
+        assert np.abs(r.eigenvalues - w_ch).max() < 1e-6, kw
     net.close()
