@@ -248,7 +248,13 @@ struct opaw_ctx {
   int oxc_nchunk = 1;
   int64_t *oxc_roff = nullptr, *oxc_phioff = nullptr;
   double *oxc_r = nullptr, *oxc_w = nullptr, *oxc_core = nullptr, *oxc_tcore = nullptr;
-  double *oxc_phi = nullptr, *oxc_tphi = nullptr, *oxc_gaunt = nullptr, *oxc_scratch = nullptr;
+  double *oxc_phi = nullptr, *oxc_tphi = nullptr, *oxc_gaunt = nullptr;
+  opaw::DeviceBuf oxc_part;  // partial radial integrals [set][atom][part][chunk][L][pair]
+  opaw::DeviceBuf oxc_sets;  // D_xc of the unperturbed and every kicked set (mixed step)
+  // a second stream of the context: the on-site XC term of the mixed step
+  // runs there while the Hartree solves run on `stream` (fork / join events)
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_fork = nullptr, side_join = nullptr;
   double *oxc_dxc = nullptr;
 
   // kinetic separable tables: k^2 per axis (double, exact copies of the
@@ -380,8 +386,10 @@ int vxc_of(opaw_ctx *c, const double *dens, const double *core, double *out);
 int onsite_init(opaw_ctx *c, const opaw_system *s);
 void onsite_free(opaw_ctx *c);
 int onsite_xc_of(opaw_ctx *c, const double *rhoij, double *dxc);
+int onsite_xc_sets(opaw_ctx *c, const double *rhoij, int nsets, double *dxc, cudaStream_t st);
 // D_ij (get_dij.f90) from rho_ij and the potential v_ks - v_xc of Dhat (vxc may be null)
-int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vxc, double *out);
+int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vxc, double *out,
+           const double *dxc_pre = nullptr);
 // (mixed.cu) nsteps mixed-precision TDDFT steps of the unperturbed set and
 // the c->nkick kicked sets (strengths gamma_dev[k]); 3 + 6 nkick doubles per
 // step into dd_dev: dip, then dip'_k and d_dip_k of every kick

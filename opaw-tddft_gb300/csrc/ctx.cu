@@ -65,6 +65,9 @@ static int build(opaw_ctx *c, const opaw_system *s) {
   c->nnb = (int64_t)c->nxb * c->nyb * c->nzb;
   c->natom = s->natom;
   OPAW_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  OPAW_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  OPAW_CUDA(cudaEventCreateWithFlags(&c->side_fork, cudaEventDisableTiming));
+  OPAW_CUDA(cudaEventCreateWithFlags(&c->side_join, cudaEventDisableTiming));
   {
     int dev = 0;
     OPAW_CUDA(cudaGetDevice(&dev));
@@ -401,6 +404,11 @@ static void destroy(opaw_ctx *c) {
   if (c->h_red) cudaFreeHost(c->h_red);
   fft3_free(c->fft);
   fft3_free(c->fftb);
+  if (c->side) cudaStreamSynchronize(c->side);
+  if (c->side_fork) cudaEventDestroy(c->side_fork);
+  if (c->side_join) cudaEventDestroy(c->side_join);
+  if (c->side) cudaStreamDestroy(c->side);
+  cudaFree(c->oxc_sets.p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

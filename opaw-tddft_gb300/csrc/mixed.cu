@@ -1302,6 +1302,19 @@ static int mix_potentials(opaw_ctx *c, Mix &m) {
     MIX_LAUNCHED();
   }
   (void)sv;
+  // the on-site XC term of every set depends on rho_ij alone: it runs on the
+  // side stream while the compensation charges, the Hartree solves and v_ks
+  // run here, and joins before D_ij
+  double *dxc_sets = nullptr;
+  if (c->oxc_on && c->nd > 0 && c->side) {
+    OPAW_CHECK(ensure(c->oxc_sets, sizeof(double) * (size_t)(1 + K) * c->nd));
+    dxc_sets = (double *)c->oxc_sets.p;
+    OPAW_CUDA(cudaEventRecord(c->side_fork, c->stream));
+    OPAW_CUDA(cudaStreamWaitEvent(c->side, c->side_fork, 0));
+    OPAW_CHECK(onsite_xc_sets(c, c->d_rhoij[0], 1, dxc_sets, c->side));
+    OPAW_CHECK(onsite_xc_sets(c, c->d_rhoij[1], K, dxc_sets + c->nd, c->side));
+    OPAW_CUDA(cudaEventRecord(c->side_join, c->side));
+  }
   for (int k = 0; k < K; k++)  // n^ is linear in rho_ij
     OPAW_CHECK(nhat_raw_of(c, m.drhoij + (size_t)k * c->nd, m.dhraw + (size_t)k * c->nn));
   // charge renormalisation of every set
@@ -1333,10 +1346,12 @@ static int mix_potentials(opaw_ctx *c, Mix &m) {
   MIX_LAUNCHED();
   OPAW_CUDA(cudaMemcpyAsync(c->d_vh[0], m.vh, sizeof(double) * c->nn, cudaMemcpyDeviceToDevice, c->stream));
   // D_ij of every set (FP64) and the kicks' differences
-  OPAW_CHECK(dij_of(c, c->d_rhoij[0], c->d_vks[0], c->d_vxc[0], c->d_dij[0]));
+  if (dxc_sets) OPAW_CUDA(cudaStreamWaitEvent(c->stream, c->side_join, 0));
+  OPAW_CHECK(dij_of(c, c->d_rhoij[0], c->d_vks[0], c->d_vxc[0], c->d_dij[0], dxc_sets));
   for (int k = 0; k < K; k++)
     OPAW_CHECK(dij_of(c, c->d_rhoij[1] + (size_t)k * c->nd, c->d_vks[1] + (size_t)k * c->nn,
-                      c->d_vxc[1] + (size_t)k * c->nn, c->d_dij[1] + (size_t)k * c->nd));
+                      c->d_vxc[1] + (size_t)k * c->nn, c->d_dij[1] + (size_t)k * c->nd,
+                      dxc_sets ? dxc_sets + (size_t)(1 + k) * c->nd : nullptr));
   if (c->nd > 0) {
     k_mix_ddij<<<dim3(grid1(c->nd, 128), K), 128, 0, c->stream>>>(c->d_dij[0], c->d_dij[1], m.ddij, c->nd);
     MIX_LAUNCHED();

@@ -228,6 +228,7 @@ struct OxcTabs {
   const int64_t *doff, *soff;
   const int *dslot;        // atom of every D_ij entry
   int nchunk;              // radial chunks of the longest mesh
+  int natom, nd;
 };
 
 // index of the unordered wave pair (a, b) among the nw (nw + 1) / 2
@@ -252,13 +253,13 @@ __device__ __forceinline__ int oxc_pair(int a, int b, int nw) {
 // CTAs, and every sum runs in a fixed order.
 __global__ void __launch_bounds__(kOxcChunk) k_oxc_radial(OxcTabs T, const double *__restrict__ rho,
                                                           double *__restrict__ part) {
-  const int a = blockIdx.x, s = blockIdx.y, ch = blockIdx.z, t = threadIdx.x;
+  const int a = blockIdx.x, s = blockIdx.y & 1, set = blockIdx.y >> 1, ch = blockIdx.z, t = threadIdx.x;
   const int m = T.ms[a], nr = T.rad_n[a], nw = T.nphi[a], np = nw * (nw + 1) / 2;
   if (ch * kOxcChunk >= nr) return;
   __shared__ double C[kOxcL][kOxcMaxP];
   __shared__ double Vw[kOxcL][kOxcChunk];
   __shared__ double Us[kOxcMaxW][kOxcChunk];
-  const double *R = rho + T.doff[a];
+  const double *R = rho + (int64_t)set * T.nd + T.doff[a];
   const double *G = T.gaunt + (int64_t)kOxcL * T.doff[a];
   const int *pw = T.pwave + T.soff[a];
   for (int e = t; e < kOxcL * np; e += blockDim.x) {
@@ -317,7 +318,7 @@ __global__ void __launch_bounds__(kOxcChunk) k_oxc_radial(OxcTabs T, const doubl
 #pragma unroll
   for (int L = 0; L < kOxcL; L++) Vw[L][t] = V[L];
   __syncthreads();
-  double *out = part + (((int64_t)a * 2 + s) * T.nchunk + ch) * (kOxcL * kOxcMaxP);
+  double *out = part + ((((int64_t)set * T.natom + a) * 2 + s) * T.nchunk + ch) * (kOxcL * kOxcMaxP);
   for (int e = t; e < kOxcL * np; e += blockDim.x) {
     const int L = e / np, p = e % np;
     int wa = 0, q = p;
@@ -335,10 +336,12 @@ __global__ void __launch_bounds__(kOxcChunk) k_oxc_radial(OxcTabs T, const doubl
 // D_xc_ij = sum_L G^L_ij sum_chunks (I^L_{pw_i pw_j} - I~^L_{pw_i pw_j}): a
 // warp per entry, lanes over (L, chunk) in a fixed order (the same arithmetic
 // for ij and ji, so every block is exactly symmetric)
-__global__ void __launch_bounds__(256) k_oxc_assemble(OxcTabs T, const double *__restrict__ part, int nd,
+__global__ void __launch_bounds__(256) k_oxc_assemble(OxcTabs T, const double *__restrict__ part, int nsets,
                                                       double *__restrict__ dxc) {
-  const int e = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-  if (e >= nd) return;
+  const int64_t ea = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (ea >= (int64_t)nsets * T.nd) return;
+  const int set = (int)(ea / T.nd), e = (int)(ea - (int64_t)set * T.nd);
   const int a = T.dslot[e];
   const int m = T.ms[a], nr = T.rad_n[a], nw = T.nphi[a];
   const int loc = e - (int)T.doff[a], i = loc % m, j = loc / m;
@@ -346,7 +349,7 @@ __global__ void __launch_bounds__(256) k_oxc_assemble(OxcTabs T, const double *_
   const double *G = T.gaunt + (int64_t)kOxcL * T.doff[a];
   const int *pw = T.pwave + T.soff[a];
   const int p = oxc_pair(pw[i], pw[j], nw);
-  const double *ae = part + ((int64_t)a * 2) * T.nchunk * (kOxcL * kOxcMaxP);
+  const double *ae = part + (((int64_t)set * T.natom + a) * 2) * T.nchunk * (kOxcL * kOxcMaxP);
   const double *ps = ae + (int64_t)T.nchunk * (kOxcL * kOxcMaxP);
   double acc = 0.0;
   for (int q = lane; q < kOxcL * nch; q += 32) {
@@ -356,7 +359,7 @@ __global__ void __launch_bounds__(256) k_oxc_assemble(OxcTabs T, const double *_
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) dxc[e] = acc;
+  if (lane == 0) dxc[ea] = acc;
 }
 
 // ---- set-up: validate and upload the radial tables (ctx.cu calls this)
@@ -415,7 +418,6 @@ int onsite_init(opaw_ctx *c, const opaw_system *s) {
   OPAW_CHECK(up((void **)&c->oxc_pwave, pwave.data(), sizeof(int) * pwave.size()));
   OPAW_CHECK(up((void **)&c->oxc_gaunt, gaunt.data(), sizeof(double) * gaunt.size()));
   OPAW_CHECK(up((void **)&c->oxc_nphi, s->nphi, sizeof(int) * na));
-  OPAW_CHECK(up((void **)&c->oxc_scratch, nullptr, sizeof(double) * (size_t)na * 2 * nchunk * kOxcL * kOxcMaxP));
   c->oxc_nchunk = nchunk;
   c->oxc_on = 1;
   return OPAW_OK;
@@ -423,17 +425,23 @@ int onsite_init(opaw_ctx *c, const opaw_system *s) {
 
 void onsite_free(opaw_ctx *c) {
   void *p[] = {c->oxc_rad_n, c->oxc_roff, c->oxc_r, c->oxc_w, c->oxc_core, c->oxc_tcore, c->oxc_phioff,
-               c->oxc_phi, c->oxc_tphi, c->oxc_pwave, c->oxc_gaunt, c->oxc_scratch, c->oxc_nphi};
+               c->oxc_phi, c->oxc_tphi, c->oxc_pwave, c->oxc_gaunt, c->oxc_nphi, c->oxc_part.p};
   for (void *q : p) cudaFree(q);
+  c->oxc_part = DeviceBuf();
 }
 
-// D_xc of every atom from rho_ij (device [nd]) into dxc (device [nd])
-int onsite_xc_of(opaw_ctx *c, const double *rhoij, double *dxc) {
-  if (!c->oxc_on || c->natom == 0) return OPAW_OK;
+// D_xc of every atom for nsets consecutive rho_ij blocks (device [nsets][nd])
+// into dxc (device [nsets][nd]), on stream st
+int onsite_xc_sets(opaw_ctx *c, const double *rhoij, int nsets, double *dxc, cudaStream_t st) {
+  if (!c->oxc_on || c->natom == 0 || nsets <= 0) return OPAW_OK;
+  OPAW_CHECK(ensure(c->oxc_part,
+                    sizeof(double) * (size_t)nsets * c->natom * 2 * c->oxc_nchunk * kOxcL * kOxcMaxP));
   OxcTabs T;
   T.rad_n = c->oxc_rad_n;
   T.nphi = c->oxc_nphi;
   T.nchunk = c->oxc_nchunk;
+  T.natom = c->natom;
+  T.nd = c->nd;
   T.roff = c->oxc_roff;
   T.r = c->oxc_r;
   T.w = c->oxc_w;
@@ -448,11 +456,17 @@ int onsite_xc_of(opaw_ctx *c, const double *rhoij, double *dxc) {
   T.doff = c->d_doff;
   T.soff = c->d_soff;
   T.dslot = c->d_dslot_atom;
-  k_oxc_radial<<<dim3(c->natom, 2, c->oxc_nchunk), kOxcChunk, 0, c->stream>>>(T, rhoij, c->oxc_scratch);
-  k_oxc_assemble<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(T, c->oxc_scratch, c->nd, dxc);
+  double *part = (double *)c->oxc_part.p;
+  k_oxc_radial<<<dim3(c->natom, 2 * nsets, c->oxc_nchunk), kOxcChunk, 0, st>>>(T, rhoij, part);
+  k_oxc_assemble<<<grid1((int64_t)nsets * c->nd * 32, 256), 256, 0, st>>>(T, part, nsets, dxc);
   c->launches += 2;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
+}
+
+// D_xc of every atom from rho_ij (device [nd]) into dxc (device [nd])
+int onsite_xc_of(opaw_ctx *c, const double *rhoij, double *dxc) {
+  return onsite_xc_sets(c, rhoij, 1, dxc, c->stream);
 }
 
 }  // namespace opaw

@@ -747,17 +747,21 @@ int vxc_of(opaw_ctx *c, const double *dens, const double *core, double *out) {
   return OPAW_OK;
 }
 
-int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vxc, double *out) {
+// dxc_pre: the on-site XC term already computed for this rho_ij (the mixed
+// step computes it on the side stream), else it is computed here
+int dij_of(opaw_ctx *c, const double *rhoij, const double *vks, const double *vxc, double *out,
+           const double *dxc_pre) {
   if (c->natom == 0) return OPAW_OK;
   OPAW_CHECK(ensure(c->red, sizeof(double) * (2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1) * 2)));
   double *prod = red_scratch(c) + 2 * kRedBlocks + 64 + 64 * (size_t)(c->natom + 1);
   const int L = c->nlmmax > 0 ? c->nlmmax : 1;
   k_dhat_prod<<<c->natom, 256, 0, c->stream>>>(vks, vxc, c->d_gpt, c->d_goff, c->d_ngrid, c->d_nlm, c->d_g3off, c->d_g3d, L,
                                                 c->dv, prod);
-  OPAW_CHECK(onsite_xc_of(c, rhoij, c->oxc_dxc));
+  if (!dxc_pre) OPAW_CHECK(onsite_xc_of(c, rhoij, c->oxc_dxc));
+  const double *dxc = c->oxc_on ? (dxc_pre ? dxc_pre : c->oxc_dxc) : nullptr;
   k_dij<<<grid1((int64_t)c->nd * 32, 256), 256, 0, c->stream>>>(prod, L, rhoij, c->d_qijlm, c->d_dij0, c->d_eijkl, c->d_ms, c->d_nlm,
                                                   c->d_doff, c->d_qoff, c->d_eoff, c->d_dslot_atom, c->nd, c->dij_max,
-                                                  c->oxc_on ? c->oxc_dxc : nullptr, out);
+                                                  dxc, out);
   c->launches += 2;
   OPAW_CUDA(cudaGetLastError());
   return OPAW_OK;
