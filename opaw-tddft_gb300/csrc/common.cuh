@@ -300,6 +300,7 @@ struct opaw_ctx {
   opaw::DeviceBuf red;           // reductions
   opaw::DeviceBuf pre;           // per-orbital arguments of the preconditioners
   opaw::DeviceBuf g2part;        // segment partials of the two-table gather
+  opaw::DeviceBuf g2other;       // the unused table's sums when one table is wanted
   double *h_red = nullptr;       // pinned host mirror of small reductions
 };
 

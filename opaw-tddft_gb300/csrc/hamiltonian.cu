@@ -123,6 +123,15 @@ __global__ void __launch_bounds__(32 * kGatherWarps)
 template <typename R>
 int gather(opaw_ctx *c, int which, const typename Tr<R>::C *pin, int norb, double2 *coef) {
   if (c->natom == 0) return OPAW_OK;
+  if constexpr (sizeof(R) == 4) {
+    // complex64: the pipelined two-table pass (k_gather2) is faster than the
+    // warp-per-orbital one even with the other table's sums discarded
+    if (c->msmax <= 8) {
+      OPAW_CHECK(ensure(c->g2other, sizeof(double2) * (size_t)c->ns * norb + 16));
+      double2 *o = (double2 *)c->g2other.p;
+      return which == 0 ? gather2<R>(c, pin, norb, coef, o) : gather2<R>(c, pin, norb, o, coef);
+    }
+  }
   const R *P = ProjTab<R>::get(c, which);
   const dim3 grid(c->natom, (norb + kGatherWarps - 1) / kGatherWarps);
   if (c->msmax <= 8) {

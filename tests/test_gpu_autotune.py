@@ -44,3 +44,29 @@ def test_tuned_run_equals_untuned(kind):
     assert any(t["site"].startswith("box terms") for t in done)
     # switched off after the context's set-up: nothing decided since
     assert all(t["chosen"] < 0 for t in out[False][3])
+
+
+def test_graph_replay_equals_plain_launches():
+    """A block of steps replays a captured two-step graph; the same call with
+    kernel timing on (which issues every launch one by one) gives
+    bit-identical dipoles and orbitals, with an odd step count (the last step
+    runs plain after the replays)."""
+    s = synthetic.small_system("spec", norb=4)
+    psi = synthetic.orbitals(s, 4, seed=8).reshape(4, -1)
+    out = []
+    for block in (True, False):
+        c = pkg.Context(s)
+        c.tune_enable(False)
+        c.set_vks(0, s.vks0)
+        c.set_dij(0, s.dij_init)
+        c.upload(0, psi)
+        c.excite(1, 1e-3)
+        if not block:
+            c.ktime_begin()
+        d = c.tddft_steps(11, 0.05, 1e-3, pkg.PREC_MIXED)
+        if not block:
+            assert c.ktime_end()[1] > 0  # the dense pass ran as timed plain launches
+        out.append((d, c.download(0, 4), c.download(1, 4)))
+        c.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
