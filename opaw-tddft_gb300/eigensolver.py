@@ -13,15 +13,22 @@ preconditioned residuals, previous directions), with
 * in the complex128 phase, that preconditioner's direction K r together
   with the one corrected by the learned 3D-conv network, K r + |r| N
   (opaw_precond_learned_dev, `learned.Net`): both join the basis, so the
-  Rayleigh-Ritz step uses the network's direction as far as it helps.
+  Rayleigh-Ritz step uses the network's direction as far as it helps (or
+  the learned direction alone, with K r as the fallback when it stalls).
+  In the complex64 phase the augmented basis converges far more slowly
+  (measured: 351 instead of 79 complex64 iterations on C26H16), so the
+  network is not used there.
 
 Every operator runs in libopaw_gb300.so: S^-1/2 H S^-1/2 (opaw_shs_apply_dev),
 the Gram matrices of the Rayleigh-Ritz step (opaw_gram_herm_dev), the subspace
 rotations (opaw_rotate_dev), the preconditioners and the kinetic energies
 they scale with; the small dense eigenproblems (3m x 3m) run on the host in
 FP64.  The iteration runs in complex64 until the largest residual is below
-`switch_tol`, then in complex128 until the judge, the unpreconditioned
-eigen-residual max_i |H x_i - eps_i x_i| (dv norm), is below `tol`.
+`switch_tol` (1e-5: a complex64 iteration costs a fraction of a complex128
+one, whose Gram work is FP64), then in complex128 until the judge, the
+unpreconditioned eigen-residual max_i |H x_i - eps_i x_i| (dv norm), is
+below `tol`.  Converged columns are soft-locked: they stay in X and in the
+Rayleigh-Ritz step but add no W or P directions.
 """
 from __future__ import annotations
 
@@ -67,7 +74,7 @@ def _rr(ctx, dt, S, HS, m, drop=1e-12):
     return th[:m], B @ C[:, :m]
 
 
-def lobpcg(ctx, X0, net=None, tol=1e-8, switch_tol=1e-3, max_iter=400, record=None, record_every=4,
+def lobpcg(ctx, X0, net=None, tol=1e-8, switch_tol=1e-5, max_iter=400, record=None, record_every=4,
            verbose=False, learned_mode="augment", lock=True):
     """Lowest len(X0) eigenpairs of S^-1/2 H S^-1/2 (set 0's v_ks and D_ij)
     from the starting orbitals X0 [m, nn].  net: a trained `learned.Net`
@@ -114,7 +121,7 @@ def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbo
         X, HX, w = Xn, HXn, th
         P = HP = None
         pvalid = None
-        hist64 = []
+        hist = []  # largest residual per iteration of the phase
         fallback = False
         fresh = True  # HX is H X itself, not the rotated recurrence
         since = 0
@@ -148,12 +155,11 @@ def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbo
                 continue
             if record is not None and dt == pkg.OPAW_C128 and it % record_every == 0:
                 record.append((X.clone(), R.clone(), np.array(w, np.float64)))
-            if dt == pkg.OPAW_C128:
-                hist64.append(float(rn.max()))
-                if (net is not None and learned_mode == "replace" and not fallback and len(hist64) > 6
-                        and hist64[-1] > 0.9 * hist64[-7]):
-                    fallback = True  # the learned direction stalls: the kinetic one takes over
-                    res.fallback_iteration = it
+            hist.append(float(rn.max()))
+            if (net is not None and learned_mode == "replace" and not fallback and len(hist) > 6
+                    and hist[-1] > 0.9 * hist[-7]):
+                fallback = True  # the learned direction stalls: the kinetic one takes over
+                res.fallback_iteration = it
             # soft locking: converged columns add no directions
             ia = np.nonzero(rn >= ptol)[0] if lock else np.arange(m)
             ia_t = torch.as_tensor(ia, device="cuda")
