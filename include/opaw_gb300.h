@@ -41,8 +41,12 @@ enum opaw_status {
   OPAW_ERR_NODEV = 7      /* no CUDA device */
 };
 
-/* element type of a device orbital buffer */
-enum opaw_dtype { OPAW_C128 = 0, OPAW_C64 = 1 };
+/* element type of a device orbital buffer.  OPAW_C128_DD: complex128 data
+ * whose Gram matrices and rotations (opaw_gram_dev, opaw_gram_herm_dev,
+ * opaw_rotate_dev) are computed in double-FP32 arithmetic (hi + lo FP32
+ * pairs, about 1e-14 relative instead of FP64's 1e-16, several times faster
+ * on a GPU whose FP64 rate is 1/64 of FP32); elsewhere it is not accepted */
+enum opaw_dtype { OPAW_C128 = 0, OPAW_C64 = 1, OPAW_C128_DD = 2 };
 
 /* arithmetic of a propagation: FP64 everywhere, or FP32 FFT / v_ks /
  * projector work with FP64 RK4 accumulation, D_ij, S^-1/2 coefficients and

@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libopaw_gb300.so")
 
 OPAW_OK = 0
-OPAW_C128, OPAW_C64 = 0, 1
+OPAW_C128, OPAW_C64, OPAW_C128_DD = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 STATUS = {1: "OPAW_ERR_ARG", 2: "OPAW_ERR_CUDA", 3: "OPAW_ERR_STATE", 4: "OPAW_ERR_BOX",
           5: "OPAW_ERR_NOMEM", 6: "OPAW_ERR_NONFINITE", 7: "OPAW_ERR_NODEV"}

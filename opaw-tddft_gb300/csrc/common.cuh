@@ -301,6 +301,7 @@ struct opaw_ctx {
   opaw::DeviceBuf pre;           // per-orbital arguments of the preconditioners
   opaw::DeviceBuf g2part;        // segment partials of the two-table gather
   opaw::DeviceBuf g2other;       // the unused table's sums when one table is wanted
+  opaw::DeviceBuf ddsplit;       // hi / lo complex64 halves of complex128 operands (gram.cu)
   double *h_red = nullptr;       // pinned host mirror of small reductions
 };
 

@@ -402,6 +402,7 @@ static void destroy(opaw_ctx *c) {
   cudaFree(c->pre.p);
   cudaFree(c->g2part.p);
   cudaFree(c->g2other.p);
+  cudaFree(c->ddsplit.p);
   if (c->h_red) cudaFreeHost(c->h_red);
   fft3_free(c->fft);
   fft3_free(c->fftb);

@@ -159,6 +159,194 @@ int rotate_t(opaw_ctx *c, const typename Tr<R>::C *A, int na, const double2 *Mde
   return OPAW_OK;
 }
 
+// ---- complex128 contractions in double-FP32 arithmetic --------------------
+// GB300's FP64 rate is 1/64 of its FP32 rate, so the complex128 Gram matrices
+// and rotations of the eigensolver run on FP32 pairs: every complex128 input
+// is split once into hi + lo complex64 arrays (hi = fl32(x), lo = fl32(x -
+// hi), together ~48 significant bits), each real product is formed as
+// hi_x hi_y exactly (FMA error term) plus the two cross terms, and sums are
+// carried as an FP32 value with a compensation term (two-sum), flushed into
+// FP64 every sub-block.  Relative accuracy about 1e-14 of the sum of |terms|,
+// against 1e-16 for FP64 and 1e-7 for complex64, at about five times the
+// FP64 speed.
+
+// x -> (hi, lo) complex64
+__global__ void k_split_dd(const double2 *__restrict__ x, int64_t n, float2 *__restrict__ hi,
+                           float2 *__restrict__ lo) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double2 v = x[i];
+  const float hx = __double2float_rn(v.x), hy = __double2float_rn(v.y);
+  hi[i] = make_float2(hx, hy);
+  lo[i] = make_float2(__double2float_rn(v.x - (double)hx), __double2float_rn(v.y - (double)hy));
+}
+
+// S += (xh + xl)(yh + yl) with S = sh + sl: the product's hi part exactly
+// (ph + its FMA error), the xl yl term dropped (2^-48 relative); sh keeps
+// the running FP32 sum and sl collects the two-sum errors and the small terms
+__device__ __forceinline__ void dd_mac(float &sh, float &sl, float xh, float xl, float yh, float yl) {
+  const float ph = __fmul_rn(xh, yh);
+  float pl = __fmaf_rn(xh, yh, -ph);
+  pl = __fmaf_rn(xh, yl, pl);
+  pl = __fmaf_rn(xl, yh, pl);
+  const float s = __fadd_rn(sh, ph);
+  const float v = __fsub_rn(s, sh);
+  const float e = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, v)), __fsub_rn(ph, v));
+  sh = s;
+  sl = __fadd_rn(sl, __fadd_rn(e, pl));
+}
+
+// part[z][i][j] = sum over the z-th slice of conj(A_i) B_j, as k_gram
+__global__ void __launch_bounds__(256) k_gram_dd(const float2 *__restrict__ Ah, const float2 *__restrict__ Al,
+                                                 int na, const float2 *__restrict__ Bh,
+                                                 const float2 *__restrict__ Bl, int nb, int64_t nn,
+                                                 double2 *__restrict__ part, int herm) {
+  __shared__ float4 sa[kGramTile][kGramK + 1];
+  __shared__ float4 sb[kGramTile][kGramK + 1];
+  const int ti = threadIdx.x / kGramTile, tj = threadIdx.x % kGramTile;
+  const int i0 = blockIdx.x * kGramTile, j0 = blockIdx.y * kGramTile;
+  if (herm && i0 > j0) return;
+  const int z = blockIdx.z, nz = gridDim.z;
+  const int64_t k0 = nn * z / nz, k1 = nn * (z + 1) / nz;
+  double accx = 0, accy = 0;
+  for (int64_t kb = k0; kb < k1; kb += kGramK) {
+    for (int e = threadIdx.x; e < kGramTile * kGramK; e += 256) {
+      const int r = e / kGramK, k = e % kGramK;
+      const int64_t g = kb + k;
+      float4 va = make_float4(0.f, 0.f, 0.f, 0.f), vb = va;
+      if (g < k1) {
+        if (i0 + r < na) {
+          const int64_t o = (int64_t)(i0 + r) * nn + g;
+          const float2 h = Ah[o], l = Al[o];
+          va = make_float4(h.x, h.y, l.x, l.y);
+        }
+        if (j0 + r < nb) {
+          const int64_t o = (int64_t)(j0 + r) * nn + g;
+          const float2 h = Bh[o], l = Bl[o];
+          vb = make_float4(h.x, h.y, l.x, l.y);
+        }
+      }
+      sa[r][k] = va;
+      sb[r][k] = vb;
+    }
+    __syncthreads();
+    float xh = 0.f, xl = 0.f, yh = 0.f, yl = 0.f;
+#pragma unroll 4
+    for (int k = 0; k < kGramK; k++) {
+      const float4 a = sa[ti][k], b = sb[tj][k];
+      // conj(a) b = (ar br + ai bi) + i (ar bi - ai br)
+      dd_mac(xh, xl, a.x, a.z, b.x, b.z);
+      dd_mac(xh, xl, a.y, a.w, b.y, b.w);
+      dd_mac(yh, yl, a.x, a.z, b.y, b.w);
+      dd_mac(yh, yl, -a.y, -a.w, b.x, b.z);
+    }
+    accx += (double)xh + (double)xl;
+    accy += (double)yh + (double)yl;
+    __syncthreads();
+  }
+  const int i = i0 + ti, j = j0 + tj;
+  if (i < na && j < nb) part[((int64_t)z * na + i) * nb + j] = make_double2(accx, accy);
+}
+
+// out_j = sum_i A_i M[i + na j] (as k_rotate), complex128 output
+__global__ void __launch_bounds__(256) k_rotate_dd(const float2 *__restrict__ Ah, const float2 *__restrict__ Al,
+                                                   int na, const double2 *__restrict__ M, int nb, int64_t nn,
+                                                   double2 *__restrict__ out) {
+  __shared__ float4 sm[kGramTile][kGramTile];
+  const int64_t g = blockIdx.x * (int64_t)256 + threadIdx.x;
+  const int j0 = blockIdx.y * kGramTile;
+  float rh[kGramTile], rl[kGramTile], ih[kGramTile], il[kGramTile];
+#pragma unroll
+  for (int jj = 0; jj < kGramTile; jj++) rh[jj] = rl[jj] = ih[jj] = il[jj] = 0.f;
+  for (int i0 = 0; i0 < na; i0 += kGramTile) {
+    {
+      const int r = threadIdx.x / kGramTile, q = threadIdx.x % kGramTile;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i0 + r < na && j0 + q < nb) {
+        const double2 d = M[(i0 + r) + (int64_t)na * (j0 + q)];
+        const float hx = __double2float_rn(d.x), hy = __double2float_rn(d.y);
+        v = make_float4(hx, hy, __double2float_rn(d.x - (double)hx), __double2float_rn(d.y - (double)hy));
+      }
+      sm[r][q] = v;
+    }
+    __syncthreads();
+    if (g < nn) {
+      for (int ii = 0; ii < kGramTile && i0 + ii < na; ii++) {
+        const int64_t o = (int64_t)(i0 + ii) * nn + g;
+        const float2 ah = Ah[o], al = Al[o];
+#pragma unroll
+        for (int jj = 0; jj < kGramTile; jj++) {
+          const float4 m = sm[ii][jj];
+          // a m = (ar mr - ai mi) + i (ar mi + ai mr)
+          dd_mac(rh[jj], rl[jj], ah.x, al.x, m.x, m.z);
+          dd_mac(rh[jj], rl[jj], -ah.y, -al.y, m.y, m.w);
+          dd_mac(ih[jj], il[jj], ah.x, al.x, m.y, m.w);
+          dd_mac(ih[jj], il[jj], ah.y, al.y, m.x, m.z);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (g < nn) {
+#pragma unroll
+    for (int jj = 0; jj < kGramTile; jj++)
+      if (j0 + jj < nb)
+        out[(int64_t)(j0 + jj) * nn + g] = make_double2((double)rh[jj] + (double)rl[jj], (double)ih[jj] + (double)il[jj]);
+  }
+}
+
+// hi / lo complex64 copies of n complex128 values into c->ddsplit at
+// offset `slot` (in units of n elements of one half)
+static int split_dd(opaw_ctx *c, const double2 *x, int64_t n, float2 **hi, float2 **lo, size_t *used) {
+  const size_t need = *used + 2 * (size_t)n;
+  OPAW_CHECK(ensure(c->ddsplit, sizeof(float2) * need + 16));
+  float2 *base = (float2 *)c->ddsplit.p;
+  *hi = base + *used;
+  *lo = *hi + n;
+  *used = need;
+  k_split_dd<<<grid1(n, 256), 256, 0, c->stream>>>(x, n, *hi, *lo);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+static int gram_dd(opaw_ctx *c, const double2 *A, int na, const double2 *B, int nb, double2 *Gdev, int herm) {
+  // both splits first (ensure may move the split buffer), then the pointers
+  const int64_t nA = (int64_t)na * c->nn, nB = (int64_t)nb * c->nn;
+  const bool same = A == B && na == nb;
+  OPAW_CHECK(ensure(c->ddsplit, sizeof(float2) * 2 * (size_t)(nA + (same ? 0 : nB)) + 16));
+  size_t used = 0;
+  float2 *ah, *al, *bh, *bl;
+  OPAW_CHECK(split_dd(c, A, nA, &ah, &al, &used));
+  if (same) {
+    bh = ah;
+    bl = al;
+  } else {
+    OPAW_CHECK(split_dd(c, B, nB, &bh, &bl, &used));
+  }
+  OPAW_CHECK(ensure(c->gram, sizeof(double2) * (size_t)kGramSplit * na * nb + 16));
+  double2 *part = (double2 *)c->gram.p;
+  dim3 grid((na + kGramTile - 1) / kGramTile, (nb + kGramTile - 1) / kGramTile, kGramSplit);
+  k_gram_dd<<<grid, 256, 0, c->stream>>>(ah, al, na, bh, bl, nb, c->nn, part, herm);
+  k_gram_reduce<<<grid1((int64_t)na * nb, 128), 128, 0, c->stream>>>(part, kGramSplit, na, nb, c->dv, Gdev, herm);
+  c->launches += 2;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
+static int rotate_dd(opaw_ctx *c, const double2 *A, int na, const double2 *Mdev, int nb, double2 *out) {
+  const int64_t nA = (int64_t)na * c->nn;
+  size_t used = 0;
+  float2 *ah, *al;
+  OPAW_CHECK(ensure(c->ddsplit, sizeof(float2) * 2 * (size_t)nA + 16));
+  OPAW_CHECK(split_dd(c, A, nA, &ah, &al, &used));
+  dim3 grid(grid1(c->nn, 256), (nb + kGramTile - 1) / kGramTile);
+  k_rotate_dd<<<grid, 256, 0, c->stream>>>(ah, al, na, Mdev, nb, c->nn, out);
+  c->launches++;
+  OPAW_CUDA(cudaGetLastError());
+  return OPAW_OK;
+}
+
 // ---- FP64 orthonormalisation on the device -------------------------------
 // Cholesky of the Hermitian positive definite Gram matrix G (n x n,
 // column-major) in one CTA, G = L L^H (right-looking, a column at a time),
@@ -328,9 +516,10 @@ int opaw_gram_dev(opaw_ctx *c, int dtype, const void *A, int na, const void *B, 
   OPAW_CHECK(ensure(c->gramout, sizeof(double2) * (size_t)na * nb));
   double2 *Gd = (double2 *)c->gramout.p;
   if (dtype == OPAW_C128) OPAW_CHECK(gram_t<double>(c, (const double2 *)A, na, (const double2 *)B, nb, Gd));
+  else if (dtype == OPAW_C128_DD) OPAW_CHECK(gram_dd(c, (const double2 *)A, na, (const double2 *)B, nb, Gd, 0));
   else if (dtype == OPAW_C64) OPAW_CHECK(gram_t<float>(c, (const float2 *)A, na, (const float2 *)B, nb, Gd));
   else {
-    set_error("dtype must be OPAW_C128 or OPAW_C64");
+    set_error("dtype must be OPAW_C128, OPAW_C128_DD or OPAW_C64");
     return OPAW_ERR_ARG;
   }
   OPAW_CUDA(cudaMemcpyAsync(G, Gd, sizeof(double2) * (size_t)na * nb, cudaMemcpyDeviceToHost, c->stream));
@@ -346,6 +535,7 @@ int opaw_gram_herm_dev(opaw_ctx *c, int dtype, const void *A, const void *B, int
   OPAW_CHECK(ensure(c->gramout, sizeof(double2) * (size_t)n * n));
   double2 *Gd = (double2 *)c->gramout.p;
   if (dtype == OPAW_C128) OPAW_CHECK(gram_t<double>(c, (const double2 *)A, n, (const double2 *)B, n, Gd, 1));
+  else if (dtype == OPAW_C128_DD) OPAW_CHECK(gram_dd(c, (const double2 *)A, n, (const double2 *)B, n, Gd, 1));
   else if (dtype == OPAW_C64) OPAW_CHECK(gram_t<float>(c, (const float2 *)A, n, (const float2 *)B, n, Gd, 1));
   else {
     set_error("dtype must be OPAW_C128 or OPAW_C64");
@@ -365,6 +555,7 @@ int opaw_rotate_dev(opaw_ctx *c, int dtype, const void *A, int na, const double 
   double2 *Md = (double2 *)c->gramout.p;
   OPAW_CUDA(cudaMemcpyAsync(Md, M, sizeof(double2) * (size_t)na * nb, cudaMemcpyHostToDevice, c->stream));
   if (dtype == OPAW_C128) OPAW_CHECK(rotate_t<double>(c, (const double2 *)A, na, Md, nb, (double2 *)out));
+  else if (dtype == OPAW_C128_DD) OPAW_CHECK(rotate_dd(c, (const double2 *)A, na, Md, nb, (double2 *)out));
   else if (dtype == OPAW_C64) OPAW_CHECK(rotate_t<float>(c, (const float2 *)A, na, Md, nb, (float2 *)out));
   else {
     set_error("dtype must be OPAW_C128 or OPAW_C64");

@@ -21,7 +21,8 @@ preconditioned residuals, previous directions), with
 
 Every operator runs in libopaw_gb300.so: S^-1/2 H S^-1/2 (opaw_shs_apply_dev),
 the Gram matrices of the Rayleigh-Ritz step (opaw_gram_herm_dev), the subspace
-rotations (opaw_rotate_dev), the preconditioners and the kinetic energies
+rotations (opaw_rotate_dev) — in the complex128 phase both in double-FP32
+arithmetic (OPAW_C128_DD) — the preconditioners and the kinetic energies
 they scale with; the small dense eigenproblems (3m x 3m) run on the host in
 FP64.  The iteration runs in complex64 until the largest residual is below
 `switch_tol` (1e-5: a complex64 iteration costs a fraction of a complex128
@@ -107,17 +108,20 @@ def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbo
     it = 0
     w = None
     for dt, tdt, ptol in phases:
+        # the complex128 phase's Gram matrices and rotations in double-FP32
+        # arithmetic (~1e-14 relative; FP64 runs at 1/64 of the FP32 rate)
+        gdt = pkg.OPAW_C128_DD if dt == pkg.OPAW_C128 else dt
         X = X.to(tdt).contiguous()
         nn = X.shape[1]
         # orthonormal start of the phase, its Ritz pairs
         HX = torch.empty_like(X)
         ctx.shs_apply_dev(0, dt, X.data_ptr(), HX.data_ptr(), m)
         S0 = X
-        th, Y = _rr(ctx, dt, S0, HX, m)
+        th, Y = _rr(ctx, gdt, S0, HX, m)
         Xn = torch.empty_like(X)
-        ctx.rotate_dev(dt, X.data_ptr(), m, Y, Xn.data_ptr())
+        ctx.rotate_dev(gdt, X.data_ptr(), m, Y, Xn.data_ptr())
         HXn = torch.empty_like(X)
-        ctx.rotate_dev(dt, HX.data_ptr(), m, Y, HXn.data_ptr())
+        ctx.rotate_dev(gdt, HX.data_ptr(), m, Y, HXn.data_ptr())
         X, HX, w = Xn, HXn, th
         P = HP = None
         pvalid = None
@@ -192,20 +196,20 @@ def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbo
                     hblocks.append(HPa / pn)
             S = torch.cat(blocks)
             HS = torch.cat(hblocks)
-            th, Y = _rr(ctx, dt, S, HS, m, drop)
+            th, Y = _rr(ctx, gdt, S, HS, m, drop)
             ns = S.shape[0]
             Xn = torch.empty_like(X)
             HXn = torch.empty_like(X)
-            ctx.rotate_dev(dt, S.data_ptr(), ns, Y, Xn.data_ptr())
-            ctx.rotate_dev(dt, HS.data_ptr(), ns, Y, HXn.data_ptr())
+            ctx.rotate_dev(gdt, S.data_ptr(), ns, Y, Xn.data_ptr())
+            ctx.rotate_dev(gdt, HS.data_ptr(), ns, Y, HXn.data_ptr())
             # the new directions of the active columns: the part of their Ritz
             # vectors outside span(X)
             Ya = np.ascontiguousarray(Y[m:][:, ia])
             St, HSt = S[m:].contiguous(), HS[m:].contiguous()
             Pn_a = torch.empty_like(Ra)
             HPn_a = torch.empty_like(Ra)
-            ctx.rotate_dev(dt, St.data_ptr(), ns - m, Ya, Pn_a.data_ptr())
-            ctx.rotate_dev(dt, HSt.data_ptr(), ns - m, Ya, HPn_a.data_ptr())
+            ctx.rotate_dev(gdt, St.data_ptr(), ns - m, Ya, Pn_a.data_ptr())
+            ctx.rotate_dev(gdt, HSt.data_ptr(), ns - m, Ya, HPn_a.data_ptr())
             if len(ia) == m:
                 P, HP = Pn_a, HPn_a
             else:

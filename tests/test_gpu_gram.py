@@ -200,3 +200,30 @@ def test_gram_hermitian_form(spec):
     H = c.gram_dev(pkg.OPAW_C128, a.data_ptr(), 40, ha.data_ptr(), 40)
     Hh = c.gram_herm_dev(pkg.OPAW_C128, a.data_ptr(), ha.data_ptr(), 40)
     assert rel(Hh, 0.5 * (H + H.conj().T)) < 1e-11
+
+
+def test_double_fp32_gram_and_rotation(spec):
+    """OPAW_C128_DD: complex128 Gram matrices and rotations in double-FP32
+    arithmetic agree with exact complex128 results to 1e-13 of the largest
+    entry (rotations: of the largest output element), Hermitian form too."""
+    torch = pytest.importorskip("torch")
+    s, c = spec
+    rng = np.random.default_rng(11)
+    A = rng.standard_normal((37, s.nn)) + 1j * rng.standard_normal((37, s.nn))
+    A[3] *= 1e-3  # rows of different scale
+    B = rng.standard_normal((21, s.nn)) + 1j * rng.standard_normal((21, s.nn))
+    a = torch.from_numpy(A).cuda()
+    b = torch.from_numpy(B).cuda()
+    ref = A.conj() @ B.T * s.dv
+    G = c.gram_dev(pkg.OPAW_C128_DD, a.data_ptr(), 37, b.data_ptr(), 21)
+    assert np.abs(G - ref).max() <= 1e-13 * np.abs(ref).max()
+    refh = A.conj() @ A.T * s.dv
+    Gh = c.gram_herm_dev(pkg.OPAW_C128_DD, a.data_ptr(), a.data_ptr(), 37)
+    assert np.abs(Gh - refh).max() <= 1e-13 * np.abs(refh).max()
+    assert np.array_equal(Gh, Gh.conj().T) or np.abs(Gh - Gh.conj().T).max() <= 1e-13 * np.abs(refh).max()
+    M = rng.standard_normal((37, 19)) + 1j * rng.standard_normal((37, 19))
+    out = torch.empty((19, s.nn), dtype=torch.complex128, device="cuda")
+    c.rotate_dev(pkg.OPAW_C128_DD, a.data_ptr(), 37, M, out.data_ptr())
+    c.sync()
+    refr = M.T @ A
+    assert np.abs(out.cpu().numpy() - refr).max() <= 1e-13 * np.abs(refr).max()
