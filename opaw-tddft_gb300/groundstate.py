@@ -204,16 +204,17 @@ def _lowest_states(ctx, psi0, n_iter, degree, tol, fp64_polish, nbuf, seed, verb
     H64 = torch.empty_like(X64)
     S64 = torch.empty_like(X64)
     dt64 = pkg.OPAW_C128
-    _orthonormalise(ctx, dt64, X64, S64)
+    dtg = pkg.OPAW_C128_DD  # Gram matrices and rotations in double-FP32 arithmetic
+    _orthonormalise(ctx, dtg, X64, S64)
     _shs(ctx, dt64, X64, H64)
-    w = _rayleigh_ritz(ctx, dt64, X64, H64, S64)
+    w = _rayleigh_ritz(ctx, dtg, X64, H64, S64)
     for _ in range(fp64_polish):
         ww = torch.as_tensor(w, device="cuda", dtype=torch.float64)
         R = H64 - X64 * ww[:, None]
         X64.sub_(R / (lam_max - ww[:, None]))
-        _orthonormalise(ctx, dt64, X64, S64)
+        _orthonormalise(ctx, dtg, X64, S64)
         _shs(ctx, dt64, X64, H64)
-        w = _rayleigh_ritz(ctx, dt64, X64, H64, S64)
+        w = _rayleigh_ritz(ctx, dtg, X64, H64, S64)
     res = _residuals(X64, H64, w, dv)
     if not np.all(np.isfinite(res)):
         raise RuntimeError("ground-state iteration produced non-finite orbitals")
