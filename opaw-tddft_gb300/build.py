@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libopaw_gb300.so")
-SOURCES = ["ctx.cu", "fft.cu", "hamiltonian.cu", "rebuild.cu", "propagate.cu", "mixed.cu", "noalloc.cu", "gram.cu", "precond_net.cu", "onsite_xc.cu", "autotune.cu"]
+SOURCES = ["ctx.cu", "fft.cu", "hamiltonian.cu", "rebuild.cu", "propagate.cu", "mixed.cu", "noalloc.cu", "gram.cu", "precond_net.cu", "onsite_xc.cu", "autotune.cu", "tma.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -2,6 +2,7 @@
 // translation units of libopaw_gb300.so (the sm_103a OPAW-TDDFT path).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -302,6 +303,7 @@ struct opaw_ctx {
   opaw::DeviceBuf g2part;        // segment partials of the two-table gather
   opaw::DeviceBuf g2other;       // the unused table's sums when one table is wanted
   opaw::DeviceBuf ddsplit;       // hi / lo complex64 halves of complex128 operands (gram.cu)
+  int *d_tma_err = nullptr;      // set by a TMA-staged kernel whose barrier wait ran out
   double *h_red = nullptr;       // pinned host mirror of small reductions
 };
 
@@ -403,6 +405,12 @@ int ensemble_steps(opaw_ctx *const *cs, int n, int nsteps, double dt, double *co
 int tune_begin(opaw_ctx *c, const std::string &key, const std::vector<std::string> &labels, int dflt,
                TuneSite **timed);
 int tune_end(opaw_ctx *c, TuneSite *timed);
+// 3D tensor map of a batch of nlines x nz arrays of 8-byte elements (tma.cu)
+int tma_map_lines(CUtensorMap *m, const void *base, uint64_t nlines, uint64_t nz, uint64_t batch, uint64_t bstride,
+                  uint32_t box_lines, uint32_t box_z);
+// after a stream synchronisation: OPAW_ERR_CUDA when a TMA-staged kernel's
+// barrier wait ran out (the flag is cleared)
+int tma_status(opaw_ctx *c);
 void tune_free(opaw_ctx *c);
 // LDA potential of n points (device arrays)
 int vxc_points(opaw_ctx *c, const double *dens, double *vxc, int64_t n);

@@ -68,6 +68,8 @@ static int build(opaw_ctx *c, const opaw_system *s) {
   OPAW_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
   OPAW_CUDA(cudaEventCreateWithFlags(&c->side_fork, cudaEventDisableTiming));
   OPAW_CUDA(cudaEventCreateWithFlags(&c->side_join, cudaEventDisableTiming));
+  OPAW_CUDA(cudaMalloc(&c->d_tma_err, sizeof(int)));
+  OPAW_CUDA(cudaMemset(c->d_tma_err, 0, sizeof(int)));
   {
     int dev = 0;
     OPAW_CUDA(cudaGetDevice(&dev));
@@ -403,6 +405,7 @@ static void destroy(opaw_ctx *c) {
   cudaFree(c->g2part.p);
   cudaFree(c->g2other.p);
   cudaFree(c->ddsplit.p);
+  cudaFree(c->d_tma_err);
   if (c->h_red) cudaFreeHost(c->h_red);
   fft3_free(c->fft);
   fft3_free(c->fftb);
@@ -617,7 +620,7 @@ int opaw_ktime_end(opaw_ctx *c, double *ms, int *launches, double *bytes) {
 int opaw_sync(opaw_ctx *c) {
   OPAW_CHECK(check_ctx(c));
   OPAW_CUDA(cudaStreamSynchronize(c->stream));
-  return OPAW_OK;
+  return tma_status(c);
 }
 
 int opaw_psi_upload(opaw_ctx *c, int set, const double *psi, int norb) {

@@ -704,22 +704,138 @@ int launch_ct_tl(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, co
   return OPAW_OK;
 }
 
+// ---- z pass with the tile staged by the Tensor Memory Accelerator --------
+// The k-space-hook z pass (forward transform, kinetic factor, inverse
+// transform of 32 consecutive (x, y) lines) with its input tile brought into
+// shared memory by one cp.async.bulk.tensor load (32 lines x N planes, 8-byte
+// elements, completion on an mbarrier) instead of per-thread global loads in
+// the first stage.  The tile lands dense ([plane][line], stride 32: a warp's
+// lanes read 32 consecutive lines of one plane, so no bank conflicts) in the
+// buffer the first stage does not write; the stages and the hook are those
+// of k_fft_ct.  Lines past the end of the grid are zero-filled by the TMA
+// unit.  The wait on the barrier is bounded: after kTmaSpin polls the CTA
+// records the failure in *err and leaves.
+template <typename C, int TL> struct DenseAcc {  // [element][line] with line stride TL
+  const C *p;
+  __device__ __forceinline__ C get(int j, int l) const { return p[j * TL + l]; }
+};
+constexpr int kTmaSpin = 1 << 20;
+
+template <class Op, class = void> struct HasBufStride : std::false_type {};
+template <class Op>
+struct HasBufStride<Op, std::void_t<decltype(std::declval<Op>().buf), decltype(std::declval<Op>().bstride)>>
+    : std::true_type {};
+
+template <int N, class Op>
+__global__ void __launch_bounds__(256) k_fft_z_tma(const __grid_constant__ CUtensorMap tmap, Dims3 d,
+                                                  const float2 *__restrict__ twg, Op op, int *__restrict__ err) {
+  typedef float2 C;
+  constexpr int TL = 32, NT = 256, LS = TL + 1;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  typedef decltype(op.line(0)) L;
+  __shared__ L lvs[TL];
+  C *tw = reinterpret_cast<C *>(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  C *bufa = tw + N;
+  C *bufb = bufa + N * LS;  // 128-byte aligned: N (1 + LS) 8 bytes is a multiple of 128 for N % 16 == 0
+  const int b = blockIdx.y;
+  const int nlines = d.n0 * d.n1;
+  const int64_t base = (int64_t)blockIdx.x * TL;
+  const int nl = min(TL, nlines - (int)base);
+  const uint32_t sbar = (uint32_t)__cvta_generic_to_shared(&bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(sbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t sdst = (uint32_t)__cvta_generic_to_shared(bufb);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(sbar), "r"(TL * N * 8) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+            sdst),
+        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"((int)base), "r"(0), "r"(b), "r"(sbar)
+        : "memory");
+  }
+  // twiddles and the hook's line values while the tile is in flight
+  for (int t = threadIdx.x; t < N; t += NT) tw[t] = twg[t];
+  if (threadIdx.x < nl) lvs[threadIdx.x] = op.line(base + threadIdx.x);
+  uint32_t done = 0;
+  for (int it = 0; it < kTmaSpin && !done; it++)
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(sbar)
+        : "memory");
+  if (!done) {
+    atomicExch(err, 1);
+    return;
+  }
+  __syncthreads();  // twiddles and line values
+  MidAcc<C, TL, Op, L> mo{bufa, op, b, 1, nlines, nl, base, lvs};
+  C *res = ct_fwd_mid<C, N, TL, NT, 0>(DenseAcc<C, TL>{bufb}, bufa, bufb, tw, mo);
+  ct_inv_out<C, N, TL, NT, 0>(res, res == bufa ? bufb : bufa, tw, GlobOut<C, Op>{op, b, 1, nlines, nl, base});
+}
+
+template <int N, class Op>
+int launch_z_tma(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, const Op &op) {
+  constexpr int TL = 32;
+  CUtensorMap m;
+  OPAW_CHECK(tma_map_lines(&m, op.buf, (uint64_t)d.n0 * d.n1, (uint64_t)d.n2, (uint64_t)batch,
+                           (uint64_t)op.bstride, TL, N));
+  const int64_t tiles = ((int64_t)d.n0 * d.n1 + TL - 1) / TL;
+  const size_t smem = sizeof(float2) * ((size_t)N + 2 * (size_t)N * (TL + 1)) + 128;
+  auto kern = k_fft_z_tma<N, Op>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      set_error(std::string("fft smem attribute: ") + cudaGetErrorString(e));
+      return OPAW_ERR_CUDA;
+    }
+  }
+  kern<<<dim3((unsigned)tiles, (unsigned)batch), 256, smem, c->stream>>>(m, d, a.tw32, op, c->d_tma_err);
+  c->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error(std::string("fft z TMA launch: ") + cudaGetErrorString(e));
+    return OPAW_ERR_CUDA;
+  }
+  return OPAW_OK;
+}
+
 // z pass: the tile width (lines per CTA) is tuned between the default and
 // half of it (the lines are transformed the same way in either); the other
 // axes take the default
 template <typename C, int N, int AXIS, class Op>
 int launch_ct(opaw_ctx *c, const FFTAxis &a, Dims3 d, int batch, int sign, const Op &op, const LineSub *lsub) {
   constexpr int TL = ct_tile<C, N>();
+  // a third candidate for the complex64 k-space-hook pass over a plain batch:
+  // the tile staged by the TMA unit
+  constexpr bool kTma = AXIS == 2 && TL == 32 && sizeof(C) == 8 && Op::kMid && HasBufStride<Op>::value &&
+                        N % 16 == 0;
   if constexpr (AXIS == 2 && TL >= 16) {
-    static const std::vector<std::string> labels = {std::to_string(TL) + " lines per CTA",
-                                                    std::to_string(TL / 2) + " lines per CTA"};
+    static const std::vector<std::string> labels =
+        kTma ? std::vector<std::string>{std::to_string(TL) + " lines per CTA", std::to_string(TL / 2) + " lines per CTA",
+                                        "32 lines per CTA, tile staged by TMA"}
+             : std::vector<std::string>{std::to_string(TL) + " lines per CTA",
+                                        std::to_string(TL / 2) + " lines per CTA"};
     const std::string key = std::string("z pass ") + (sizeof(C) == 8 ? "c64" : "c128") + " n " + std::to_string(N) +
                             " lines " + std::to_string((int64_t)d.n0 * d.n1) + " batch " + std::to_string(batch) +
                             " op " + OpNameOf<Op>::get();
     TuneSite *ts = nullptr;
     const int cand = tune_begin(c, key, labels, 0, &ts);
-    const int st = cand == 1 ? launch_ct_tl<C, N, TL / 2, AXIS>(c, a, d, batch, sign, op, lsub)
-                             : launch_ct_tl<C, N, TL, AXIS>(c, a, d, batch, sign, op, lsub);
+    int st;
+    if constexpr (kTma) {
+      const bool tma_ok = !lsub && ((uintptr_t)op.buf & 15) == 0 && ((int64_t)d.n0 * d.n1) % 2 == 0 &&
+                          op.bstride % 2 == 0;
+      if (cand == 2 && tma_ok) st = launch_z_tma<N, Op>(c, a, d, batch, op);
+      else if (cand == 1) st = launch_ct_tl<C, N, TL / 2, AXIS>(c, a, d, batch, sign, op, lsub);
+      else st = launch_ct_tl<C, N, TL, AXIS>(c, a, d, batch, sign, op, lsub);
+    } else {
+      st = cand == 1 ? launch_ct_tl<C, N, TL / 2, AXIS>(c, a, d, batch, sign, op, lsub)
+                     : launch_ct_tl<C, N, TL, AXIS>(c, a, d, batch, sign, op, lsub);
+    }
     OPAW_CHECK(st);
     return tune_end(c, ts);
   } else {

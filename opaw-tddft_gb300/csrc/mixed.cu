@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(128)
 // each set run in the order of the generic kernel above.  MODE bit 0: the B
 // terms (stage), bit 1: the G terms (write_t).
 template <int MODE, int MS, int OG>
-__global__ void __launch_bounds__(kUTile, 6)
+__global__ void __launch_bounds__(kUTile, OG >= 8 ? 4 : 6)
     k_mix_boxcoef_t(int nunion, int norb, int ns, int amax, int nset, const int *__restrict__ ustart,
                     const int4 *__restrict__ uent, const int2 *__restrict__ utile, const int *__restrict__ utile_na,
                     const float *__restrict__ P0, const float *__restrict__ P1, const float4 *__restrict__ cab,
@@ -1144,7 +1144,7 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
   f.first = first;
   f.write_t = write_t;
   constexpr int MS = 8;
-  const size_t bsmem = sizeof(float4) * 3 * 4 * MS * (size_t)c->uamax;  // at the larger orbital group
+  const size_t bsmem = sizeof(float4) * 3 * 8 * MS * (size_t)c->uamax;  // at the largest orbital group
   if (c->nunion > 0 && c->ns > 0 && c->d_uent && c->msmax <= MS && bsmem <= 48 * 1024 && (stage || write_t)) {
     const int mode = (stage ? 1 : 0) | (write_t ? 2 : 0);
     // orbitals per CTA (tuned): every (union point, orbital) term is the same sum either way
@@ -1157,13 +1157,15 @@ static int mix_fused(opaw_ctx *c, Mix &m, int stage, int first, int write_t, flo
       kern<<<nb, kUTile, sm, c->stream>>>(c->nunion, m.norb, c->ns, c->uamax, m.nset, c->d_ustart, c->d_uent,
                                           c->d_utile, c->d_utile_na, c->d_p3d_f, c->d_p3d1_f, m.cab, m.cg, m.bg);
     };
-    static const std::vector<std::string> labels = {"4 orbitals per CTA", "2 orbitals per CTA"};
+    static const std::vector<std::string> labels = {"4 orbitals per CTA", "2 orbitals per CTA",
+                                                    "8 orbitals per CTA"};
     TuneSite *ts = nullptr;
     const int cand = tune_begin(c, "box terms mode " + std::to_string(mode) + " union " +
                                        std::to_string(c->nunion) + " orbitals " + std::to_string(m.norb) +
                                        " sets " + std::to_string(m.nset),
                                 labels, 0, &ts);
     if (cand == 1) launch(std::integral_constant<int, 2>());
+    else if (cand == 2) launch(std::integral_constant<int, 8>());
     else launch(std::integral_constant<int, 4>());
     MIX_LAUNCHED();
     OPAW_CHECK(tune_end(c, ts));

@@ -474,7 +474,7 @@ static int check_cs(opaw_ctx *c, int set) {
 static int finish(opaw_ctx *c) {
   OPAW_CUDA(cudaGetLastError());
   OPAW_CUDA(cudaStreamSynchronize(c->stream));
-  return OPAW_OK;
+  return tma_status(c);
 }
 
 int opaw_rhoij(opaw_ctx *c, int set, int precision) {

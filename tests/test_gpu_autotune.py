@@ -42,6 +42,11 @@ def test_tuned_run_equals_untuned(kind):
         assert len(site["ms"]) == len(site["candidates"]) and min(site["ms"]) > 0
     assert any(t["site"].startswith("dense pass") for t in done)
     assert any(t["site"].startswith("box terms") for t in done)
+    if kind == "spec":  # z = 64 has a compile-time z pass
+        # the kinetic z pass has timed its TMA-staged candidate as well (so
+        # the bitwise equality above covers it)
+        tma = [t for t in done if any("TMA" in x for x in t["candidates"])]
+        assert tma and all(len(t["ms"]) == 3 and min(t["ms"]) > 0 for t in tma), rep
     # switched off after the context's set-up: nothing decided since
     assert all(t["chosen"] < 0 for t in out[False][3])
 
