@@ -76,13 +76,16 @@ def _rr(ctx, dt, S, HS, m, drop=1e-12):
 
 
 def lobpcg(ctx, X0, net=None, tol=1e-8, switch_tol=1e-5, max_iter=400, record=None, record_every=4,
-           verbose=False, learned_mode="augment", lock=True):
+           verbose=False, learned_mode="augment", lock=True, learned_frac=1.0):
     """Lowest len(X0) eigenpairs of S^-1/2 H S^-1/2 (set 0's v_ks and D_ij)
     from the starting orbitals X0 [m, nn].  net: a trained `learned.Net`
     (None: the plain kinetic preconditioner).  learned_mode: "augment" puts
     both K r and the learned K r + |r| N in the basis; "replace" uses the
     learned direction alone, falling back to K r for the rest of the solve
     when the largest residual has not fallen by 10% over 6 iterations.
+    learned_frac: in "augment" mode the learned direction is formed only for
+    this fraction of the unconverged columns, those with the largest
+    residuals (the Rayleigh-Ritz basis grows by that many vectors).
     lock: columns whose residual is below tol contribute no W or P
     directions (soft locking; they stay in X and in the Rayleigh-Ritz step).
     record: a list that receives (X, R, eps) of every `record_every`-th
@@ -92,12 +95,14 @@ def lobpcg(ctx, X0, net=None, tol=1e-8, switch_tol=1e-5, max_iter=400, record=No
         raise ValueError("learned_mode must be 'augment' or 'replace'")
     torch = _torch()
     with torch.cuda.stream(torch.cuda.ExternalStream(ctx.stream)):
-        out = _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbose, learned_mode, lock)
+        out = _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbose, learned_mode, lock,
+                      learned_frac)
         torch.cuda.current_stream().synchronize()
     return out
 
 
-def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbose, learned_mode, lock):
+def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbose, learned_mode, lock,
+            learned_frac):
     torch = _torch()
     res = Result()
     dv = ctx.system.dv
@@ -177,8 +182,16 @@ def _lobpcg(ctx, X0, net, tol, switch_tol, max_iter, record, record_every, verbo
                 # augment: the learned direction joins the kinetic one
                 # (span[X, K r, K r + |r| N, P]), so the Rayleigh-Ritz step
                 # takes what helps; replace: the learned direction alone
-                WL = torch.empty_like(Ra)
-                net.apply(ctx, dt, Ra.data_ptr(), wa, ekin, WL.data_ptr(), len(ia))
+                if learned_mode == "augment" and learned_frac < 1.0:
+                    nb = max(1, int(np.ceil(learned_frac * len(ia))))
+                    ib = np.argsort(-rn[ia])[:nb]  # the hardest columns
+                    ib_t = torch.as_tensor(ib, device="cuda")
+                    Rb = Ra[ib_t].contiguous()
+                    WL = torch.empty_like(Rb)
+                    net.apply(ctx, dt, Rb.data_ptr(), wa[ib], np.asarray(ekin)[ib], WL.data_ptr(), nb)
+                else:
+                    WL = torch.empty_like(Ra)
+                    net.apply(ctx, dt, Ra.data_ptr(), wa, ekin, WL.data_ptr(), len(ia))
                 W = torch.cat([W, WL]) if learned_mode == "augment" else WL
             # unit columns: the residual directions shrink with convergence
             # and would otherwise fall under the Gram matrix's drop threshold
