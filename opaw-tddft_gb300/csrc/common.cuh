@@ -298,6 +298,7 @@ struct opaw_ctx {
   opaw::DeviceBuf coefr;         // single-precision copy of the scatter coefficients
   opaw::DeviceBuf gram, gramout; // Gram partials, small matrices
   opaw::DeviceBuf mix[16];       // buffers of the mixed-precision difference step
+  opaw::DeviceBuf href;          // FP64 reference source and Hartree potential of the unperturbed set
   opaw::DeviceBuf red;           // reductions
   opaw::DeviceBuf pre;           // per-orbital arguments of the preconditioners
   opaw::DeviceBuf g2part;        // segment partials of the two-table gather

@@ -405,6 +405,7 @@ static void destroy(opaw_ctx *c) {
   cudaFree(c->g2part.p);
   cudaFree(c->g2other.p);
   cudaFree(c->ddsplit.p);
+  cudaFree(c->href.p);
   cudaFree(c->d_tma_err);
   if (c->h_red) cudaFreeHost(c->h_red);
   fft3_free(c->fft);

@@ -1022,6 +1022,10 @@ struct Mix {
   float4 *cab;         // [set][orbital][slot]: (-i cD, -i c2) in FP32
   float2 *cg;          // [set][orbital][slot]: c3 in FP32
   double *r0raw, *h0raw, *drraw, *dhraw, *src, *ddens, *vh;  // src, vh: [set][point]
+  // the unperturbed set's Hartree source and potential when the call's first
+  // rebuild ran (FP64): later rebuilds transform only the change in complex64
+  double *src_ref, *vh_ref;
+  bool ref_ready = false;
   float *dvf;          // [kick][point]
   double *drhoij, *ddij, *fac, *part0, *partd, *mean, *npart0, *npart1, *nfac, *dpart, *dorb;
   float *facf;         // FP32 copy of nfac
@@ -1086,6 +1090,10 @@ static int mix_bufs(opaw_ctx *c, int norb, int nkick, Mix &m) {
   m.ddens = m.src + S * nn;
   m.vh = m.ddens + K * nn;
   m.dvf = (float *)(m.vh + S * nn);
+  OPAW_CHECK(ensure(c->href, sizeof(double) * 2 * nn + 64));
+  m.src_ref = (double *)c->href.p;
+  m.vh_ref = m.src_ref + nn;
+  m.ref_ready = false;
   const size_t nparts = K * (size_t)norb * kMixNormBlocks;
   const size_t small = 2 * K * (size_t)c->nd + 4 * K + 16 + 2 * kRedBlocks * (1 + K + S) + S + 16 +
                        4 * nparts + 3 * K * norb + 6 * nparts + 6 * K * norb + 2 * K * norb + 64;
@@ -1291,6 +1299,12 @@ static int mix_stage(opaw_ctx *c, Mix &m, int st, float w, double dts) {
 // the rest of the rebuild (ncpaw_make_hamiltonian.f90:119-129) from <p~|t>
 // and the raw densities of every set: rho_ij, n^, renormalisation, Hartree,
 // v_ks, D_ij of set 0 and of every kick, and the kicks' differences
+// x += a y over n points (FP64)
+__global__ void k_mix_axpy(double *__restrict__ x, const double *__restrict__ y, double a, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) x[i] += a * y[i];
+}
+
 static int mix_potentials(opaw_ctx *c, Mix &m) {
   const int norb = m.norb, K = m.nkick;
   const int nb = grid1(c->nn, 256);
@@ -1332,8 +1346,23 @@ static int mix_potentials(opaw_ctx *c, Mix &m) {
   // Hartree of n0 + n^0 and of every difference: one batch of complex64
   // transforms, so each difference keeps its own relative precision (packing
   // it with the ~1e3 times larger n0 into one transform would round it
-  // relative to n0)
+  // relative to n0).  The unperturbed source itself goes in as its change
+  // since the call's first rebuild, whose potential is solved once in FP64:
+  // v_H[n0] = v_H[ref] + v_H[n0 - ref].  A complex64 solve of n0 rounds
+  // relative to all of n0 (its low-k and k = 0 terms, amplified by the
+  // Martyna-Tuckerman kernel, shift every orbital's potential), and that
+  // error grows in the dipole step after step; the change since the first
+  // rebuild is orders of magnitude smaller than n0.
+  if (!m.ref_ready) {
+    OPAW_CUDA(cudaMemcpyAsync(m.src_ref, m.src, sizeof(double) * c->nn, cudaMemcpyDeviceToDevice, c->stream));
+    OPAW_CHECK(hartree_batch_t<double>(c, m.src_ref, 1, m.vh_ref));
+    m.ref_ready = true;
+  }
+  k_mix_axpy<<<nb, 256, 0, c->stream>>>(m.src, m.src_ref, -1.0, c->nn);
+  MIX_LAUNCHED();
   OPAW_CHECK(hartree_batch_t<float>(c, m.src, m.nset, m.vh));
+  k_mix_axpy<<<nb, 256, 0, c->stream>>>(m.vh, m.vh_ref, 1.0, c->nn);
+  MIX_LAUNCHED();
   const double *mean = nullptr;
   if (c->periodic) {  // tddft_pot.f90:42-45
     for (int b = 0; b < m.nset; b++)
