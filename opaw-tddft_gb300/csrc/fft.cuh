@@ -768,11 +768,11 @@ __global__ void __launch_bounds__(256) k_fft_z_tma(const __grid_constant__ CUten
         : "=r"(done)
         : "r"(sbar)
         : "memory");
-  if (!done) {
-    atomicExch(err, 1);
+  // one decision for the whole CTA (a thread that gave up leaves with all)
+  if (__syncthreads_or(!done)) {  // also orders the twiddles and line values
+    if (threadIdx.x == 0) atomicExch(err, 1);
     return;
   }
-  __syncthreads();  // twiddles and line values
   MidAcc<C, TL, Op, L> mo{bufa, op, b, 1, nlines, nl, base, lvs};
   C *res = ct_fwd_mid<C, N, TL, NT, 0>(DenseAcc<C, TL>{bufb}, bufa, bufb, tw, mo);
   ct_inv_out<C, N, TL, NT, 0>(res, res == bufa ? bufb : bufa, tw, GlobOut<C, Op>{op, b, 1, nlines, nl, base});
