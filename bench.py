@@ -708,6 +708,7 @@ def main():
     for _ in range(args.warmup):
         ctx.tddft_steps(1, DT, GAMMA, pkg.PREC_MIXED, want_dipoles=False)
     fresh()
+    ctx.tune_enable("frozen")  # no autotuner timing inside the timed region
     torch.cuda.synchronize()
     barrier(dist)
     clocks = Clocks(local)
@@ -730,6 +731,7 @@ def main():
     units = sum_over_ranks(dist, 2.0 * norb * args.steps)
     value = units / (el_max / 1e3)
 
+    ctx.tune_enable(True)
     # the roofline of the dominant kernel: a separate call of the same steps
     # with CUDA events around each of its launches (not inside the headline)
     fresh()

@@ -133,8 +133,11 @@ int opaw_ktime_end(opaw_ctx *ctx, double *ms, int *launches, double *bytes);
  * (L2 prefetch distance of the copy plane pass, lines per CTA of the z pass,
  * orbitals per CTA of the box terms, block size of the dense stage pass);
  * the context times each candidate twice on the launches it makes anyway and
- * keeps the fastest per launch shape.  On by default; off: the defaults. */
-int opaw_tune_enable(opaw_ctx *ctx, int on);
+ * keeps the fastest per launch shape.  mode 1 (the default): timing;
+ * 2: frozen, the sites decided so far keep their choice, the others take
+ * their default and nothing more is timed (for a timed region); 0: off, every
+ * site takes its default. */
+int opaw_tune_enable(opaw_ctx *ctx, int mode);
 /* the tuner's state as JSON, [{"site", "candidates", "ms", "chosen"}, ...]
  * (chosen -1: still timing); writes at most len bytes with the terminating
  * NUL, *needed = the full length + 1 */

@@ -237,8 +237,10 @@ class Context:
         _check(lib().opaw_sync(self.h))
 
     def tune_enable(self, on=True):
-        """Switches the launch-shape autotuner on (the default) or off."""
-        _check(lib().opaw_tune_enable(self.h, 1 if on else 0))
+        """Launch-shape autotuner: True (timing, the default), False (off:
+        the defaults) or "frozen" (decided sites kept, no more timing)."""
+        mode = 2 if on == "frozen" else (1 if on else 0)
+        _check(lib().opaw_tune_enable(self.h, mode))
 
     def tune_report(self):
         """The autotuner's sites: [{"site", "candidates", "ms", "chosen"}]."""

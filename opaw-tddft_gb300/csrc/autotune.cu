@@ -34,9 +34,10 @@ int tune_begin(opaw_ctx *c, const std::string &key, const std::vector<std::strin
                TuneSite **timed) {
   *timed = nullptr;
   const int n = (int)labels.size();
-  if (!c->tune_on || n <= 1) return dflt;
+  if (c->tune_on == 0 || n <= 1) return dflt;
   TuneSite *s = find_site(c, key);
   if (s && s->chosen >= 0) return s->chosen;
+  if (c->tune_on == 2) return dflt;  // frozen: no more timing
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return dflt;
   if (!s) {
@@ -93,9 +94,10 @@ void tune_free(opaw_ctx *c) {
 
 using namespace opaw;
 
-int opaw_tune_enable(opaw_ctx *c, int on) {
+int opaw_tune_enable(opaw_ctx *c, int mode) {
   OPAW_ARG(c, "null context");
-  c->tune_on = on != 0;
+  OPAW_ARG(mode >= 0 && mode <= 2, "mode must be 0 (off), 1 (on) or 2 (frozen)");
+  c->tune_on = mode;
   return OPAW_OK;
 }
 

@@ -175,7 +175,7 @@ struct opaw_ctx {
   // live timing of the fused dense pass (opaw_ktime_begin / _end)
   bool ktime_on = false;
   // autotuner state: launch site key -> site (autotune.cu)
-  bool tune_on = true;
+  int tune_on = 1;  // 1 timing, 2 frozen (decided sites kept, no timing), 0 off (defaults)
   std::deque<std::pair<std::string, opaw::TuneSite>> tune;
   std::vector<cudaEvent_t> kev;  // start/stop pairs, reused
   int kev_used = 0;
