@@ -299,6 +299,11 @@ struct opaw_ctx {
   opaw::DeviceBuf gram, gramout; // Gram partials, small matrices
   opaw::DeviceBuf mix[16];       // buffers of the mixed-precision difference step
   opaw::DeviceBuf href;          // FP64 reference source and Hartree potential of the unperturbed set
+  // generation of set 0's contents, bumped whenever they are replaced from
+  // outside the propagation (upload, orthogonalisation, device pointer handed
+  // out); the Hartree reference is reused by later mixed calls of the same
+  // generation
+  int64_t psi0_gen = 0, href_gen = -1;
   opaw::DeviceBuf red;           // reductions
   opaw::DeviceBuf pre;           // per-orbital arguments of the preconditioners
   opaw::DeviceBuf g2part;        // segment partials of the two-table gather

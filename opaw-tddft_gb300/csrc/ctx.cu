@@ -636,6 +636,7 @@ int opaw_psi_upload(opaw_ctx *c, int set, const double *psi, int norb) {
     c->norb[set] = norb;
   }
   if (set == 1) c->nkick = 1;  // one kicked set, uploaded as it is
+  if (set == 0) c->psi0_gen++;
   OPAW_CUDA(cudaMemcpyAsync(c->d_psi[set], psi, sizeof(double2) * (size_t)c->nn * norb, cudaMemcpyHostToDevice,
                             c->stream));
   OPAW_CUDA(cudaStreamSynchronize(c->stream));
@@ -657,7 +658,11 @@ int opaw_psi_download(opaw_ctx *c, int set, double *psi, int norb) {
   return OPAW_OK;
 }
 
-void *opaw_psi_device(opaw_ctx *c, int set) { return (c && (set == 0 || set == 1)) ? c->d_psi[set] : nullptr; }
+void *opaw_psi_device(opaw_ctx *c, int set) {
+  if (!c || (set != 0 && set != 1)) return nullptr;
+  if (set == 0) c->psi0_gen++;  // the caller may write through the pointer
+  return c->d_psi[set];
+}
 
 static int put(opaw_ctx *c, void *dst, const void *src, size_t bytes) {
   OPAW_ARG(src, "null input");

@@ -597,6 +597,7 @@ int opaw_orthog(opaw_ctx *c, int set, double *eig_out) {
     for (int j = 0; j < n; j++) eig_out[j] = w[j];
   OPAW_CHECK(ensure(c->work[7], sizeof(double2) * (size_t)c->nn * n));
   OPAW_CHECK(opaw_rotate_dev(c, OPAW_C128, c->d_psi[set], n, (const double *)V.data(), n, c->work[7].p));
+  if (set == 0) c->psi0_gen++;
   OPAW_CUDA(cudaMemcpyAsync(c->d_psi[set], c->work[7].p, sizeof(double2) * (size_t)c->nn * n,
                             cudaMemcpyDeviceToDevice, c->stream));
   OPAW_CUDA(cudaStreamSynchronize(c->stream));
@@ -673,6 +674,7 @@ int opaw_orthonormalize_dev(opaw_ctx *c, int set, int method, double *offdiag) {
   OPAW_CUDA(cudaGetLastError());
   OPAW_CHECK(ensure(c->work[7], sizeof(double2) * (size_t)c->nn * n));
   OPAW_CHECK(rotate_t<double>(c, c->d_psi[set], n, M, n, (double2 *)c->work[7].p));
+  if (set == 0) c->psi0_gen++;
   OPAW_CUDA(cudaMemcpyAsync(c->d_psi[set], c->work[7].p, sizeof(double2) * (size_t)c->nn * n,
                             cudaMemcpyDeviceToDevice, c->stream));
   OPAW_CUDA(cudaStreamSynchronize(c->stream));

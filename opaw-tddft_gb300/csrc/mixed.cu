@@ -1022,8 +1022,9 @@ struct Mix {
   float4 *cab;         // [set][orbital][slot]: (-i cD, -i c2) in FP32
   float2 *cg;          // [set][orbital][slot]: c3 in FP32
   double *r0raw, *h0raw, *drraw, *dhraw, *src, *ddens, *vh;  // src, vh: [set][point]
-  // the unperturbed set's Hartree source and potential when the call's first
-  // rebuild ran (FP64): later rebuilds transform only the change in complex64
+  // the unperturbed set's Hartree source and potential at the first rebuild
+  // of a mixed call since set 0 was last replaced from outside (FP64): later
+  // rebuilds transform only the change in complex64
   double *src_ref, *vh_ref;
   bool ref_ready = false;
   float *dvf;          // [kick][point]
@@ -1090,10 +1091,12 @@ static int mix_bufs(opaw_ctx *c, int norb, int nkick, Mix &m) {
   m.ddens = m.src + S * nn;
   m.vh = m.ddens + K * nn;
   m.dvf = (float *)(m.vh + S * nn);
+  const void *href_old = c->href.p;
   OPAW_CHECK(ensure(c->href, sizeof(double) * 2 * nn + 64));
+  if (c->href.p != href_old) c->href_gen = -1;  // a new buffer holds no reference
   m.src_ref = (double *)c->href.p;
   m.vh_ref = m.src_ref + nn;
-  m.ref_ready = false;
+  m.ref_ready = c->href_gen == c->psi0_gen;  // a reference of this generation of set 0 exists
   const size_t nparts = K * (size_t)norb * kMixNormBlocks;
   const size_t small = 2 * K * (size_t)c->nd + 4 * K + 16 + 2 * kRedBlocks * (1 + K + S) + S + 16 +
                        4 * nparts + 3 * K * norb + 6 * nparts + 6 * K * norb + 2 * K * norb + 64;
@@ -1347,16 +1350,18 @@ static int mix_potentials(opaw_ctx *c, Mix &m) {
   // transforms, so each difference keeps its own relative precision (packing
   // it with the ~1e3 times larger n0 into one transform would round it
   // relative to n0).  The unperturbed source itself goes in as its change
-  // since the call's first rebuild, whose potential is solved once in FP64:
+  // since a reference source (the first mixed rebuild after set 0 was last
+  // replaced from outside), whose potential is solved once in FP64:
   // v_H[n0] = v_H[ref] + v_H[n0 - ref].  A complex64 solve of n0 rounds
   // relative to all of n0 (its low-k and k = 0 terms, amplified by the
   // Martyna-Tuckerman kernel, shift every orbital's potential), and that
-  // error grows in the dipole step after step; the change since the first
-  // rebuild is orders of magnitude smaller than n0.
+  // error grows in the dipole step after step; the change since the
+  // reference is orders of magnitude smaller than n0.
   if (!m.ref_ready) {
     OPAW_CUDA(cudaMemcpyAsync(m.src_ref, m.src, sizeof(double) * c->nn, cudaMemcpyDeviceToDevice, c->stream));
     OPAW_CHECK(hartree_batch_t<double>(c, m.src_ref, 1, m.vh_ref));
     m.ref_ready = true;
+    c->href_gen = c->psi0_gen;
   }
   k_mix_axpy<<<nb, 256, 0, c->stream>>>(m.src, m.src_ref, -1.0, c->nn);
   MIX_LAUNCHED();
