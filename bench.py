@@ -357,7 +357,7 @@ def series_leg(pkg, torch, name, nsteps, precisions):
     error of the mixed d_dip(t) series against the FP64 one over all steps,
     max_t |d_mixed - d_fp64| / max_t |d_fp64|, and the first absorption peak
     of each series (spectrum.first_peak of the damped Fourier transform)."""
-    from opaw_tddft_gb300 import spectrum, synthetic
+    from opaw_tddft_gb300 import synthetic
 
     nring, n, h = synthetic.MOLECULES[name]
     s = synthetic.molecule(name)
@@ -365,12 +365,43 @@ def series_leg(pkg, torch, name, nsteps, precisions):
     t0 = time.perf_counter()
     s, psi0, res = ground_state(pkg, s, norb)
     prep = time.perf_counter() - t0
-    ctx = pkg.Context(s)
-    stream = torch.cuda.ExternalStream(ctx.stream)
     out = {"molecule": f"{name} C{4 * nring + 2}H{2 * nring + 4} (generated planar geometry, C-C 1.40 A, "
                        f"C-H 1.09 A), synthetic C/H projectors", "grid": list(n), "h": h, "orbitals_per_set": norb,
            "atoms": int(s.natom), "steps": nsteps, "dt": DT, "gamma": GAMMA, "kick": "x",
            "max_eigen_residual": res, "prep_seconds": prep}
+    return propagate_series(pkg, torch, s, psi0, norb, nsteps, precisions, out)
+
+
+def jth_series_leg(pkg, torch, nsteps, precisions):
+    """The reference's own naphthalene example: the JTH LDA datasets of C and
+    H and cnt.ini's geometry on dim_paw.inp's 56 x 52 x 32 grid (h = 0.5
+    Bohr), through the PAW set-up chain (pawsetup.py), its self-consistent
+    LDA ground state (groundstate.self_consistent_state), then the same
+    whole-series comparison as `series_leg`."""
+    from opaw_tddft_gb300 import groundstate, pawsetup
+
+    t0 = time.perf_counter()
+    s = pawsetup.from_bundle(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                                          "jth_naphthalene.npz"))
+    t_setup = time.perf_counter() - t0
+    norb = int(round(s.rnel / 2))
+    t0 = time.perf_counter()
+    s, psi0, w, res, hist = groundstate.self_consistent_state(s, norb)
+    t_scf = time.perf_counter() - t0
+    out = {"molecule": "naphthalene C10H8, the reference's example input (cnt.ini geometry, JTH LDA PAW datasets "
+                       "C.LDA_PW-JTH.xml / H.LDA_PW-JTH.xml, dim_paw.inp grid)",
+           "grid": [s.nx, s.ny, s.nz], "h": s.dx, "orbitals_per_set": norb, "atoms": int(s.natom),
+           "steps": nsteps, "dt": DT, "gamma": GAMMA, "kick": "x", "setup_seconds": t_setup,
+           "scf_iterations": len(hist), "scf_seconds": t_scf, "max_eigen_residual": res,
+           "homo_ha": float(w[-1]), "occupied_eigenvalues_ha": [round(float(x), 6) for x in w]}
+    return propagate_series(pkg, torch, s, psi0, norb, nsteps, precisions, out)
+
+
+def propagate_series(pkg, torch, s, psi0, norb, nsteps, precisions, out):
+    from opaw_tddft_gb300 import spectrum
+
+    ctx = pkg.Context(s)
+    stream = torch.cuda.ExternalStream(ctx.stream)
     series = {}
     for prec, label in precisions:
         ctx.upload(0, psi0)
@@ -807,6 +838,10 @@ def main():
         both = [(pkg.PREC_MIXED, "mixed"), (pkg.PREC_FP64, "fp64")]
         series = {"naphthalene": series_leg(pkg, torch, "naphthalene", 2000 if full else 200, both),
                   "tetracene": series_leg(pkg, torch, "tetracene", 4000 if full else 200, both)}
+        try:
+            series["naphthalene_jth"] = jth_series_leg(pkg, torch, 2000 if full else 200, both)
+        except Exception as exc:  # reported, not fatal to the headline line
+            series["naphthalene_jth"] = {"error": f"{type(exc).__name__}: {exc}"}
 
     ensemble = None
     if rank == 0 and not args.no_ensemble:

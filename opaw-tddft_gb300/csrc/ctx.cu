@@ -558,10 +558,10 @@ int opaw_dev_init(const opaw_system *sys, opaw_ctx **out) {
     }
     for (int k = 0; k < 3; k++) {
       int m = nd3[k];
-      for (int r : {2, 3, 5, 7})
+      for (int r : {2, 3, 5, 7, 11, 13})
         while (m % r == 0) m /= r;
       if (m != 1) {
-        set_error("grid extent " + std::to_string(nd3[k]) + " has a prime factor other than 2, 3, 5, 7");
+        set_error("grid extent " + std::to_string(nd3[k]) + " has a prime factor other than 2, 3, 5, 7, 11, 13");
         return OPAW_ERR_ARG;
       }
     }

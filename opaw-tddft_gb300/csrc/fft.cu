@@ -10,7 +10,7 @@ static int plan_axis(FFTAxis &a, int n) {
   a.n = n;
   a.nstage = 0;
   int m = n;
-  const int pref[] = {8, 4, 2, 3, 5, 7};
+  const int pref[] = {8, 4, 2, 3, 5, 7, 11, 13};
   for (int r : pref) {
     while (m % r == 0 && a.nstage < 16) {
       a.radix[a.nstage++] = r;
@@ -18,7 +18,7 @@ static int plan_axis(FFTAxis &a, int n) {
     }
   }
   if (m != 1) {
-    set_error("grid extent " + std::to_string(n) + " has a prime factor other than 2, 3, 5, 7");
+    set_error("grid extent " + std::to_string(n) + " has a prime factor other than 2, 3, 5, 7, 11, 13");
     return OPAW_ERR_ARG;
   }
   std::vector<double2> t64(n);

@@ -188,7 +188,7 @@ template <typename C> struct Butterfly<C, 16> {
   }
 };
 
-// generic odd radix (5, 7) from the twiddle table: y_s = sum_q u_q W_r^{qs}
+// generic odd radix (5, 7, 11, 13) from the twiddle table: y_s = sum_q u_q W_r^{qs}
 template <typename C, int R> struct Butterfly {
   static __device__ __forceinline__ void run(C *u, const C *tw, int n, int sign) {
     C y[R];
@@ -251,6 +251,8 @@ __device__ C *tile_fft(C *a, C *b, const AxisDev &ax, int TL, int ls, int js, bo
       case 4: stage<C, 4>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
       case 5: stage<C, 5>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
       case 7: stage<C, 7>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
+      case 11: stage<C, 11>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
+      case 13: stage<C, 13>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
       default: stage<C, 8>(a, b, ax.n, p, TL, ls, js, linefast, tw, sign); break;
     }
     __syncthreads();

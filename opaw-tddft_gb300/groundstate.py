@@ -299,3 +299,31 @@ def scf(ctx, psi0, max_iter=60, tol_v=1e-7, tol_res=1e-5, beta=0.3, ndiis=6, fil
         raise RuntimeError(f"SCF did not converge in {max_iter} iterations: last (max |dv|, residual) "
                            f"{hist[-1] if hist else None}")
     return w, psi, hist
+
+
+def self_consistent_state(system, norb, seed=2025, max_iter=100, tol_v=1e-6, tol_res=1e-5, polish_tol=1e-6,
+                          verbose=False):
+    """Self-consistent ground state of `system` with `norb` doubly occupied
+    orbitals, from its initial potentials (system.vks0, system.dij_init):
+    Chebyshev-filtered lowest states in that potential, the SCF loop of
+    `scf` (main.f90:67-96), the lowest states polished to `polish_tol` in the
+    last rebuilt potential, and `stationary_system` so that the rebuild of the
+    returned orbitals reproduces that potential exactly (the shifts are of
+    the size of the SCF's last potential change).  Returns (system with the
+    self-consistent v_ks and D_ij as vks0 / dij_init, orbitals complex128
+    [norb, nn], eigenvalues, max eigen-residual, SCF history)."""
+    from . import synthetic
+
+    psi0 = synthetic.orbitals(system, norb, seed=seed).reshape(norb, -1)
+    ctx = pkg.Context(system)
+    try:
+        ctx.set_vks(0, system.vks0)
+        ctx.set_dij(0, system.dij_init)
+        w, psi, res = lowest_states(ctx, psi0, n_iter=80, tol=1e-3)
+        w, psi, hist = scf(ctx, psi, max_iter=max_iter, tol_v=tol_v, tol_res=tol_res, verbose=verbose)
+        vks, dij = ctx.get_vks(0), ctx.get_dij(0)
+        w, psi, res = lowest_states(ctx, psi, n_iter=80, tol=polish_tol)
+    finally:
+        ctx.close()
+    s1 = stationary_system(dataclasses.replace(system, vks0=vks, dij_init=dij), psi)
+    return s1, psi, w, float(res.max()), hist

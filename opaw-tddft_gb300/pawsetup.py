@@ -242,20 +242,26 @@ class Species:
         return nrough
 
     def dij0(self):
-        """atompaw_dij0 (libpaw 2_m_paw_atom.F90:362-450): K_ij +
-        <phi_i|v_H(n_Zc)|phi_j> - <phi~_i|v_H(n~_Zc)|phi~_j> for channels of
-        equal (l, m); v_H(n_Zc) = -Z/r + v_H[n_c], v_H(n~_Zc) the Bloechl
-        local ionic potential."""
+        """atompaw_dij0 (libpaw 2_m_paw_atom.F90:362-518): K_ij +
+        <phi_i|v_H(n_Zc)|phi_j> - <phi~_i|v_H(n~_Zc)|phi~_j> - q_ij int
+        v_H(n~_Zc) g_0 r^2 dr for channels of equal (l, m); v_H(n_Zc) = -Z/r
+        + v_H[n_c], v_H(n~_Zc) the Bloechl local ionic potential, q_ij the
+        L = 0 moment of phi_i phi_j - phi~_i phi~_j and g_0 the shape
+        function normalised to int g_0 r^2 dr = 1 (the interaction of the
+        compensation charge with v_H(n~_Zc), :475-518)."""
         r, dr, d = self.r, self.dr, self.d
         nc = np.asarray(d["ae_core"]) / SQ4PI
         vzc = -self.Z / r + hartree_radial(nc, r, dr, 0)
         vtzc = np.asarray(d["vloc_blochl"]) / SQ4PI
+        nc_ = self.nrcomp
+        intvh = cumint(vtzc[:nc_] * self.gl[0, :nc_] * r[:nc_] ** 2, dr[:nc_])[-1]
         ns = self.lstate.size
         M = np.zeros((ns, ns))
         for i in range(ns):
             for j in range(ns):
                 f = (self.phi[i] * self.phi[j] * vzc - self.tphi[i] * self.tphi[j] * vtzc) * r * r
-                M[i, j] = cumint(f, dr)[-1]
+                q = cumint((self.phi[i] * self.phi[j] - self.tphi[i] * self.tphi[j]) * r * r, dr)[-1]
+                M[i, j] = cumint(f, dr)[-1] - intvh * q
         K = np.asarray(d["kij"])
         D = np.zeros((self.ms, self.ms))
         for p, (i, li, mi) in enumerate(self.chan):

@@ -56,7 +56,7 @@ def test_box_outside_nonperiodic_grid_is_rejected():
 
 def test_bad_grid_factor_is_rejected():
     s = synthetic.small_system("tiny", norb=2)
-    s.nx = 22  # 2 * 11
+    s.nx = 34  # 2 * 17
     status, msg = _ctx_status(s)
     assert status == 1 and "prime factor" in msg
 

@@ -194,3 +194,63 @@ def test_read_dataset_errors(tmp_path):
     bad.write_text("<not_paw/>")
     with pytest.raises(ValueError):
         pawxml.read_dataset(str(bad))
+
+
+@pytest.mark.parametrize("el", ["C", "H"])
+def test_atom_reproduces_dataset_eigenvalues(bundle, el):
+    """The whole chain against the dataset's own numbers: one atom on a 28^3
+    grid (h = 0.5 Bohr), its density built from the dataset's bound pseudo
+    partial waves with the dataset's occupations (spherical: each m of a
+    shell gets f / (2l + 1)), one rebuild (n~, n^, v_H, v_xc, D0 + E rho +
+    D_xc + Dhat through the oracle), then the lowest eigenvalues of
+    S^-1/2 H S^-1/2.  They equal the atomic eigenvalues the dataset states
+    (`e` of its bound valence states: C 2s -0.5012, 2p -0.1990; H 1s
+    -0.2335 Ha) to the grid's discretisation error."""
+    import scipy.sparse.linalg as sla
+
+    import oracle as orc
+
+    ds = bundle[0]
+    d = ds[el]
+    n, h = 28, 0.5
+    c0 = np.array([0.1, 0.05, 0.02])
+    s = pawsetup.build(ds, [el], c0[None, :], (n, n, n), (h, h, h))
+    s.rnel = float(d["valence"])
+    sp = s.extra["species"][el]
+    xs = -n * h / 2 + np.arange(n) * h
+    Z, Y, X = np.meshgrid(xs - c0[2], xs - c0[1], xs - c0[0], indexing="ij")
+    R = np.maximum(np.sqrt(X * X + Y * Y + Z * Z), 1e-8).ravel()
+    i0, w1, w2 = pawsetup.bracket(sp.r, R)
+    orbs = []
+    for i, (l, f) in enumerate(zip(d["l"], d["f"])):
+        if f <= 0:
+            continue
+        rad = d["tphi"][i][i0] * w1 + d["tphi"][i][i0 + 1] * w2
+        for m in range(-l, l + 1):
+            yl = pawsetup.ylm(l, m, X.ravel() / R, Y.ravel() / R, Z.ravel() / R)
+            orbs.append(np.sqrt(f / 2 / (2 * l + 1)) * rad * yl)
+    o = orc.Oracle(s)
+    o.set_vks(0, s.vks0)
+    o.set_dij(0, s.dij_init)
+    o.rebuild(o.sn_phi(np.array(orbs, dtype=np.complex128), 0.5), 0)
+    k = 2 * np.pi * np.fft.fftfreq(n, h)
+    K2 = (k[:, None, None] ** 2 + k[None, :, None] ** 2 + k[None, None, :] ** 2) / 2
+
+    def mv(V):
+        V = np.asarray(V).reshape(s.nn, -1)
+        return np.stack([o.shs(V[:, j].astype(np.complex128)[None, :], 0)[0].real for j in range(V.shape[1])], 1)
+
+    def pc(V):
+        V = np.asarray(V).reshape(s.nn, -1)
+        return np.stack([np.fft.ifftn(np.fft.fftn(V[:, j].reshape(n, n, n)) / (K2 + 1.0)).real.ravel()
+                         for j in range(V.shape[1])], 1)
+
+    A = sla.LinearOperator((s.nn, s.nn), matvec=mv, matmat=mv, dtype=np.float64)
+    M = sla.LinearOperator((s.nn, s.nn), matvec=pc, matmat=pc, dtype=np.float64)
+    w, _ = sla.lobpcg(A, np.random.default_rng(0).standard_normal((s.nn, 5)), M=M, largest=False,
+                      tol=1e-8, maxiter=500)
+    w = np.sort(w)
+    bound = {int(l): e for l, e, f in zip(d["l"], d["e"], d["f"]) if f > 0}
+    assert w[0] == pytest.approx(bound[0], abs=2e-3)
+    if 1 in bound:
+        assert np.abs(w[1:4] - bound[1]).max() < 3e-3
