@@ -240,7 +240,8 @@ def stationary_system(system, psi):
     return s1
 
 
-def scf(ctx, psi0, max_iter=60, tol_v=1e-7, tol_res=1e-5, beta=0.3, ndiis=6, filter_iter=2, verbose=False):
+def scf(ctx, psi0, max_iter=60, tol_v=1e-7, tol_res=1e-5, beta=0.3, ndiis=6, filter_iter=2, verbose=False,
+        filter_tol_frac=0.0):
     """Self-consistent ground state on the device, the loop of main.f90:67-96:
     each iteration rebuilds v_ks and D_ij from the current orbitals
     (ncpaw_make_hamiltonian: rho_ij, density, n^, Hartree, LDA, D_ij, all
@@ -249,6 +250,10 @@ def scf(ctx, psi0, max_iter=60, tol_v=1e-7, tol_res=1e-5, beta=0.3, ndiis=6, fil
     a history of ndiis pairs, linear mixing beta), and runs `filter_iter`
     warm-started Chebyshev filter passes with orthogonalisation and
     Rayleigh-Ritz (chebyr_m.f90, orthog_phi.f90, diag.f90) in that potential.
+    With filter_tol_frac > 0 the filter passes of an iteration stop early
+    once the largest eigen-residual is below filter_tol_frac x the last
+    max |dv_ks| (up to `filter_iter` passes): the subspace then follows the
+    potential as closely as the potential has converged.
     Stops when the largest change of v_ks is below tol_v and the largest
     eigen-residual below tol_res.  The orbitals live in set 0 of ctx; the
     input potentials of the first iteration are the ones ctx holds.  Returns
@@ -293,7 +298,8 @@ def scf(ctx, psi0, max_iter=60, tol_v=1e-7, tol_res=1e-5, beta=0.3, ndiis=6, fil
         ctx.set_vks(0, x_next[:nn])
         ctx.set_dij(0, x_next[nn:])
         x_in = x_next
-        w, psi, res = lowest_states(ctx, psi, n_iter=filter_iter, tol=0.0, fp64_polish=1,
+        ftol = max(1e-9, filter_tol_frac * dv) if filter_tol_frac > 0 else 0.0
+        w, psi, res = lowest_states(ctx, psi, n_iter=filter_iter, tol=ftol, fp64_polish=3 if ftol > 0 else 1,
                                     seed=it, verbose=False)
     else:
         raise RuntimeError(f"SCF did not converge in {max_iter} iterations: last (max |dv|, residual) "
@@ -301,7 +307,7 @@ def scf(ctx, psi0, max_iter=60, tol_v=1e-7, tol_res=1e-5, beta=0.3, ndiis=6, fil
     return w, psi, hist
 
 
-def self_consistent_state(system, norb, seed=2025, max_iter=100, tol_v=1e-6, tol_res=1e-5, polish_tol=1e-6,
+def self_consistent_state(system, norb, seed=2025, max_iter=100, tol_v=3e-6, tol_res=1e-5, polish_tol=1e-6,
                           verbose=False):
     """Self-consistent ground state of `system` with `norb` doubly occupied
     orbitals, from its initial potentials (system.vks0, system.dij_init):
@@ -320,7 +326,8 @@ def self_consistent_state(system, norb, seed=2025, max_iter=100, tol_v=1e-6, tol
         ctx.set_vks(0, system.vks0)
         ctx.set_dij(0, system.dij_init)
         w, psi, res = lowest_states(ctx, psi0, n_iter=80, tol=1e-3)
-        w, psi, hist = scf(ctx, psi, max_iter=max_iter, tol_v=tol_v, tol_res=tol_res, verbose=verbose)
+        w, psi, hist = scf(ctx, psi, max_iter=max_iter, tol_v=tol_v, tol_res=tol_res, verbose=verbose,
+                           filter_iter=16, filter_tol_frac=0.03)
         vks, dij = ctx.get_vks(0), ctx.get_dij(0)
         w, psi, res = lowest_states(ctx, psi, n_iter=80, tol=polish_tol)
     finally:
