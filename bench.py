@@ -372,24 +372,37 @@ def series_leg(pkg, torch, name, nsteps, precisions):
     return propagate_series(pkg, torch, s, psi0, norb, nsteps, precisions, out)
 
 
-def jth_series_leg(pkg, torch, nsteps, precisions):
-    """The reference's own naphthalene example: the JTH LDA datasets of C and
-    H and cnt.ini's geometry on dim_paw.inp's 56 x 52 x 32 grid (h = 0.5
-    Bohr), through the PAW set-up chain (pawsetup.py), its self-consistent
-    LDA ground state (groundstate.self_consistent_state), then the same
-    whole-series comparison as `series_leg`."""
-    from opaw_tddft_gb300 import groundstate, pawsetup
+JTH_BUNDLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "jth_naphthalene.npz")
+
+
+def jth_series_leg(pkg, torch, nsteps, precisions, name="naphthalene"):
+    """A molecule on the JTH LDA datasets of C and H through the PAW set-up
+    chain (pawsetup.py), from its self-consistent LDA ground state
+    (groundstate.self_consistent_state), then the same whole-series
+    comparison as `series_leg`.  naphthalene: the reference's own example
+    input (cnt.ini's geometry on dim_paw.inp's 56 x 52 x 32 grid, h = 0.5
+    Bohr); tetracene: the generated planar geometry on the 96 x 64 x 48 grid
+    at h = 0.45 Bohr."""
+    from opaw_tddft_gb300 import groundstate, pawsetup, pawxml, synthetic
 
     t0 = time.perf_counter()
-    s = pawsetup.from_bundle(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
-                                          "jth_naphthalene.npz"))
+    if name == "naphthalene":
+        s = pawsetup.from_bundle(JTH_BUNDLE)
+        what = ("naphthalene C10H8, the reference's example input (cnt.ini geometry, JTH LDA PAW datasets "
+                "C.LDA_PW-JTH.xml / H.LDA_PW-JTH.xml, dim_paw.inp grid)")
+    else:
+        nring, n, h = synthetic.MOLECULES[name]
+        ds = pawxml.load_bundle(JTH_BUNDLE)[0]
+        sym, xyz = synthetic.polyacene_geometry(nring)
+        s = pawsetup.build(ds, sym, xyz, n, (h, h, h))
+        what = (f"{name} C{4 * nring + 2}H{2 * nring + 4} (generated planar geometry, C-C 1.40 A, C-H 1.09 A), "
+                "JTH LDA PAW datasets of C and H")
     t_setup = time.perf_counter() - t0
     norb = int(round(s.rnel / 2))
     t0 = time.perf_counter()
     s, psi0, w, res, hist = groundstate.self_consistent_state(s, norb)
     t_scf = time.perf_counter() - t0
-    out = {"molecule": "naphthalene C10H8, the reference's example input (cnt.ini geometry, JTH LDA PAW datasets "
-                       "C.LDA_PW-JTH.xml / H.LDA_PW-JTH.xml, dim_paw.inp grid)",
+    out = {"molecule": what,
            "grid": [s.nx, s.ny, s.nz], "h": s.dx, "orbitals_per_set": norb, "atoms": int(s.natom),
            "steps": nsteps, "dt": DT, "gamma": GAMMA, "kick": "x", "setup_seconds": t_setup,
            "scf_iterations": len(hist), "scf_seconds": t_scf, "max_eigen_residual": res,
@@ -836,12 +849,14 @@ def main():
     if rank == 0 and args.series != "none":
         full = args.series == "full"
         both = [(pkg.PREC_MIXED, "mixed"), (pkg.PREC_FP64, "fp64")]
-        series = {"naphthalene": series_leg(pkg, torch, "naphthalene", 2000 if full else 200, both),
-                  "tetracene": series_leg(pkg, torch, "tetracene", 4000 if full else 200, both)}
-        try:
-            series["naphthalene_jth"] = jth_series_leg(pkg, torch, 2000 if full else 200, both)
-        except Exception as exc:  # reported, not fatal to the headline line
-            series["naphthalene_jth"] = {"error": f"{type(exc).__name__}: {exc}"}
+        # the synthetic naphthalene, then both configurations on the JTH
+        # datasets (naphthalene: the reference's own input)
+        series = {"naphthalene": series_leg(pkg, torch, "naphthalene", 2000 if full else 200, both)}
+        for mol, nst in (("naphthalene", 2000), ("tetracene", 4000)):
+            try:
+                series[f"{mol}_jth"] = jth_series_leg(pkg, torch, nst if full else 200, both, mol)
+            except Exception as exc:  # reported, not fatal to the headline line
+                series[f"{mol}_jth"] = {"error": f"{type(exc).__name__}: {exc}"}
 
     ensemble = None
     if rank == 0 and not args.no_ensemble:
