@@ -81,3 +81,50 @@ def opaw_tddft(ctx, nt, dt, gamma, workdir=".", ipol=1, psi0=None, wf_path=None,
                 restart.save(ctx, save_dir, it - 1, norb)
     d = np.concatenate(out) if out else np.zeros((0, 3))
     return istart, d
+
+
+def run_folder(folder, precision=PREC_MIXED, nt=None, block=50, n_restart=0):
+    """The reference's program on one of its input folders (main.f90 with
+    `dim_paw.inp`'s `tddft` switch): the set-up chain of the folder's
+    datasets and geometry (`pawsetup.from_folder`); for `tddft` -1 or 0 the
+    self-consistent ground state, written to wf_bar.bin or wf_bar.txt as
+    `flg_bin` says (write_wf.f90); for `tddft` 0 or 1 (1: orbitals read from
+    that file) the kick `strength` along `exct_pol` and `nt` steps of `dt`
+    (theory 3, TDDFT) in `precision`, with d_dip.dat and dip.dat written in
+    the folder (tddft_plot.f90).  Returns a dict of what ran."""
+    import opaw_tddft_gb300 as pkg
+
+    from . import groundstate, pawsetup, pawxml
+
+    params = pawxml.read_parameters(os.path.join(folder, "dim_paw.inp"))
+    mode = int(params.get("tddft", "-1"))
+    if mode not in (-1, 0, 1):
+        raise ValueError(f"tddft = {mode}: expected -1, 0 or 1")
+    if mode >= 0 and int(params.get("theory", "3")) != 3:
+        raise ValueError("only theory 3 (TDDFT with the rebuild of every stage) is on this path")
+    s = pawsetup.from_folder(folder)
+    norb = int(round(s.rnel / 2))
+    binary = params.get("flg_bin", "F").upper().startswith("T")
+    wf_path = os.path.join(folder, "wf_bar.bin" if binary else "wf_bar.txt")
+    out = {"norb": norb, "grid": (s.nx, s.ny, s.nz)}
+    psi = None
+    if mode in (-1, 0):
+        s, psi, w, res, hist = groundstate.self_consistent_state(s, norb)
+        wfio.write_wf(wf_path, psi.reshape(norb, s.nz, s.ny, s.nx), w, s.dx, s.dy, s.dz, norb, binary=binary)
+        out.update(eigenvalues=w, scf_iterations=len(hist), max_eigen_residual=res)
+        if mode == -1:
+            return out
+    else:
+        psi = orbitals_from_wf(wf_path, norb)
+    nt = int(params["nt"]) if nt is None else int(nt)
+    dt = pawxml.fortran_float(params["dt"])
+    gamma = pawxml.fortran_float(params["strength"])
+    ipol = int(params.get("exct_pol", "1"))
+    ctx = pkg.Context(s)
+    try:
+        _, d = opaw_tddft(ctx, nt, dt, gamma, workdir=folder, ipol=ipol, psi0=psi, precision=precision,
+                          block=block, n_restart=n_restart)
+    finally:
+        ctx.close()
+    out.update(d_dip=d, nt=nt, dt=dt, gamma=gamma, ipol=ipol)
+    return out

@@ -602,7 +602,22 @@ def from_bundle(path, **kw):
     periodic, finegrid, ekcut)."""
     from . import pawxml
 
-    datasets, symbols, coords, params = pawxml.load_bundle(path)
+    return from_parts(*pawxml.load_bundle(path), **kw)
+
+
+def from_folder(folder, **kw):
+    """The system of one of the reference's input folders (`pawfiles`, the
+    datasets it names, `cnt.ini`, `dim_paw.inp`)."""
+    from . import pawxml
+
+    return from_parts(*pawxml.read_folder(folder), **kw)
+
+
+def from_parts(datasets, symbols, coords, params, **kw):
+    """`build` with the grid, box, boundary, fine-grid and kinetic-cap
+    settings of `dim_paw.inp` (main.f90:326-344)."""
+    from . import pawxml
+
     n = tuple(int(params[k]) for k in ("nx", "ny", "nz"))
     box = [pawxml.fortran_float(params[k]) for k in ("box_x", "box_y", "box_z")]
     h = tuple(b / nk for b, nk in zip(box, n))  # main.f90:326-328

@@ -168,3 +168,71 @@ def load_bundle(path):
         datasets[s] = d
     params = {str(k): str(v) for k, v in zip(z["param_keys"], z["param_vals"])}
     return datasets, [str(v) for v in z["symbols"]], z["coords"], params
+
+
+def _fmt(a, per_line=3):
+    a = np.asarray(a, dtype=np.float64).reshape(-1)
+    lines = []
+    for i in range(0, a.size, per_line):
+        lines.append(" ".join(f"{v: .17e}" for v in a[i:i + per_line]))
+    return "\n".join(lines)
+
+
+def write_dataset(path, d):
+    """Writes a dataset dict (the keys `read_dataset` returns) as PAW-XML with
+    one shared radial grid; `read_dataset` reads it back bit for bit."""
+    out = ['<?xml version="1.0"?>', '<paw_dataset version="0.7">',
+           f'<atom symbol="{d["symbol"]}" Z="{d["Z"]!r}" core="{d["core"]!r}" valence="{d["valence"]!r}"/>',
+           f'<paw_radius rc="{d["rpaw"]!r}"/>', "<valence_states>"]
+    for sid, l, f, rc, e in zip(d["ids"], d["l"], d["f"], d["rc_state"], d["e"]):
+        out.append(f'  <state l="{int(l)}" f="{float(f)!r}" rc="{float(rc)!r}" e="{float(e)!r}" id="{sid}"/>')
+    out.append("</valence_states>")
+    n = len(d["r"])
+    out.append(f'<radial_grid eq="{d.get("grid_eq", "")}" istart="0" iend="{n - 1}" id="g1">')
+    out += ["  <values>", _fmt(d["r"]), "  </values>", "  <derivatives>", _fmt(d["dr"]), "  </derivatives>",
+            "</radial_grid>"]
+    out.append(f'<shape_function type="{d["shape_type"]}" rc="{d["rcomp"]!r}"/>')
+    for tag, key in _FUNCS.items():
+        out += [f'<{tag} grid="g1">', _fmt(d[key]), f"</{tag}>"]
+    for i, sid in enumerate(d["ids"]):
+        for tag, key in (("ae_partial_wave", "phi"), ("pseudo_partial_wave", "tphi"), ("projector_function", "ptilde")):
+            out += [f'<{tag} state="{sid}" grid="g1">', _fmt(d[key][i]), f"</{tag}>"]
+    out += ["<kinetic_energy_differences>", _fmt(d["kij"]), "</kinetic_energy_differences>", "</paw_dataset>"]
+    with open(path, "w") as fh:
+        fh.write("\n".join(out) + "\n")
+
+
+def read_folder(folder):
+    """The reference's input folder: `pawfiles` (element symbol and dataset
+    file per line), the datasets, `cnt.ini` and `dim_paw.inp`.  Returns
+    (datasets, symbols, coords, params) like `load_bundle`."""
+    import os
+
+    datasets = {}
+    with open(os.path.join(folder, "pawfiles")) as fh:
+        for line in fh:
+            t = line.split()
+            if len(t) >= 2:
+                datasets[t[0]] = read_dataset(os.path.join(folder, t[1]))
+    symbols, coords = read_geometry(os.path.join(folder, "cnt.ini"))
+    missing = sorted(set(symbols) - set(datasets))
+    if missing:
+        raise ValueError(f"{folder}: no dataset in pawfiles for {missing}")
+    return datasets, symbols, coords, read_parameters(os.path.join(folder, "dim_paw.inp"))
+
+
+def write_folder(folder, datasets, symbols, coords, params):
+    """Lays out an input folder as the reference reads it: one `<symbol>.xml`
+    per dataset listed in `pawfiles`, `cnt.ini` and `dim_paw.inp`."""
+    import os
+
+    with open(os.path.join(folder, "pawfiles"), "w") as fh:
+        for s, d in datasets.items():
+            write_dataset(os.path.join(folder, f"{s}.xml"), d)
+            fh.write(f"{s}     {s}.xml\n")
+    with open(os.path.join(folder, "cnt.ini"), "w") as fh:
+        for s, p in zip(symbols, coords):
+            fh.write(f" {s} {float(p[0])!r} {float(p[1])!r} {float(p[2])!r}\n")
+    with open(os.path.join(folder, "dim_paw.inp"), "w") as fh:
+        for k, v in params.items():
+            fh.write(f"{k} {v}\n")

@@ -106,3 +106,25 @@ def test_radix_11_and_13_grids(n):
         assert rel(c.download(0, 3).reshape(p1.shape), p1) < 1e-5
     finally:
         c.close()
+
+
+def test_run_folder(tmp_path):
+    """driver.run_folder on an input folder laid out like the reference's
+    (`tddft 0`: ground state, wf_bar.txt, then 12 mixed steps): the dipole
+    files and the wave-function file are written, and d_dip.dat holds the
+    (it - 1) dt stamps and the dipoles the run returned."""
+    from opaw_tddft_gb300 import dipfile, driver, pawxml, wfio
+
+    ds, sym, xyz, par = pawxml.load_bundle(BUNDLE)
+    pawxml.write_folder(str(tmp_path), ds, sym, xyz, dict(par, tddft="0", nt="12"))
+    out = driver.run_folder(str(tmp_path), precision=driver.PREC_MIXED, block=6)
+    assert out["nt"] == 12 and out["d_dip"].shape == (12, 3)
+    assert np.all(np.isfinite(out["d_dip"])) and np.abs(out["d_dip"][:, 0]).max() > 0
+    wf = wfio.read_wf(str(tmp_path / "wf_bar.txt"))
+    assert wf["nstates"] == 24
+    rows = dipfile.read_series(str(tmp_path / "d_dip.dat"))
+    assert rows.shape[0] == 12
+    # time stamps (it - 1) dt and the x component as computed
+    assert np.allclose(rows[:, 0], np.arange(12) * out["dt"])
+    assert np.allclose(rows[:, 1], out["d_dip"][:, 0], rtol=1e-7, atol=1e-12)
+    assert (tmp_path / "dip.dat").exists()

@@ -254,3 +254,21 @@ def test_atom_reproduces_dataset_eigenvalues(bundle, el):
     assert w[0] == pytest.approx(bound[0], abs=2e-3)
     if 1 in bound:
         assert np.abs(w[1:4] - bound[1]).max() < 3e-3
+
+
+def test_xml_round_trip_and_folder(bundle, naph, tmp_path):
+    """write_dataset / read_dataset return every array bit for bit, and a
+    folder laid out like the reference's input folder gives the system of
+    the bundle."""
+    ds = bundle[0]
+    for s, d in ds.items():
+        p = tmp_path / f"{s}.xml"
+        pawxml.write_dataset(str(p), d)
+        e = pawxml.read_dataset(str(p))
+        for k in ("r", "dr", "phi", "tphi", "ptilde", "kij", "ae_core", "ps_core", "vloc_blochl", "l", "f", "e"):
+            assert np.array_equal(np.asarray(e[k]), np.asarray(d[k])), (s, k)
+        assert (e["Z"], e["rpaw"], e["rcomp"], e["shape_type"]) == (d["Z"], d["rpaw"], d["rcomp"], d["shape_type"])
+    pawxml.write_folder(str(tmp_path), *bundle)
+    f = pawsetup.from_folder(str(tmp_path))
+    for k in ("p3d", "p3d1", "s", "qijlm", "g3d", "vloc", "ncoret", "dij0", "eijkl"):
+        assert np.array_equal(getattr(f, k), getattr(naph, k)), k
