@@ -432,6 +432,10 @@ def build(datasets, symbols, coords, n, h, ekcut=None, nfovnr=None, finegrid=0.1
     dx, dy, dz = (float(v) for v in h)
     coords = np.asarray(coords, dtype=np.float64)
     natom = len(symbols)
+    if periodic:
+        # the long-range -Z_val erf(r / r_g) / r part of v_loc is summed
+        # without images; a periodic box needs its lattice sum
+        raise ValueError("the set-up chain builds isolated systems (periodic F)")
     if nfovnr is None:
         nfovnr = max(1, max(math.ceil(hk / finegrid) for hk in (dx, dy, dz)))
     if ekcut is None:
