@@ -250,6 +250,8 @@ struct opaw_ctx {
   int64_t *oxc_roff = nullptr, *oxc_phioff = nullptr;
   double *oxc_r = nullptr, *oxc_w = nullptr, *oxc_core = nullptr, *oxc_tcore = nullptr;
   double *oxc_phi = nullptr, *oxc_tphi = nullptr, *oxc_gaunt = nullptr;
+  short *oxc_live = nullptr;  // per atom: (L, pair) entries with non-zero Gaunt coefficients
+  int *oxc_nlive = nullptr;
   opaw::DeviceBuf oxc_part;  // partial radial integrals [set][atom][part][chunk][L][pair]
   opaw::DeviceBuf oxc_sets;  // D_xc of the unperturbed and every kicked set (mixed step)
   // a second stream of the context: the on-site XC term of the mixed step

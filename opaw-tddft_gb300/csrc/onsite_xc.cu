@@ -215,6 +215,7 @@ __device__ __forceinline__ Ts oxc_vxc_series(double n0) {
 constexpr int kOxcMaxW = 6;                          // partial waves per atom
 constexpr int kOxcMaxP = kOxcMaxW * (kOxcMaxW + 1) / 2;  // unordered wave pairs
 constexpr int kOxcChunk = 64;                        // radial points per CTA
+constexpr int kOxcLiveMax = kOxcL * kOxcMaxP;        // (L, pair) entries of one atom
 
 struct OxcTabs {
   const int *rad_n, *nphi;
@@ -227,6 +228,9 @@ struct OxcTabs {
   const int *ms;
   const int64_t *doff, *soff;
   const int *dslot;        // atom of every D_ij entry
+  const short *live;       // per atom [kOxcLiveMax]: the (L, pair) entries L np + p with a
+                           // non-zero Gaunt coefficient, ascending
+  const int *nlive;        // per atom: their count
   int nchunk;              // radial chunks of the longest mesh
   int natom, nd;
 };
@@ -250,7 +254,11 @@ __device__ __forceinline__ int oxc_pair(int a, int b, int nw) {
 // C^L_ab = sum_{ij: {pw_i, pw_j} = {a, b}} rho_ij G^L_ij: the moments and the
 // integrals run over wave pairs (at most 21) instead of projector pairs
 // (64 for 8 projectors), the FP64 work is spread over (atom, part, chunk)
-// CTAs, and every sum runs in a fixed order.
+// CTAs, and every sum runs in a fixed order.  Only the (L, pair) entries
+// whose Gaunt coefficients are not all zero are formed (33 of 90 for two s
+// and two p waves: s s pairs have L = 0 only, s p pairs l = 1, p p pairs
+// L = 0 and l = 2); the others are exact zeros, so D_xc is the same bit for
+// bit with fewer FP64 operations.
 __global__ void __launch_bounds__(kOxcChunk) k_oxc_radial(OxcTabs T, const double *__restrict__ rho,
                                                           double *__restrict__ part) {
   const int a = blockIdx.x, s = blockIdx.y & 1, set = blockIdx.y >> 1, ch = blockIdx.z, t = threadIdx.x;
@@ -262,8 +270,12 @@ __global__ void __launch_bounds__(kOxcChunk) k_oxc_radial(OxcTabs T, const doubl
   const double *R = rho + (int64_t)set * T.nd + T.doff[a];
   const double *G = T.gaunt + (int64_t)kOxcL * T.doff[a];
   const int *pw = T.pwave + T.soff[a];
-  for (int e = t; e < kOxcL * np; e += blockDim.x) {
-    const int L = e / np, p = e % np;
+  const short *lv = T.live + (int64_t)a * kOxcLiveMax;
+  const int nl = T.nlive[a];
+  for (int e = t; e < kOxcL * np; e += blockDim.x) C[e / np][e % np] = 0.0;
+  __syncthreads();
+  for (int q = t; q < nl; q += blockDim.x) {
+    const int e = lv[q], L = e / np, p = e % np;
     double acc = 0.0;
     for (int j = 0; j < m; j++)
       for (int i = 0; i < m; i++)
@@ -319,8 +331,10 @@ __global__ void __launch_bounds__(kOxcChunk) k_oxc_radial(OxcTabs T, const doubl
   for (int L = 0; L < kOxcL; L++) Vw[L][t] = V[L];
   __syncthreads();
   double *out = part + ((((int64_t)set * T.natom + a) * 2 + s) * T.nchunk + ch) * (kOxcL * kOxcMaxP);
-  for (int e = t; e < kOxcL * np; e += blockDim.x) {
-    const int L = e / np, p = e % np;
+  for (int e = t; e < kOxcL * np; e += blockDim.x) out[(e / np) * kOxcMaxP + e % np] = 0.0;
+  __syncthreads();
+  for (int li = t; li < nl; li += blockDim.x) {
+    const int e = lv[li], L = e / np, p = e % np;
     int wa = 0, q = p;
     while (q >= nw - wa) {
       q -= nw - wa;
@@ -399,6 +413,27 @@ int onsite_init(opaw_ctx *c, const opaw_system *s) {
           gaunt[(size_t)kOxcL * c->h_doff[a] + (L * m + i) * m + j] = gl[(L * 4 + ai) * 4 + aj];
         }
   }
+  // the (L, pair) entries with a non-zero Gaunt coefficient, per atom
+  std::vector<short> live((size_t)kOxcLiveMax * (na > 0 ? na : 1), 0);
+  std::vector<int> nlive(na > 0 ? na : 1, 0);
+  for (int a = 0; a < na; a++) {
+    const int m = c->h_ms[a], nw = s->nphi[a], np = nw * (nw + 1) / 2;
+    for (int L = 0; L < kOxcL; L++)
+      for (int p = 0; p < np; p++) {
+        bool any = false;
+        for (int j = 0; j < m && !any; j++)
+          for (int i = 0; i < m; i++) {
+            int wa = pwave[c->h_soff[a] + i], wb = pwave[c->h_soff[a] + j];
+            if (wa > wb) std::swap(wa, wb);
+            const int pp = wa * nw - wa * (wa - 1) / 2 + (wb - wa);
+            if (pp == p && gaunt[(size_t)kOxcL * c->h_doff[a] + (L * m + i) * m + j] != 0.0) {
+              any = true;
+              break;
+            }
+          }
+        if (any) live[(size_t)kOxcLiveMax * a + nlive[a]++] = (short)(L * np + p);
+      }
+  }
   for (int64_t k = 0; k < roff[na]; k++) OPAW_ARG(s->rad_r[k] > 0.0, "on-site XC: radii must be > 0");
   auto up = [&](void **dst, const void *src, size_t bytes) -> int {
     OPAW_CUDA(cudaMalloc(dst, bytes > 0 ? bytes : 8));
@@ -418,6 +453,8 @@ int onsite_init(opaw_ctx *c, const opaw_system *s) {
   OPAW_CHECK(up((void **)&c->oxc_pwave, pwave.data(), sizeof(int) * pwave.size()));
   OPAW_CHECK(up((void **)&c->oxc_gaunt, gaunt.data(), sizeof(double) * gaunt.size()));
   OPAW_CHECK(up((void **)&c->oxc_nphi, s->nphi, sizeof(int) * na));
+  OPAW_CHECK(up((void **)&c->oxc_live, live.data(), sizeof(short) * live.size()));
+  OPAW_CHECK(up((void **)&c->oxc_nlive, nlive.data(), sizeof(int) * nlive.size()));
   c->oxc_nchunk = nchunk;
   c->oxc_on = 1;
   return OPAW_OK;
@@ -425,7 +462,8 @@ int onsite_init(opaw_ctx *c, const opaw_system *s) {
 
 void onsite_free(opaw_ctx *c) {
   void *p[] = {c->oxc_rad_n, c->oxc_roff, c->oxc_r, c->oxc_w, c->oxc_core, c->oxc_tcore, c->oxc_phioff,
-               c->oxc_phi, c->oxc_tphi, c->oxc_pwave, c->oxc_gaunt, c->oxc_nphi, c->oxc_part.p};
+               c->oxc_phi, c->oxc_tphi, c->oxc_pwave, c->oxc_gaunt, c->oxc_nphi, c->oxc_part.p,
+               c->oxc_live, c->oxc_nlive};
   for (void *q : p) cudaFree(q);
   c->oxc_part = DeviceBuf();
 }
@@ -456,6 +494,8 @@ int onsite_xc_sets(opaw_ctx *c, const double *rhoij, int nsets, double *dxc, cud
   T.doff = c->d_doff;
   T.soff = c->d_soff;
   T.dslot = c->d_dslot_atom;
+  T.live = c->oxc_live;
+  T.nlive = c->oxc_nlive;
   double *part = (double *)c->oxc_part.p;
   k_oxc_radial<<<dim3(c->natom, 2 * nsets, c->oxc_nchunk), kOxcChunk, 0, st>>>(T, rhoij, part);
   k_oxc_assemble<<<grid1((int64_t)nsets * c->nd * 32, 256), 256, 0, st>>>(T, part, nsets, dxc);
