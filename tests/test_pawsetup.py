@@ -272,3 +272,15 @@ def test_xml_round_trip_and_folder(bundle, naph, tmp_path):
     f = pawsetup.from_folder(str(tmp_path))
     for k in ("p3d", "p3d1", "s", "qijlm", "g3d", "vloc", "ncoret", "dij0", "eijkl"):
         assert np.array_equal(getattr(f, k), getattr(naph, k)), k
+
+
+def test_folder_errors(bundle, tmp_path):
+    """A geometry atom without a dataset in pawfiles, and a periodic box, are
+    refused before any table is built."""
+    ds, sym, xyz, par = bundle
+    only_c = {"C": ds["C"]}
+    pawxml.write_folder(str(tmp_path), only_c, sym, xyz, par)
+    with pytest.raises(ValueError, match="no dataset"):
+        pawxml.read_folder(str(tmp_path))
+    with pytest.raises(ValueError, match="isolated"):
+        pawsetup.build(ds, sym, xyz, (56, 52, 32), (0.5, 0.5, 0.5), periodic=1)
