@@ -132,9 +132,9 @@ def hartree_radial(n, r, dr, L):
 
 class Species:
     """Per-element tables of readpaw (read_paw.f90), transform_pphi and libpaw's
-    pawinit for one dataset at grid spacings h = (dx, dy, dz)."""
+    pawinit for one dataset (they do not depend on the grid)."""
 
-    def __init__(self, d, h, nfovnr):
+    def __init__(self, d):
         self.d = d
         self.symbol = d["symbol"]
         self.Z, self.zval = float(d["Z"]), float(d["valence"])
@@ -236,8 +236,7 @@ class Species:
         self.qijlm = Q
 
     def box(self, h):
-        """nrough (get_nrcut, read_paw.f90:247-250) and the spline transfer
-        matrices b[rough, fine] (get_b, read_paw.f90:274-345)."""
+        """nrough per axis for spacings h (get_nrcut, read_paw.f90:247-250)."""
         nrough = [2 * (math.ceil((self.rcut + RPAD) / hk) + 1) for hk in h]
         return nrough
 
@@ -441,7 +440,7 @@ def build(datasets, symbols, coords, n, h, ekcut=None, nfovnr=None, finegrid=0.1
     if ekcut is None:
         ekcut = synthetic.reference_ekcut((nx, ny, nz), (dx, dy, dz))
     half = np.array([nx * dx, ny * dy, nz * dz]) / 2.0
-    species = {s: Species(datasets[s], (dx, dy, dz), nfovnr) for s in sorted(set(symbols))}
+    species = {s: Species(datasets[s]) for s in sorted(set(symbols))}
     for s, sp in species.items():
         if np.any(sp.rcut > half):
             raise ValueError(f"{s}: rcut larger than half the box (get_rcut, read_paw.f90:213-226)")
