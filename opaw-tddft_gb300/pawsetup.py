@@ -10,7 +10,7 @@ This is the host-side chain the reference runs once before the propagation
   :146-190: O^-1/2 on the projectors, O^1/2 on the partial waves, then the
   eigenvectors of O^1/2 (phi^2 - phi~^2) O^1/2), the channel layout (state,
   m) (get_nm, :429-480), the compensation shape functions g_l normalised to
-  sum r^(l+2) g_l dr = 1 (get_gl, :112-182; the `sinc` form), the moments
+  sum r^(l+2) g_l dr = 1 (get_gl, :112-182; the `sinc` and `bessel` forms), the moments
   Q_ij^LM = n_ij^L G^LM_ij and the diagonal overlap s_ij from the
   orthogonalised waves (calc_qijlm, :695-782), the box size nrough (get_nrcut,
   :229-272) and the natural-cubic-spline transfer matrices from the fine
@@ -128,6 +128,35 @@ def hartree_radial(n, r, dr, L):
     return 4.0 * math.pi / (2 * L + 1) * (inner / r ** (L + 1) + outer * r ** L)
 
 
+def _sph_jn(l, x, derivative=False):
+    from scipy.special import spherical_jn
+
+    return spherical_jn(l, x, derivative=derivative)
+
+
+def _bessel_shape(l, rc):
+    """atompaw_shapebes: q_1, q_2 = the first two positive zeros of j_l over
+    rc, and (a_1, a_2) with sum a_i q_i j_l'(q_i rc) = 0 and sum a_i
+    rc^(l+2) j_(l+1)(q_i rc) / q_i = 1 (the moment int_0^rc j_l(q r)
+    r^(l+2) dr)."""
+    from scipy.optimize import brentq
+
+    roots = []
+    x = 1e-3
+    f0 = _sph_jn(l, x)
+    while len(roots) < 2:
+        x1 = x + 0.05
+        f1 = _sph_jn(l, x1)
+        if f0 * f1 < 0:
+            roots.append(brentq(lambda t: _sph_jn(l, t), x, x1, xtol=1e-15))
+        x, f0 = x1, f1
+    q = np.array(roots) / rc
+    A = np.array([[q[i] * _sph_jn(l, q[i] * rc, derivative=True) for i in range(2)],
+                  [rc ** (l + 2) * _sph_jn(l + 1, q[i] * rc) / q[i] for i in range(2)]])
+    a = np.linalg.solve(A, np.array([0.0, 1.0]))
+    return a, q
+
+
 # ---------------------------------------------------------------- species
 
 class Species:
@@ -191,17 +220,27 @@ class Species:
         self._moments()
 
     def _shape_functions(self):
-        """get_gl (read_paw.f90:112-182), `sinc` form."""
+        """get_gl (read_paw.f90:112-182): the `sinc` form (sin(x)/x)^2 r^l,
+        x = pi r / rc, and the `bessel` form a_1 j_l(q_1 r) + a_2 j_l(q_2 r)
+        (libpaw atompaw_shapebes, 2_m_paw_atom.F90:211-256: q_i rc the first
+        two zeros of j_l, a_i from a zero derivative at rc and unit
+        moment), each then normalised to sum r^(l+2) g_l dr = 1."""
         d, r, dr = self.d, self.r, self.dr
-        if d["shape_type"] != "sinc":
-            raise ValueError(f"{self.symbol}: shape function {d['shape_type']!r} not supported (sinc only)")
+        kind = d["shape_type"]
+        if kind not in ("sinc", "bessel"):
+            raise ValueError(f"{self.symbol}: shape function {kind!r} not supported (sinc, bessel)")
         nc = upper_count(r, self.rcomp)
         self.nrcomp = nc
         gl = np.zeros((self.nL, r.size))
-        arg = math.pi * r[1:nc] / self.rcomp
+        rc = self.rcomp
         for L in range(self.nL):
-            gl[L, 0] = 1.0 if L == 0 else 0.0
-            gl[L, 1:nc] = (np.sin(arg) / arg) ** 2 * r[1:nc] ** L
+            if kind == "sinc":
+                arg = math.pi * r[1:nc] / rc
+                gl[L, 0] = 1.0 if L == 0 else 0.0
+                gl[L, 1:nc] = (np.sin(arg) / arg) ** 2 * r[1:nc] ** L
+            else:
+                a, q = _bessel_shape(L, rc)
+                gl[L, :nc] = a[0] * _sph_jn(L, q[0] * r[:nc]) + a[1] * _sph_jn(L, q[1] * r[:nc])
             gl[L] /= np.sum(r[:nc] ** (L + 2) * dr[:nc] * gl[L, :nc])
         self.gl = gl
 
