@@ -312,3 +312,19 @@ def test_bessel_shape_functions(bundle):
     wb = _atom_levels(ds, "C")
     ws = _atom_levels(bundle[0], "C")
     assert np.abs(wb[:4] - ws[:4]).max() < 1e-3
+
+
+def test_run_folder_refuses_other_modes(bundle, tmp_path):
+    """driver.run_folder checks dim_paw.inp's switches before it builds
+    anything: tddft must be -1, 0 or 1, and a propagation needs theory 3
+    (the other theories are not on this path)."""
+    from opaw_tddft_gb300 import driver
+
+    ds, sym, xyz, par = bundle
+    pawxml.write_folder(str(tmp_path), ds, sym, xyz, dict(par, tddft="2"))
+    with pytest.raises(ValueError, match="tddft"):
+        driver.run_folder(str(tmp_path))
+    pawxml.write_folder(str(tmp_path), ds, sym, xyz, dict(par, tddft="0", theory="2"))
+    with pytest.raises(ValueError, match="theory 3"):
+        driver.run_folder(str(tmp_path))
+    assert pawxml.fortran_float("-1d0") == -1.0 and pawxml.fortran_float("1e-3") == 1e-3
