@@ -707,6 +707,8 @@ def main():
     ap.add_argument("--no-roofline", action="store_true", help="skip the standalone FFT timing")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched kicks x molecules leg")
     ap.add_argument("--no-precond", action="store_true", help="skip the learned-preconditioner eigensolver leg")
+    ap.add_argument("--synthetic-series", action="store_true",
+                    help="also run the whole-propagation legs on the synthetic stand-ins of the two molecules")
     ap.add_argument("--series", default="full", choices=["full", "short", "none"],
                     help="whole-propagation legs: naphthalene 2000 steps and tetracene 4000 steps in FP64 and mixed "
                          "precision (full), 200 steps each (short), or none")
@@ -850,8 +852,11 @@ def main():
         full = args.series == "full"
         both = [(pkg.PREC_MIXED, "mixed"), (pkg.PREC_FP64, "fp64")]
         # both configurations on the JTH datasets (naphthalene: the
-        # reference's own input); `series_leg` runs the synthetic stand-ins
+        # reference's own input); the synthetic stand-ins on request
         series = {}
+        if args.synthetic_series:
+            for mol, nst in (("naphthalene", 2000), ("tetracene", 4000)):
+                series[mol] = series_leg(pkg, torch, mol, nst if full else 200, both)
         for mol, nst in (("naphthalene", 2000), ("tetracene", 4000)):
             try:
                 series[f"{mol}_jth"] = jth_series_leg(pkg, torch, nst if full else 200, both, mol)
