@@ -254,3 +254,35 @@ def test_tddft_steps_deterministic(tiny):
     a = o.tddft_steps(psi, pp, 2, 0.05, 1e-3)
     b = o.tddft_steps(psi, pp, 2, 0.05, 1e-3)
     assert np.array_equal(a[2], b[2]) and np.array_equal(a[0], b[0])
+
+
+def test_vxc_against_the_reference_in_tree_lda():
+    """The reference's own LDA (the routines libxc replaced in it):
+    get_vx_lda and get_vcn_spn_lda (exchange_corr_lda_spn.f90:1-30, nspn =
+    1: a forward difference of n e_c with dn = 1e-5 n) over ec_pw
+    (lib/library_exc_lda_9.f90:513-560, Perdew-Wang 1992 with its Table I
+    parameters; at zero polarisation only the first column enters) agree
+    with the oracle's analytic v_xc to the forward difference's error."""
+    pi = math.pi
+
+    def gf(rs, A, a1, b1, b2, b3, b4):  # PW92 eq. 10, p = 1
+        return -2.0 * A * (1.0 + a1 * rs) * math.log(
+            1.0 + 1.0 / (2.0 * A * (b1 * rs ** 0.5 + b2 * rs + b3 * rs ** 1.5 + b4 * rs ** 2)))
+
+    def ec_pw(nup, ndn):
+        rs = (3.0 / (4.0 * pi * (nup + ndn))) ** (1.0 / 3.0)
+        return gf(rs, 0.031091, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294)
+
+    def v_ref(n):
+        vx = -0.738558766382022046 * 4.0 / 3.0 * max(n, 1e-20) ** (1.0 / 3.0)
+        n1 = max(1e-20, n / 2.0)
+        nnn = 2.0 * n1
+        e0 = ec_pw(n1, n1)
+        dn = 1e-5 * nnn
+        de1 = (ec_pw(n1 + dn / 2.0, n1 + dn / 2.0) - e0) / dn
+        return vx + e0 + nnn * de1
+
+    ns = np.array([1e-5, 1e-3, 1e-2, 0.1, 0.5, 2.0])
+    v = orc.vxc(ns)
+    for n, vv in zip(ns, v):
+        assert abs(vv - v_ref(n)) < 2e-6 * abs(vv), (n, vv, v_ref(n))
